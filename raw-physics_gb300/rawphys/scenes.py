@@ -1,0 +1,340 @@
+"""Seeded synthetic scenes for raw-physics' rigid-body step.
+
+A Scene is backend-neutral: meshes (the OBJ-loader form of rawphys.meshes), per-body colliders,
+poses, masses, material coefficients, initial velocities and external constraints, plus the
+per-frame call parameters of pbd_simulate (dt, substeps, position iterations, collisions) and the
+gravity the caller applies as a force -g/inverse_mass (src/examples/stack.cpp:93-96).
+
+Workloads (all seeded; none is a published dataset):
+  stack_scene        10 unit cubes on a fixed 40x40 m floor, xz jitter U(-0.02, 0.02) m,
+                     dt=1/60, 20 substeps, 1 iteration, friction 0.5/0.3, restitution 0
+  large_scene        4096 bodies drawn uniformly from {cube, icosahedron, 32-segment cylinder,
+                     42-vertex icosphere}, uniform scale U(0.5, 1.5), density 1, uniform random
+                     orientation (Shoemake), v ~ N(0, 1) m/s, inside a fixed floor + 4 walls box
+                     of 40x40x60 m; positions uniform in the box, rejection-sampled so no two
+                     bounding spheres overlap at t=0
+  tower_scene        a tower of unit cubes with alternating mass ratio
+  chain_scene        cube links joined by hinge or spherical joints
+  domino_scene       a row of 0.2x1x2 m dominoes and a thrown cube
+  random_pile_scene  small mixed-shape piles for parity tests
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import meshes as M
+
+# PBD_Axis_Type (src/physics/pbd.h:5-12)
+POS_X, NEG_X, POS_Y, NEG_Y, POS_Z, NEG_Z = range(6)
+
+
+@dataclass
+class Collider:
+    kind: str                    # "hull" or "sphere"
+    mesh: int = -1               # index into Scene.meshes for hulls
+    scale: tuple = (1.0, 1.0, 1.0)
+    radius: float = 0.0          # spheres (stored as float32 by the reference)
+
+
+@dataclass
+class Constraint:
+    kind: str                    # "positional" | "mutual_orientation" | "hinge" | "spherical"
+    e1: int
+    e2: int
+    r1: tuple = (0.0, 0.0, 0.0)
+    r2: tuple = (0.0, 0.0, 0.0)
+    compliance: float = 0.0
+    distance: tuple = (0.0, 0.0, 0.0)
+    axis1: int = POS_X
+    axis2: int = POS_X
+    limited: bool = False
+    limit_axis1: int = POS_Y
+    limit_axis2: int = POS_Y
+    lower: float = 0.0
+    upper: float = 0.0
+    swing_axis1: int = POS_X
+    swing_axis2: int = POS_X
+    twist_axis1: int = POS_Y
+    twist_axis2: int = POS_Y
+    swing_lower: float = 0.0
+    swing_upper: float = 0.0
+    twist_lower: float = 0.0
+    twist_upper: float = 0.0
+
+
+@dataclass
+class Scene:
+    name: str
+    meshes: List[M.Mesh] = field(default_factory=list)
+    colliders: List[List[Collider]] = field(default_factory=list)
+    pos: Optional[np.ndarray] = None          # (N, 3) float64
+    rot: Optional[np.ndarray] = None          # (N, 4) float64, (x, y, z, w)
+    mass: Optional[np.ndarray] = None         # (N,) float64 (ignored for fixed bodies)
+    fixed: Optional[np.ndarray] = None        # (N,) bool
+    mus: Optional[np.ndarray] = None
+    mud: Optional[np.ndarray] = None
+    rest: Optional[np.ndarray] = None
+    vel: Optional[np.ndarray] = None          # (N, 3)
+    omega: Optional[np.ndarray] = None        # (N, 3)
+    constraints: List[Constraint] = field(default_factory=list)
+    dt: float = 1.0 / 60.0
+    substeps: int = 20
+    pos_iters: int = 1
+    collisions: bool = True
+    gravity: float = 10.0
+    steps: int = 300
+
+    @property
+    def num_bodies(self) -> int:
+        return 0 if self.pos is None else int(self.pos.shape[0])
+
+    @property
+    def num_dynamic(self) -> int:
+        return int(np.count_nonzero(~self.fixed))
+
+
+class _Builder:
+    def __init__(self, name: str):
+        self.scene = Scene(name)
+        self._mesh_ids = {}
+        self._cols, self._pos, self._rot, self._mass, self._fixed = [], [], [], [], []
+        self._mus, self._mud, self._rest, self._v, self._w = [], [], [], [], []
+
+    def mesh(self, name: str) -> int:
+        if name not in self._mesh_ids:
+            self._mesh_ids[name] = len(self.scene.meshes)
+            self.scene.meshes.append(M.MESHES[name]())
+        return self._mesh_ids[name]
+
+    def body(self, colliders, pos, rot=(0.0, 0.0, 0.0, 1.0), mass=1.0, fixed=False, mus=0.5, mud=0.3, rest=0.0,
+             v=(0.0, 0.0, 0.0), w=(0.0, 0.0, 0.0)) -> int:
+        self._cols.append(list(colliders))
+        self._pos.append(pos)
+        self._rot.append(rot)
+        self._mass.append(mass)
+        self._fixed.append(bool(fixed))
+        self._mus.append(mus)
+        self._mud.append(mud)
+        self._rest.append(rest)
+        self._v.append(v)
+        self._w.append(w)
+        return len(self._pos) - 1
+
+    def hull_body(self, mesh: str, scale, pos, **kw) -> int:
+        return self.body([Collider("hull", self.mesh(mesh), tuple(float(s) for s in scale))], pos, **kw)
+
+    def finish(self, **params) -> Scene:
+        s = self.scene
+        s.colliders = self._cols
+        s.pos = np.asarray(self._pos, dtype=np.float64).reshape(-1, 3)
+        s.rot = np.asarray(self._rot, dtype=np.float64).reshape(-1, 4)
+        s.mass = np.asarray(self._mass, dtype=np.float64)
+        s.fixed = np.asarray(self._fixed, dtype=bool)
+        s.mus = np.asarray(self._mus, dtype=np.float64)
+        s.mud = np.asarray(self._mud, dtype=np.float64)
+        s.rest = np.asarray(self._rest, dtype=np.float64)
+        s.vel = np.asarray(self._v, dtype=np.float64).reshape(-1, 3)
+        s.omega = np.asarray(self._w, dtype=np.float64).reshape(-1, 3)
+        for k, v in params.items():
+            setattr(s, k, v)
+        return s
+
+
+def random_quaternions(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform random unit quaternions (Shoemake's subgroup algorithm), (x, y, z, w)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1.0 - u1), np.sqrt(u1)
+    q = np.stack([a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2),
+                  b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)], axis=1)
+    return q
+
+
+def _floor(b: _Builder, half=(20.0, 0.5, 20.0), y_top=0.0, mus=0.5, mud=0.3):
+    return b.hull_body("cube", half, (0.0, y_top - half[1], 0.0), fixed=True, mus=mus, mud=mud)
+
+
+def stack_scene(n: int = 10, seed: int = 0) -> Scene:
+    """Cubes of edge 1 m (cube mesh scaled 0.5, density 1 -> mass 1) stacked on a 40x40 m floor."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("stack%d" % n)
+    _floor(b)
+    for i in range(n):
+        jx, jz = rng.uniform(-0.02, 0.02, size=2)
+        b.hull_body("cube", (0.5, 0.5, 0.5), (float(jx), 0.5 + i * 1.001, float(jz)), mass=1.0)
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=300)
+
+
+SHAPES = ("cube", "icosahedron", "cylinder32", "icosphere42")
+_BASE_SCALE = 0.5   # all base meshes have radius ~1; scale 0.5 makes a unit-size body
+
+
+def _mixed_body(b: _Builder, rng, shape: str, s: float, pos, rot, v, w=(0.0, 0.0, 0.0), mus=0.5, mud=0.3):
+    sc = (_BASE_SCALE * s,) * 3
+    mid = b.mesh(shape)
+    mass = M.hull_volume(b.scene.meshes[mid], sc)
+    return b.hull_body(shape, sc, pos, rot=rot, mass=mass, v=v, w=w, mus=mus, mud=mud)
+
+
+def _box_walls(b: _Builder, half_x=20.0, half_z=20.0, height=60.0, t=0.5):
+    _floor(b, (half_x, t, half_z))
+    hy = height / 2.0
+    b.hull_body("cube", (t, hy, half_z), (half_x + t, hy, 0.0), fixed=True)
+    b.hull_body("cube", (t, hy, half_z), (-half_x - t, hy, 0.0), fixed=True)
+    b.hull_body("cube", (half_x, hy, t), (0.0, hy, half_z + t), fixed=True)
+    b.hull_body("cube", (half_x, hy, t), (0.0, hy, -half_z - t), fixed=True)
+
+
+def large_scene(n: int = 4096, seed: int = 0, box=(40.0, 60.0, 40.0)) -> Scene:
+    rng = np.random.default_rng(seed)
+    b = _Builder("large%d" % n)
+    _box_walls(b, box[0] / 2.0, box[2] / 2.0, box[1])
+    shapes = rng.integers(0, len(SHAPES), size=n)
+    scales = rng.uniform(0.5, 1.5, size=n)
+    rots = random_quaternions(rng, n)
+    vels = rng.normal(0.0, 1.0, size=(n, 3))
+    # bounding radii of the base meshes (all 1) times the scale
+    radii = _BASE_SCALE * scales
+    placed = np.zeros((n, 3))
+    placed_r = np.zeros(n)
+    lo = np.array([-box[0] / 2.0, 0.0, -box[2] / 2.0])
+    hi = np.array([box[0] / 2.0, box[1], box[2] / 2.0])
+    for i in range(n):
+        r = radii[i] * math.sqrt(3.0)   # cube corners reach sqrt(3) * half-edge
+        for _ in range(10000):
+            p = rng.uniform(lo + r, hi - r)
+            if i == 0:
+                break
+            d = np.linalg.norm(placed[:i] - p, axis=1)
+            if np.all(d > placed_r[:i] + r):
+                break
+        placed[i] = p
+        placed_r[i] = r
+    for i in range(n):
+        _mixed_body(b, rng, SHAPES[shapes[i]], float(scales[i]), tuple(placed[i]), tuple(rots[i]), tuple(vels[i]))
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=600)
+
+
+def tower_scene(n: int = 64, ratio: float = 100.0, seed: int = 0, substeps: int = 50) -> Scene:
+    rng = np.random.default_rng(seed)
+    b = _Builder("tower%d" % n)
+    _floor(b)
+    for i in range(n):
+        jx, jz = rng.uniform(-0.005, 0.005, size=2)
+        mass = 1.0 if i % 2 == 0 else ratio
+        b.hull_body("cube", (0.5, 0.5, 0.5), (float(jx), 0.5 + i * 1.0005, float(jz)), mass=mass)
+    return b.finish(dt=1.0 / 60.0, substeps=substeps, pos_iters=1, collisions=True, steps=10000)
+
+
+def random_pile_scene(n: int = 12, seed: int = 0, shapes=SHAPES, spread: float = 1.6) -> Scene:
+    """A small column of mixed shapes dropped on a floor, close enough to collide within a few frames."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("pile%d_%d" % (n, seed))
+    _floor(b, (8.0, 0.5, 8.0))
+    for i in range(n):
+        shape = shapes[int(rng.integers(0, len(shapes)))]
+        s = float(rng.uniform(0.6, 1.2))
+        p = (float(rng.uniform(-spread, spread)), 0.7 + 1.2 * i, float(rng.uniform(-spread, spread)))
+        q = tuple(random_quaternions(rng, 1)[0])
+        v = tuple(rng.normal(0.0, 0.5, size=3))
+        w = tuple(rng.normal(0.0, 0.5, size=3))
+        _mixed_body(b, rng, shape, s, p, q, v, w)
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=120)
+
+
+def _axis_rotation(axis) -> tuple:
+    """Unit quaternion mapping local +X onto the given unit vector (shortest arc)."""
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    x = np.array([1.0, 0.0, 0.0])
+    c = float(np.dot(x, a))
+    if c < -0.999999:
+        return (0.0, 1.0, 0.0, 0.0)
+    v = np.cross(x, a)
+    q = np.array([v[0], v[1], v[2], 1.0 + c])
+    q /= np.linalg.norm(q)
+    return tuple(q)
+
+
+def chain_scene(links: int = 8, joint: str = "spherical", seed: int = 0, collisions: bool = True,
+                limited: bool = True) -> Scene:
+    """Cube links (0.2 x 0.2 x 0.6 m boxes) hanging from a fixed anchor, joined end to end.
+
+    Hinge chains align every link's local +X with one seeded random unit axis by rotating the
+    links' initial orientation, since the reference's joints take body-frame axes only
+    (PBD_Axis_Type, src/physics/pbd.h:5-12)."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("chain%d_%s" % (links, joint))
+    _floor(b, (10.0, 0.5, 10.0), y_top=-8.0 * links / 8.0 - 2.0)
+    half = (0.1, 0.3, 0.1)
+    axis = rng.normal(size=3)
+    rot = _axis_rotation(axis) if joint == "hinge" else (0.0, 0.0, 0.0, 1.0)
+    anchor = b.hull_body("cube", (0.1, 0.1, 0.1), (0.0, 1.0, 0.0), fixed=True, rot=rot)
+    prev = anchor
+    ids = []
+    R = _rot_matrix(rot)
+    down = R @ np.array([0.0, -1.0, 0.0])
+    y0 = np.array([0.0, 1.0, 0.0])
+    prev_off = R @ np.array([0.0, -0.1, 0.0])
+    for i in range(links):
+        centre = y0 + prev_off + down * 0.3 if i == 0 else np.asarray(b._pos[prev]) + down * 0.6
+        mass = 8.0 * half[0] * half[1] * half[2]
+        e = b.hull_body("cube", half, tuple(centre), rot=rot, mass=mass)
+        ids.append(e)
+        r1 = (0.0, -0.1, 0.0) if i == 0 else (0.0, -0.3, 0.0)
+        r2 = (0.0, 0.3, 0.0)
+        if joint == "hinge":
+            c = Constraint("hinge", prev, e, r1, r2, 0.0, axis1=POS_X, axis2=POS_X, limited=limited,
+                           limit_axis1=POS_Y, limit_axis2=POS_Y, lower=-0.5 * math.pi, upper=0.5 * math.pi)
+        else:
+            c = Constraint("spherical", prev, e, r1, r2, swing_axis1=POS_Y, swing_axis2=POS_Y,
+                           twist_axis1=POS_X, twist_axis2=POS_X, swing_lower=-math.pi, swing_upper=math.pi,
+                           twist_lower=-math.pi, twist_upper=math.pi)
+        b.scene.constraints.append(c)
+        prev = e
+    # give the chain a kick so joints and limits work
+    for k, e in enumerate(ids):
+        b._v[e] = tuple(rng.normal(0.0, 1.0, size=3))
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=collisions, steps=300)
+
+
+def _rot_matrix(q) -> np.ndarray:
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def domino_scene(n: int = 16, seed: int = 0) -> Scene:
+    """Dominoes 0.2 x 1 x 2 m (cube scaled (0.1, 0.5, 1)... standing upright: height 2 m along y)
+    spaced U(0.8, 1.2) m along x, plus a thrown unit cube with v ~ N(0, 2), w ~ N(0, 3)."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("domino%d" % n)
+    _floor(b, (max(10.0, 0.7 * n + 5.0), 0.5, 10.0))
+    x = 0.0
+    for i in range(n):
+        x += float(rng.uniform(0.8, 1.2))
+        b.hull_body("cube", (0.1, 1.0, 0.5), (x, 1.0, 0.0), mass=0.2 * 2.0 * 1.0)
+    v = rng.normal(0.0, 2.0, size=3)
+    v[0] = abs(v[0]) + 4.0
+    w = rng.normal(0.0, 3.0, size=3)
+    b.hull_body("cube", (0.5, 0.5, 0.5), (-1.0, 1.6, 0.0), mass=1.0, v=tuple(v), w=tuple(w))
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=120)
+
+
+def sphere_scene(n: int = 6, seed: int = 0) -> Scene:
+    """Analytic sphere colliders (collider_sphere_create) and a compound two-hull body."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("spheres%d" % n)
+    _floor(b, (6.0, 0.5, 6.0))
+    for i in range(n):
+        r = float(np.float32(rng.uniform(0.3, 0.6)))
+        p = (float(rng.uniform(-0.6, 0.6)), 0.8 + 1.1 * i, float(rng.uniform(-0.6, 0.6)))
+        b.body([Collider("sphere", radius=r)], p, mass=1.0, v=tuple(rng.normal(0, 0.3, size=3)))
+    cm = b.mesh("cube")
+    b.body([Collider("hull", cm, (0.3, 0.3, 0.3)), Collider("hull", cm, (0.6, 0.1, 0.1))], (0.3, 0.5 + 1.1 * n, 0.2),
+           mass=2.0)
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=120)
