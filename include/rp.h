@@ -1,0 +1,183 @@
+/*
+ * raw-physics GB300 — C ABI of the rigid-body step.
+ *
+ * The hot path of raw-physics is one call per rendered frame,
+ *   pbd_simulate_with_constraints(dt, entities, constraints, substeps, pos_iters, collisions)
+ *   (src/physics/pbd.h:93-94, src/physics/pbd.cpp:468-747),
+ * fed by the entity / collider / constraint API around it. This header exposes the same operations
+ * over plain pointers and sizes, with every step computed by CUDA kernels on one GB300:
+ *
+ *   reference                                   this ABI
+ *   collider_convex_hull_create (collider.h:48)   rp_hull_create
+ *   collider_sphere_create      (collider.h:49)   rp_collider_desc{RP_COLLIDER_SPHERE, ...}
+ *   entity_create / _fixed      (entity.h:52-55)  rp_entity_create
+ *   entity_add_force            (entity.h:65)     rp_entity_add_force
+ *   entity_clear_forces         (entity.h:66)     rp_entity_clear_forces
+ *   pbd_*_constraint_*_init     (pbd.h:96-102)    rp_constraint_*
+ *   pbd_simulate(_with_constraints) (pbd.h:93-94) rp_simulate
+ *   Entity fields read/written in place          rp_state_get / rp_state_set (snapshot/restore)
+ *   broad_get_collision_pairs   (broad.h:11)      rp_broad_pairs
+ *   colliders_get_contacts      (collider.h:55)   rp_contacts
+ *
+ * Entities are numbered in creation order (the order entity_get_all returns, entity.cpp:88).
+ * A world holds one or more independent scenes; rp_simulate advances all of them in one launch
+ * (the batched form). Every function returns RP_OK or a negative rp_status; nothing aborts.
+ *
+ * The C++-mangled pbd_simulate / pbd_simulate_with_constraints drop-in built on this ABI is declared
+ * in include/rp_compat.h.
+ */
+#ifndef RP_GB300_H
+#define RP_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rp_world rp_world;
+typedef int32_t rp_status;
+
+enum {
+    RP_OK = 0,
+    RP_ERR_INVALID = -1,        /* bad argument (unknown entity, bad size, NaN pose, ...) */
+    RP_ERR_CUDA = -2,           /* a CUDA call failed (message in rp_last_error) */
+    RP_ERR_NO_DEVICE = -3,      /* no CUDA device / the CUDA extension cannot run here */
+    RP_ERR_CAPACITY = -4,       /* a scratch buffer could not be grown enough */
+    RP_ERR_DEGENERATE = -5,     /* geometry the reference rejects with an assert */
+    RP_ERR_TIMEOUT = -6,        /* a bounded device-side wait gave up */
+    RP_ERR_STATE = -7           /* call not allowed in the current state */
+};
+
+enum { RP_PRECISION_FP32 = 0, RP_PRECISION_FP64 = 1 };
+/* RP_PRECISION_FP32: FP32 arithmetic, FP64 positions / orientations and EPA face test.
+ * RP_PRECISION_FP64: every quantity in FP64, evaluated in the reference's operation order without
+ *                    FMA contraction (reproduces the reference's FP64 results). */
+
+enum { RP_COLLIDER_SPHERE = 0, RP_COLLIDER_HULL = 1 };        /* Collider_Type, collider.h:33-36 */
+enum { RP_AXIS_POS_X = 0, RP_AXIS_NEG_X, RP_AXIS_POS_Y, RP_AXIS_NEG_Y, RP_AXIS_POS_Z, RP_AXIS_NEG_Z }; /* PBD_Axis_Type */
+
+#define RP_STATE_DOUBLES 28
+/* Per-entity state record of rp_state_get / rp_state_set (all FP64):
+ *  0..2 world_position  3..6 world_rotation (x,y,z,w)  7..9 linear_velocity  10..12 angular_velocity
+ * 13..15 previous_world_position  16..19 previous_world_rotation  20..22 previous_linear_velocity
+ * 23..25 previous_angular_velocity  26 active (0/1)  27 deactivation_time */
+
+#define RP_CONTACT_DOUBLES 9   /* rp_contacts record: collision_point1[3], collision_point2[3], normal[3] */
+
+typedef struct {
+    int32_t type;      /* RP_COLLIDER_SPHERE or RP_COLLIDER_HULL */
+    int32_t hull;      /* hull id from rp_hull_create (hulls) */
+    float radius;      /* sphere radius (spheres) */
+} rp_collider_desc;
+
+/* -- world ------------------------------------------------------------------------------------ */
+rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision);
+void      rp_world_destroy(rp_world* w);
+/* Use an existing cudaStream_t (passed as void*) for every launch and copy of this world. */
+rp_status rp_world_set_stream(rp_world* w, void* cuda_stream);
+const char* rp_last_error(void);
+/* Adds a new empty scene; scene 0 exists from creation. */
+rp_status rp_scene_create(rp_world* w, int32_t* out_scene);
+
+/* -- geometry ---------------------------------------------------------------------------------- */
+/* collider_convex_hull_create (src/physics/collider.cpp:194-364) from a triangle list: num_vertices
+ * FP64 positions (already scaled, as examples_util.cpp:5-24 does) and num_indices indices
+ * (3 per triangle, counter-clockwise seen from outside). Identical hulls are shared. */
+rp_status rp_hull_create(rp_world* w, const double* vertices, uint32_t num_vertices, const uint32_t* indices,
+                         uint32_t num_indices, int32_t* out_hull);
+/* A hull whose topology the caller already holds, in the reference's Collider_Convex_Hull form
+ * (collider.h:15-24) flattened to CSR: unique vertices, face normals, face boundary loops, and the
+ * vertex->faces, vertex->neighbours, face->neighbours lists, each *_start array having one more entry
+ * than rows. Used by the pbd_simulate drop-in, which forwards the caller's own colliders. */
+rp_status rp_hull_create_from_topology(rp_world* w, const double* vertices, int32_t num_vertices, const double* face_normals,
+                                       int32_t num_faces, const int32_t* face_start, const int32_t* face_elements,
+                                       const int32_t* v2f_start, const int32_t* v2f, const int32_t* v2n_start,
+                                       const int32_t* v2n, const int32_t* f2n_start, const int32_t* f2n,
+                                       int32_t* out_hull);
+/* Topology queries of a built hull (for tests): counts, then the arrays. */
+rp_status rp_hull_info(rp_world* w, int32_t hull, int32_t* num_vertices, int32_t* num_faces);
+rp_status rp_hull_face(rp_world* w, int32_t hull, int32_t face, double normal[3], int32_t* elements, int32_t cap,
+                       int32_t* num_elements);
+
+/* -- entities ------------------------------------------------------------------------------------ */
+/* entity_create / entity_create_fixed (src/entity.cpp:24-65): bounding radius, inverse mass and the
+ * point-mass inertia tensor are derived as the reference derives them. Returns the entity index. */
+rp_status rp_entity_create(rp_world* w, int32_t scene, const double position[3], const double rotation[4], double mass,
+                           int32_t fixed, const rp_collider_desc* colliders, uint32_t num_colliders,
+                           double static_friction, double dynamic_friction, double restitution, int32_t* out_entity);
+rp_status rp_entity_set_velocity(rp_world* w, int32_t entity, const double linear[3], const double angular[3]);
+/* entity_add_force: applies to the next rp_simulate only, as the reference's callers clear forces
+ * after every frame (src/examples/stack.cpp:100-102). */
+rp_status rp_entity_add_force(rp_world* w, int32_t entity, const double position[3], const double force[3],
+                              int32_t local_coords);
+rp_status rp_entity_clear_forces(rp_world* w, int32_t entity);
+/* Persistent gravity: before every step each entity gets the force (0, -g / inverse_mass, 0), added
+ * after its other forces, as the example scenes do (src/examples/stack.cpp:93-96). 0 disables it. */
+rp_status rp_world_set_gravity(rp_world* w, double g);
+rp_status rp_entity_get_mass_properties(rp_world* w, int32_t entity, double* inverse_mass, double inertia[9],
+                                        double inverse_inertia[9], double* bounding_radius);
+/* Overrides what rp_entity_create derived (a caller that edited Entity::inverse_mass or the
+ * inertia tensors, as the drop-in forwards them). Row-major 3x3 tensors; must be symmetric. */
+rp_status rp_entity_set_mass_properties(rp_world* w, int32_t entity, double inverse_mass, const double inertia[9],
+                                        const double inverse_inertia[9], double bounding_radius);
+int32_t   rp_num_entities(const rp_world* w);
+
+/* -- external constraints (src/physics/pbd.h:96-102); entities must share a scene --------------- */
+rp_status rp_constraint_positional(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3],
+                                   double compliance, const double distance[3], int32_t* out);
+rp_status rp_constraint_mutual_orientation(rp_world* w, int32_t e1, int32_t e2, double compliance, int32_t* out);
+rp_status rp_constraint_hinge(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3], double compliance,
+                              int32_t e1_aligned_axis, int32_t e2_aligned_axis, int32_t limited, int32_t e1_limit_axis,
+                              int32_t e2_limit_axis, double lower_limit, double upper_limit, int32_t* out);
+rp_status rp_constraint_spherical(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3],
+                                  int32_t e1_swing_axis, int32_t e2_swing_axis, int32_t e1_twist_axis,
+                                  int32_t e2_twist_axis, double swing_lower, double swing_upper, double twist_lower,
+                                  double twist_upper, int32_t* out);
+
+/* -- stepping ------------------------------------------------------------------------------------ */
+/* pbd_simulate_with_constraints for every scene of the world: num_steps frames of dt each, all on
+ * the device (one persistent launch per frame), then forces added with rp_entity_add_force are
+ * cleared. dt <= 0 is a no-op, as in the reference (pbd.cpp:471). Asynchronous with respect to the
+ * host unless a state read follows; device status is checked by rp_sync. */
+rp_status rp_simulate(rp_world* w, double dt, uint32_t num_substeps, uint32_t num_pos_iters, int32_t enable_collisions,
+                      uint32_t num_steps);
+/* Waits for the world's stream and folds device status into the return value. */
+rp_status rp_sync(rp_world* w);
+/* Device status bits accumulated since the last call (RP_STATUS_* below). */
+rp_status rp_last_status(rp_world* w, uint32_t* bits);
+enum {
+    RP_STATUS_PAIR_OVERFLOW = 1 << 0,     /* broad-phase pairs exceeded the scratch (the step is redone larger) */
+    RP_STATUS_CONTACT_OVERFLOW = 1 << 1,  /* contacts exceeded the scratch (the step is redone larger) */
+    RP_STATUS_EPA_OVERFLOW = 1 << 2,      /* an EPA polytope outgrew its fixed storage; that pair was dropped */
+    RP_STATUS_CLIP_OVERFLOW = 1 << 3,     /* a clipped polygon outgrew its fixed storage */
+    RP_STATUS_BARRIER_TIMEOUT = 1 << 4,   /* a bounded device barrier gave up */
+    RP_STATUS_DEGENERATE = 1 << 5,        /* geometry the reference would reject with an assert */
+    RP_STATUS_LEVEL_OVERFLOW = 1 << 6,    /* solver dependency depth exceeded its table */
+    RP_STATUS_EPA_NOT_CONVERGED = 1 << 8  /* informational: EPA hit its iteration cap (reference prints a warning) */
+};
+
+/* -- state --------------------------------------------------------------------------------------- */
+rp_status rp_state_get(rp_world* w, double* out /* num_entities * RP_STATE_DOUBLES */);
+rp_status rp_state_set(rp_world* w, const double* in);
+
+/* -- diagnostics and known-answer entry points --------------------------------------------------- */
+/* broad_get_collision_pairs of one scene on the current state: entity-index pairs in the reference's
+ * order. *count receives the total even when it exceeds cap. */
+rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out_pairs, uint32_t cap, uint32_t* count);
+/* colliders_update + colliders_get_contacts for one entity pair on the current state, computed by
+ * the device narrowphase. out: RP_CONTACT_DOUBLES per contact. */
+rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
+/* Counters accumulated since creation: [0] GJK iterations, [1] EPA iterations, [2] EPA calls,
+ * [3] steps, [4] substeps, [5] contacts generated (last step), [6] pairs (last step), [7] levels (last step). */
+rp_status rp_counters(rp_world* w, uint64_t out[8]);
+/* Kernel launches issued by this world since creation (every launch of the CUDA extension). */
+uint64_t  rp_kernel_launches(const rp_world* w);
+/* Average duration of the step kernel over the last rp_simulate, measured with CUDA events on the
+ * world's stream (milliseconds per launch; 0 if timing is off). */
+rp_status rp_set_timing(rp_world* w, int32_t enabled);
+rp_status rp_last_step_ms(rp_world* w, double* ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

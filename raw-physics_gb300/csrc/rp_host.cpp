@@ -1,0 +1,1161 @@
+// Host runtime of the GB300 rigid-body step and the C ABI of include/rp.h.
+//
+// The world keeps a host mirror of the reference's entity / collider / constraint data (set-up
+// only), lays it out in HBM scene by scene (rp_world.h), and drives the persistent step kernel.
+// After the first upload the device copy of the body state is authoritative: stepping never
+// touches the host, and rp_state_get / rp_state_set are the only transfers.
+#include "../../include/rp.h"
+#include "rp_hull.h"
+#include "rp_launch.h"
+#include "rp_world.h"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace rp {
+
+static thread_local std::string g_last_error;
+static rp_status fail(rp_status code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+#define RP_CUDA(call)                                                                                        \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess) return fail(RP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        size_t want = n ? n : 16;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    template <typename T> T* as() const { return (T*)p; }
+};
+
+struct Force { double pos[3], f[3]; };
+
+struct HostBody {
+    int scene = 0;
+    double pos[3], rot[4], v[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+    double ppos[3] = {0, 0, 0}, prot[4] = {0, 0, 0, 1}, pv[3] = {0, 0, 0}, pw[3] = {0, 0, 0};
+    double active = 1.0, deact = 0.0;
+    double invm = 0.0, I[9], Iinv[9], radius = 0.0;
+    int fixed = 0;
+    double mus = 0, mud = 0, rest = 0;
+    std::vector<rp_collider_desc> cols;
+    std::vector<Force> forces;
+    int slot = -1;   // index in the device layout (bodies grouped by scene)
+};
+
+struct HostExt {
+    ExtConstraint c;   // e1/e2 hold entity indices here; slots are substituted at upload
+    int scene;
+};
+
+}  // namespace rp
+
+using namespace rp;
+
+struct rp_world {
+    int device = 0;
+    int precision = RP_PRECISION_FP32;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    int grid_blocks = 0;
+
+    std::vector<std::unique_ptr<Hull>> hulls;
+    std::map<std::vector<double>, int> hull_index;   // content -> hull id (identical hulls are shared)
+    int num_scenes = 1;
+    std::vector<HostBody> bodies;
+    std::vector<HostExt> exts;
+    double gravity = 0.0;
+
+    // upload state
+    bool static_dirty = true;    // layout or constants changed: rebuild the device copy
+    bool forces_dirty = true;
+    bool device_state_valid = false;   // device holds the authoritative body state
+    std::vector<int> slot_to_entity;
+
+    // layout
+    std::vector<int32_t> scene_body, scene_ext, scene_pair_cap, scene_contact_cap, scene_node_cap;
+    int max_levels = 1024;
+    bool grid_mode = false;
+    double pair_mult = 1.0, contact_mult = 1.0;   // grown when a step overflows its scratch
+
+    // device buffers
+    DevBuf d_scene_body, d_scene_ext, d_scene_pair_cap, d_scene_contact_cap, d_scene_node_cap;
+    DevBuf d_pos, d_rot, d_ppos, d_prot, d_vel, d_omega, d_pvel, d_pomega, d_active, d_deact;
+    DevBuf d_backup;
+    DevBuf d_invm, d_I, d_Iinv, d_mat, d_radius, d_fixed, d_col_start, d_force, d_torque;
+    DevBuf d_colliders, d_shapes, d_shape_verts, d_face_normal, d_face_elem_start, d_face_elem, d_csr_start, d_csr_data;
+    DevBuf d_tverts, d_tnorms, d_ext;
+    DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
+    DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
+        d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_contacts, d_ext_lambda, d_status, d_barrier,
+        d_counters, d_kat_out, d_kat_count;
+
+    uint64_t launches = 0;
+    uint64_t steps = 0, substeps = 0;
+    uint32_t status_accum = 0;
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    uint32_t last_launches = 0;
+
+    size_t rsize() const { return precision == RP_PRECISION_FP64 ? 8 : 4; }
+};
+
+namespace {
+
+rp_status check_world(rp_world* w) {
+    if (!w) return fail(RP_ERR_INVALID, "null world");
+    return RP_OK;
+}
+
+bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+std::vector<ColliderDesc> descs(rp_world* w, const std::vector<rp_collider_desc>& cols) {
+    std::vector<ColliderDesc> d;
+    for (const rp_collider_desc& c : cols)
+        d.push_back({c.type, c.type == RP_COLLIDER_HULL ? w->hulls[(size_t)c.hull].get() : nullptr, c.radius});
+    return d;
+}
+
+template <typename T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    cudaError_t e = b.ensure(v.size() * sizeof(T));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+// convert FP64 host values to the build's working type
+template <typename T>
+std::vector<unsigned char> as_working(const std::vector<double>& v, size_t rsize) {
+    std::vector<unsigned char> out(v.size() * rsize);
+    for (size_t i = 0; i < v.size(); ++i) {
+        if (rsize == 8) std::memcpy(&out[i * 8], &v[i], 8);
+        else { float f = (float)v[i]; std::memcpy(&out[i * 4], &f, 4); }
+    }
+    return out;
+}
+
+rp_status sync_state_to_host(rp_world* w);
+
+// (Re)build the device layout: bodies grouped by scene, shapes, colliders, constraints, scratch.
+rp_status build_device(rp_world* w) {
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+    }
+    cudaStream_t st = w->stream;
+    const int S = w->num_scenes;
+    const size_t N = w->bodies.size();
+    // slots: stable by scene
+    w->scene_body.assign((size_t)S + 1, 0);
+    for (const HostBody& b : w->bodies) w->scene_body[(size_t)b.scene + 1]++;
+    for (int s = 0; s < S; ++s) w->scene_body[(size_t)s + 1] += w->scene_body[(size_t)s];
+    std::vector<int> fill(w->scene_body.begin(), w->scene_body.end() - 1);
+    w->slot_to_entity.assign(N, 0);
+    for (size_t e = 0; e < N; ++e) {
+        HostBody& b = w->bodies[e];
+        b.slot = fill[(size_t)b.scene]++;
+        w->slot_to_entity[(size_t)b.slot] = (int)e;
+    }
+    // external constraints grouped by scene
+    w->scene_ext.assign((size_t)S + 1, 0);
+    for (const HostExt& x : w->exts) w->scene_ext[(size_t)x.scene + 1]++;
+    for (int s = 0; s < S; ++s) w->scene_ext[(size_t)s + 1] += w->scene_ext[(size_t)s];
+    std::vector<ExtConstraint> ext(w->exts.size());
+    {
+        std::vector<int> ef(w->scene_ext.begin(), w->scene_ext.end() - 1);
+        for (const HostExt& x : w->exts) {
+            ExtConstraint c = x.c;
+            c.e1 = w->bodies[(size_t)c.e1].slot;
+            c.e2 = w->bodies[(size_t)c.e2].slot;
+            ext[(size_t)ef[(size_t)x.scene]++] = c;
+        }
+    }
+    // scratch capacities per scene
+    w->scene_pair_cap.assign((size_t)S + 1, 0);
+    w->scene_contact_cap.assign((size_t)S + 1, 0);
+    w->scene_node_cap.assign((size_t)S + 1, 0);
+    int max_bodies = 0;
+    for (int s = 0; s < S; ++s) {
+        long long n = w->scene_body[(size_t)s + 1] - w->scene_body[(size_t)s];
+        max_bodies = std::max(max_bodies, (int)n);
+        long long all = n * (n - 1) / 2;
+        long long pc = std::min(all, (long long)(std::max(1024.0, 48.0 * (double)n) * w->pair_mult));
+        long long cc = (long long)(std::max(256.0, 8.0 * (double)pc) * w->contact_mult);
+        if (pc > (1LL << 30) || cc > (1LL << 30)) return fail(RP_ERR_CAPACITY, "scratch sizes beyond 2^30 entries");
+        w->scene_pair_cap[(size_t)s + 1] = w->scene_pair_cap[(size_t)s] + (int32_t)pc;
+        w->scene_contact_cap[(size_t)s + 1] = w->scene_contact_cap[(size_t)s] + (int32_t)cc;
+        w->scene_node_cap[(size_t)s + 1] = w->scene_node_cap[(size_t)s] + (int32_t)pc +
+                                           (w->scene_ext[(size_t)s + 1] - w->scene_ext[(size_t)s]);
+    }
+    w->grid_mode = (S == 1 && max_bodies >= 256);
+    w->max_levels = w->grid_mode ? 8192 : 1024;
+    // shapes: every hull id used by a collider, in hull-id order
+    std::vector<Shape> shapes;
+    std::vector<double> sverts, snorm;
+    std::vector<int32_t> fstart, felem, cstart, cdata;
+    std::vector<int> shape_of_hull(w->hulls.size(), -1);
+    for (size_t h = 0; h < w->hulls.size(); ++h) {
+        const Hull& H = *w->hulls[h];
+        Shape sh;
+        sh.nv = H.nv();
+        sh.nf = H.nf();
+        sh.vert_off = (int32_t)(sverts.size() / 3);
+        sh.face_off = (int32_t)fstart.size();
+        sh.max_face_valence = 0;
+        sh.max_face_neighbours = 0;
+        sverts.insert(sverts.end(), H.verts.begin(), H.verts.end());
+        snorm.insert(snorm.end(), H.normals.begin(), H.normals.end());
+        // face element CSR over one global face numbering (face_off = the shape's first face);
+        // a single sentinel after the last shape closes the final face
+        for (int f = 0; f < sh.nf; ++f) {
+            fstart.push_back((int32_t)felem.size());
+            felem.insert(felem.end(), H.faces[(size_t)f].begin(), H.faces[(size_t)f].end());
+            sh.max_face_valence = std::max(sh.max_face_valence, (int32_t)H.faces[(size_t)f].size());
+            sh.max_face_neighbours = std::max(sh.max_face_neighbours, (int32_t)H.f2n[(size_t)f].size());
+        }
+        auto add_csr = [&](const std::vector<std::vector<int>>& rows) {
+            int32_t off = (int32_t)cstart.size();
+            for (const auto& r : rows) {
+                cstart.push_back((int32_t)cdata.size());
+                cdata.insert(cdata.end(), r.begin(), r.end());
+            }
+            cstart.push_back((int32_t)cdata.size());
+            return off;
+        };
+        sh.v2f_off = add_csr(H.v2f);
+        sh.v2n_off = add_csr(H.v2n);
+        sh.f2n_off = add_csr(H.f2n);
+        shape_of_hull[h] = (int)shapes.size();
+        shapes.push_back(sh);
+    }
+    fstart.push_back((int32_t)felem.size());
+    // colliders, transformed-geometry offsets
+    std::vector<Collider> cols;
+    std::vector<int32_t> col_start(N + 1, 0);
+    int32_t tv = 0, tn = 0;
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        col_start[slot] = (int32_t)cols.size();
+        for (const rp_collider_desc& d : b.cols) {
+            Collider c;
+            c.type = d.type;
+            c.shape = d.type == RP_COLLIDER_HULL ? shape_of_hull[(size_t)d.hull] : -1;
+            c.radius = d.radius;
+            c.tv_off = tv;
+            c.tn_off = tn;
+            if (d.type == RP_COLLIDER_HULL) {
+                tv += shapes[(size_t)c.shape].nv;
+                tn += shapes[(size_t)c.shape].nf;
+            }
+            cols.push_back(c);
+        }
+    }
+    col_start[N] = (int32_t)cols.size();
+    // body constants
+    std::vector<double> invm(N), I6(6 * N), Ii6(6 * N), mat(4 * N), rad(N);
+    std::vector<uint8_t> fixedv(N);
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        invm[slot] = b.invm;
+        const int sym[6] = {0, 4, 8, 1, 2, 5};
+        for (int k = 0; k < 6; ++k) { I6[6 * slot + (size_t)k] = b.I[sym[k]]; Ii6[6 * slot + (size_t)k] = b.Iinv[sym[k]]; }
+        mat[4 * slot] = b.mus;
+        mat[4 * slot + 1] = b.mud;
+        mat[4 * slot + 2] = b.rest;
+        mat[4 * slot + 3] = 0.0;
+        rad[slot] = b.radius;
+        fixedv[slot] = (uint8_t)b.fixed;
+    }
+    const size_t R = w->rsize();
+    RP_CUDA(upload(w->d_scene_body, w->scene_body, st));
+    RP_CUDA(upload(w->d_scene_ext, w->scene_ext, st));
+    RP_CUDA(upload(w->d_scene_pair_cap, w->scene_pair_cap, st));
+    RP_CUDA(upload(w->d_scene_contact_cap, w->scene_contact_cap, st));
+    RP_CUDA(upload(w->d_scene_node_cap, w->scene_node_cap, st));
+    RP_CUDA(upload(w->d_invm, as_working<double>(invm, R), st));
+    RP_CUDA(upload(w->d_I, as_working<double>(I6, R), st));
+    RP_CUDA(upload(w->d_Iinv, as_working<double>(Ii6, R), st));
+    RP_CUDA(upload(w->d_mat, as_working<double>(mat, R), st));
+    RP_CUDA(upload(w->d_radius, rad, st));
+    RP_CUDA(upload(w->d_fixed, fixedv, st));
+    RP_CUDA(upload(w->d_col_start, col_start, st));
+    RP_CUDA(upload(w->d_colliders, cols, st));
+    RP_CUDA(upload(w->d_shapes, shapes, st));
+    RP_CUDA(upload(w->d_shape_verts, sverts, st));
+    RP_CUDA(upload(w->d_face_normal, snorm, st));
+    RP_CUDA(upload(w->d_face_elem_start, fstart, st));
+    RP_CUDA(upload(w->d_face_elem, felem, st));
+    RP_CUDA(upload(w->d_csr_start, cstart, st));
+    RP_CUDA(upload(w->d_csr_data, cdata, st));
+    RP_CUDA(upload(w->d_ext, ext, st));
+    RP_CUDA(w->d_tverts.ensure((size_t)std::max(tv, 1) * 3 * R));
+    RP_CUDA(w->d_tnorms.ensure((size_t)std::max(tn, 1) * 3 * R));
+    // mutable state
+    RP_CUDA(w->d_pos.ensure(std::max<size_t>(N, 1) * 32));
+    RP_CUDA(w->d_rot.ensure(std::max<size_t>(N, 1) * 32));
+    RP_CUDA(w->d_ppos.ensure(std::max<size_t>(N, 1) * 32));
+    RP_CUDA(w->d_prot.ensure(std::max<size_t>(N, 1) * 32));
+    RP_CUDA(w->d_vel.ensure(std::max<size_t>(N, 1) * 3 * R));
+    RP_CUDA(w->d_omega.ensure(std::max<size_t>(N, 1) * 3 * R));
+    RP_CUDA(w->d_pvel.ensure(std::max<size_t>(N, 1) * 3 * R));
+    RP_CUDA(w->d_pomega.ensure(std::max<size_t>(N, 1) * 3 * R));
+    RP_CUDA(w->d_active.ensure(std::max<size_t>(N, 1)));
+    RP_CUDA(w->d_deact.ensure(std::max<size_t>(N, 1) * 8));
+    RP_CUDA(w->d_force.ensure(std::max<size_t>(N, 1) * 24));
+    RP_CUDA(w->d_torque.ensure(std::max<size_t>(N, 1) * 24));
+    // scratch
+    const size_t P = (size_t)w->scene_pair_cap[(size_t)S], C = (size_t)w->scene_contact_cap[(size_t)S],
+                 NN = (size_t)w->scene_node_cap[(size_t)S], E = w->exts.size();
+    RP_CUDA(w->d_pair_count.ensure((size_t)S * 4));
+    RP_CUDA(w->d_pairs.ensure(std::max<size_t>(P, 1) * 8));
+    RP_CUDA(w->d_row_count.ensure(std::max<size_t>(N, 1) * 4));
+    RP_CUDA(w->d_uf_parent.ensure(std::max<size_t>(N, 1) * 4));
+    RP_CUDA(w->d_island_awake.ensure(std::max<size_t>(N, 1)));
+    RP_CUDA(w->d_node_body.ensure(std::max<size_t>(NN, 1) * 8));
+    RP_CUDA(w->d_node_pred.ensure(std::max<size_t>(NN, 1) * 8));
+    RP_CUDA(w->d_node_level.ensure(std::max<size_t>(NN, 1) * 4));
+    RP_CUDA(w->d_tl_count.ensure(std::max<size_t>(N, 1) * 4));
+    RP_CUDA(w->d_tl_start.ensure((N + 1) * 4));
+    RP_CUDA(w->d_tl.ensure(std::max<size_t>(NN, 1) * 8));
+    RP_CUDA(w->d_level_count.ensure((size_t)S * (size_t)(w->max_levels + 1) * 4));
+    RP_CUDA(w->d_level_fill.ensure((size_t)S * (size_t)(w->max_levels + 1) * 4));
+    RP_CUDA(w->d_scan_tmp.ensure(4096 * 4));
+    RP_CUDA(w->d_level_nodes.ensure(std::max<size_t>(NN, 1) * 4));
+    RP_CUDA(w->d_scene_levels.ensure((size_t)S * 4));
+    RP_CUDA(w->d_scene_nodes.ensure((size_t)S * 4));
+    RP_CUDA(w->d_pair_cstart.ensure(std::max<size_t>(P, 1) * 4));
+    RP_CUDA(w->d_pair_ccount.ensure(std::max<size_t>(P, 1) * 4));
+    RP_CUDA(w->d_contact_count.ensure((size_t)S * 4));
+    RP_CUDA(w->d_contacts.ensure(std::max<size_t>(C, 1) * 12 * R));
+    RP_CUDA(w->d_ext_lambda.ensure(std::max<size_t>(E, 1) * 4 * 8));
+    if (!w->d_status.p) {
+        RP_CUDA(w->d_barrier.ensure(64));
+        RP_CUDA(cudaMemsetAsync(w->d_barrier.p, 0, 64, st));
+        RP_CUDA(w->d_counters.ensure(8 * 8));
+        RP_CUDA(cudaMemsetAsync(w->d_counters.p, 0, 64, st));
+    }
+    RP_CUDA(w->d_status.ensure((size_t)S * 4));
+    RP_CUDA(cudaMemsetAsync(w->d_status.p, 0, (size_t)S * 4, st));
+    RP_CUDA(cudaMemsetAsync(w->d_pair_count.p, 0, (size_t)S * 4, st));
+    RP_CUDA(cudaMemsetAsync(w->d_scene_levels.p, 0, (size_t)S * 4, st));
+    w->static_dirty = false;
+    w->forces_dirty = true;
+    // upload the host state
+    w->device_state_valid = false;
+    return RP_OK;
+}
+
+template <typename R>
+WorldView<R> make_view(rp_world* w) {
+    WorldView<R> V;
+    std::memset(&V, 0, sizeof(V));
+    V.num_scenes = w->num_scenes;
+    V.scene_body = w->d_scene_body.as<int32_t>();
+    V.scene_ext = w->d_scene_ext.as<int32_t>();
+    V.scene_pair_cap = w->d_scene_pair_cap.as<int32_t>();
+    V.scene_contact_cap = w->d_scene_contact_cap.as<int32_t>();
+    V.scene_node_cap = w->d_scene_node_cap.as<int32_t>();
+    V.pos = w->d_pos.as<double4_32a>();
+    V.rot = w->d_rot.as<double4_32a>();
+    V.prev_pos = w->d_ppos.as<double4_32a>();
+    V.prev_rot = w->d_prot.as<double4_32a>();
+    V.vel = w->d_vel.as<R>();
+    V.omega = w->d_omega.as<R>();
+    V.prev_vel = w->d_pvel.as<R>();
+    V.prev_omega = w->d_pomega.as<R>();
+    V.active = w->d_active.as<uint8_t>();
+    V.deact = w->d_deact.as<double>();
+    V.inv_mass = w->d_invm.as<R>();
+    V.inertia = w->d_I.as<R>();
+    V.inv_inertia = w->d_Iinv.as<R>();
+    V.material = w->d_mat.as<R>();
+    V.radius = w->d_radius.as<double>();
+    V.fixed = w->d_fixed.as<uint8_t>();
+    V.col_start = w->d_col_start.as<int32_t>();
+    V.force = w->d_force.as<double>();
+    V.torque = w->d_torque.as<double>();
+    V.colliders = w->d_colliders.as<Collider>();
+    V.shapes = w->d_shapes.as<Shape>();
+    V.shape_verts = w->d_shape_verts.as<double>();
+    V.face_normal = w->d_face_normal.as<double>();
+    V.face_elem_start = w->d_face_elem_start.as<int32_t>();
+    V.face_elem = w->d_face_elem.as<int32_t>();
+    V.csr_start = w->d_csr_start.as<int32_t>();
+    V.csr_data = w->d_csr_data.as<int32_t>();
+    V.tverts = w->d_tverts.as<R>();
+    V.tnorms = w->d_tnorms.as<R>();
+    V.ext = w->d_ext.as<ExtConstraint>();
+    V.pair_count = w->d_pair_count.as<int32_t>();
+    V.pairs = w->d_pairs.as<int2>();
+    V.row_count = w->d_row_count.as<int32_t>();
+    V.uf_parent = w->d_uf_parent.as<int32_t>();
+    V.island_awake = w->d_island_awake.as<uint8_t>();
+    V.node_body = w->d_node_body.as<int32_t>();
+    V.node_pred = w->d_node_pred.as<int32_t>();
+    V.node_level = w->d_node_level.as<int32_t>();
+    V.body_tl_count = w->d_tl_count.as<int32_t>();
+    V.body_tl_start = w->d_tl_start.as<int32_t>();
+    V.body_tl = w->d_tl.as<int32_t>();
+    V.level_count = w->d_level_count.as<int32_t>();
+    V.level_fill = w->d_level_fill.as<int32_t>();
+    V.scan_tmp = w->d_scan_tmp.as<int32_t>();
+    V.level_nodes = w->d_level_nodes.as<int32_t>();
+    V.scene_levels = w->d_scene_levels.as<int32_t>();
+    V.scene_nodes = w->d_scene_nodes.as<int32_t>();
+    V.pair_cstart = w->d_pair_cstart.as<int32_t>();
+    V.pair_ccount = w->d_pair_ccount.as<int32_t>();
+    V.contact_count = w->d_contact_count.as<int32_t>();
+    V.contacts = w->d_contacts.as<R>();
+    V.ext_lambda = w->d_ext_lambda.as<double>();
+    V.max_levels = w->max_levels;
+    V.status = w->d_status.as<uint32_t>();
+    V.barrier = w->d_barrier.as<unsigned int>();
+    V.counters = w->d_counters.as<unsigned long long>();
+    return V;
+}
+
+// Mutable per-body state layout on the device, for snapshots.
+struct StateSlices {
+    DevBuf* b[10];
+    size_t bytes[10];
+};
+StateSlices state_slices(rp_world* w) {
+    const size_t N = w->bodies.size(), R = w->rsize();
+    StateSlices s = {{&w->d_pos, &w->d_rot, &w->d_ppos, &w->d_prot, &w->d_vel, &w->d_omega, &w->d_pvel, &w->d_pomega,
+                      &w->d_active, &w->d_deact},
+                     {N * 32, N * 32, N * 32, N * 32, N * 3 * R, N * 3 * R, N * 3 * R, N * 3 * R, N, N * 8}};
+    return s;
+}
+
+rp_status upload_state(rp_world* w) {
+    const size_t N = w->bodies.size(), R = w->rsize();
+    std::vector<double> pos(4 * N), rot(4 * N), ppos(4 * N), prot(4 * N), deact(N);
+    std::vector<double> vel(3 * N), om(3 * N), pvel(3 * N), pom(3 * N);
+    std::vector<uint8_t> act(N);
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        for (int k = 0; k < 3; ++k) {
+            pos[4 * slot + (size_t)k] = b.pos[k];
+            ppos[4 * slot + (size_t)k] = b.ppos[k];
+            vel[3 * slot + (size_t)k] = b.v[k];
+            om[3 * slot + (size_t)k] = b.w[k];
+            pvel[3 * slot + (size_t)k] = b.pv[k];
+            pom[3 * slot + (size_t)k] = b.pw[k];
+        }
+        pos[4 * slot + 3] = 0.0;
+        ppos[4 * slot + 3] = 0.0;
+        for (int k = 0; k < 4; ++k) { rot[4 * slot + (size_t)k] = b.rot[k]; prot[4 * slot + (size_t)k] = b.prot[k]; }
+        act[slot] = b.active != 0.0 ? 1 : 0;
+        deact[slot] = b.deact;
+    }
+    cudaStream_t st = w->stream;
+    RP_CUDA(upload(w->d_pos, pos, st));
+    RP_CUDA(upload(w->d_rot, rot, st));
+    RP_CUDA(upload(w->d_ppos, ppos, st));
+    RP_CUDA(upload(w->d_prot, prot, st));
+    RP_CUDA(upload(w->d_vel, as_working<double>(vel, R), st));
+    RP_CUDA(upload(w->d_omega, as_working<double>(om, R), st));
+    RP_CUDA(upload(w->d_pvel, as_working<double>(pvel, R), st));
+    RP_CUDA(upload(w->d_pomega, as_working<double>(pom, R), st));
+    RP_CUDA(upload(w->d_active, act, st));
+    RP_CUDA(upload(w->d_deact, deact, st));
+    RP_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
+    w->device_state_valid = true;
+    return RP_OK;
+}
+
+// n working-type values (float or double) from the device, widened to double
+std::vector<double> fetch(const DevBuf& b, size_t n, size_t rsize, cudaStream_t st, cudaError_t& err) {
+    std::vector<double> out(n);
+    if (n == 0) return out;
+    if (rsize == 8) {
+        err = cudaMemcpyAsync(out.data(), b.p, n * 8, cudaMemcpyDeviceToHost, st);
+    } else {
+        std::vector<float> f(n);
+        err = cudaMemcpyAsync(f.data(), b.p, n * 4, cudaMemcpyDeviceToHost, st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+        for (size_t i = 0; i < n; ++i) out[i] = f[i];
+    }
+    return out;
+}
+
+rp_status sync_state_to_host(rp_world* w) {
+    if (!w->device_state_valid) return RP_OK;
+    const size_t N = w->bodies.size(), R = w->rsize();
+    cudaStream_t st = w->stream;
+    cudaError_t e = cudaSuccess;
+    std::vector<double> pos(4 * N), rot(4 * N), ppos(4 * N), prot(4 * N), deact(N);
+    std::vector<uint8_t> act(N);
+    if (N) {
+        RP_CUDA(cudaMemcpyAsync(pos.data(), w->d_pos.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(rot.data(), w->d_rot.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(ppos.data(), w->d_ppos.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(prot.data(), w->d_prot.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(deact.data(), w->d_deact.p, N * 8, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(act.data(), w->d_active.p, N, cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<double> vel = fetch(w->d_vel, 3 * N, R, st, e);
+    if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
+    std::vector<double> om = fetch(w->d_omega, 3 * N, R, st, e);
+    std::vector<double> pvel = fetch(w->d_pvel, 3 * N, R, st, e);
+    std::vector<double> pom = fetch(w->d_pomega, 3 * N, R, st, e);
+    if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
+    RP_CUDA(cudaStreamSynchronize(st));
+    for (size_t slot = 0; slot < N; ++slot) {
+        HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        for (int k = 0; k < 3; ++k) {
+            b.pos[k] = pos[4 * slot + (size_t)k];
+            b.ppos[k] = ppos[4 * slot + (size_t)k];
+            b.v[k] = vel[3 * slot + (size_t)k];
+            b.w[k] = om[3 * slot + (size_t)k];
+            b.pv[k] = pvel[3 * slot + (size_t)k];
+            b.pw[k] = pom[3 * slot + (size_t)k];
+        }
+        for (int k = 0; k < 4; ++k) { b.rot[k] = rot[4 * slot + (size_t)k]; b.prot[k] = prot[4 * slot + (size_t)k]; }
+        b.active = act[slot] ? 1.0 : 0.0;
+        b.deact = deact[slot];
+    }
+    return RP_OK;
+}
+
+rp_status ensure_device(rp_world* w) {
+    if (w->static_dirty) {
+        rp_status s = build_device(w);
+        if (s != RP_OK) return s;
+    }
+    if (!w->device_state_valid) {
+        rp_status s = upload_state(w);
+        if (s != RP_OK) return s;
+    }
+    return RP_OK;
+}
+
+// calculate_external_force / _torque (physics_util.cpp:5-24) over the step's forces, then gravity
+rp_status upload_forces(rp_world* w) {
+    const size_t N = w->bodies.size();
+    std::vector<double> F(3 * N, 0.0), T(3 * N, 0.0);
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        if (b.fixed) continue;
+        double f[3] = {0.0, 0.0, 0.0}, t[3] = {0.0, 0.0, 0.0};
+        std::vector<Force> all = b.forces;
+        if (w->gravity != 0.0) all.push_back({{0.0, 0.0, 0.0}, {0.0, -w->gravity * 1.0 / b.invm, 0.0}});
+        for (const Force& x : all) { f[0] = f[0] + x.f[0]; f[1] = f[1] + x.f[1]; f[2] = f[2] + x.f[2]; }
+        for (const Force& x : all) {
+            double d[3] = {x.pos[0] - 0.0, x.pos[1] - 0.0, x.pos[2] - 0.0};
+            double c[3] = {d[1] * x.f[2] - d[2] * x.f[1], d[2] * x.f[0] - d[0] * x.f[2], d[0] * x.f[1] - d[1] * x.f[0]};
+            t[0] = t[0] + c[0]; t[1] = t[1] + c[1]; t[2] = t[2] + c[2];
+        }
+        for (int k = 0; k < 3; ++k) { F[3 * slot + (size_t)k] = f[k]; T[3 * slot + (size_t)k] = t[k]; }
+    }
+    RP_CUDA(upload(w->d_force, F, w->stream));
+    RP_CUDA(upload(w->d_torque, T, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    w->forces_dirty = false;
+    return RP_OK;
+}
+
+cudaError_t launch_step(rp_world* w, const StepParams& P) {
+    cudaError_t e;
+    if (w->precision == RP_PRECISION_FP64) e = step_f64(make_view<double>(w), P, w->grid_mode, w->grid_mode ? w->grid_blocks : w->num_scenes, w->stream);
+    else e = step_f32(make_view<float>(w), P, w->grid_mode, w->grid_mode ? w->grid_blocks : w->num_scenes, w->stream);
+    w->launches++;
+    return e;
+}
+
+rp_status snapshot(rp_world* w, bool restore) {
+    StateSlices s = state_slices(w);
+    size_t total = 0;
+    for (int i = 0; i < 10; ++i) total += (s.bytes[i] + 255) & ~(size_t)255;
+    if (!restore) RP_CUDA(w->d_backup.ensure(total));
+    size_t off = 0;
+    for (int i = 0; i < 10; ++i) {
+        char* bk = (char*)w->d_backup.p + off;
+        if (s.bytes[i]) {
+            if (restore) RP_CUDA(cudaMemcpyAsync(s.b[i]->p, bk, s.bytes[i], cudaMemcpyDeviceToDevice, w->stream));
+            else RP_CUDA(cudaMemcpyAsync(bk, s.b[i]->p, s.bytes[i], cudaMemcpyDeviceToDevice, w->stream));
+        }
+        off += (s.bytes[i] + 255) & ~(size_t)255;
+    }
+    return RP_OK;
+}
+
+uint32_t read_status(rp_world* w, cudaError_t& e) {
+    std::vector<uint32_t> st((size_t)w->num_scenes, 0);
+    e = cudaMemcpyAsync(st.data(), w->d_status.p, st.size() * 4, cudaMemcpyDeviceToHost, w->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    uint32_t bits = 0;
+    for (uint32_t x : st) bits |= x;
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->d_status.p, 0, st.size() * 4, w->stream);
+    return bits;
+}
+
+}  // namespace
+
+// =====================================================================================================
+// C ABI
+extern "C" {
+
+const char* rp_last_error(void) { return g_last_error.c_str(); }
+
+rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision) {
+    if (!out) return fail(RP_ERR_INVALID, "null out");
+    *out = nullptr;
+    if (precision != RP_PRECISION_FP32 && precision != RP_PRECISION_FP64) return fail(RP_ERR_INVALID, "bad precision");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(RP_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= n) return fail(RP_ERR_INVALID, "bad device index");
+    RP_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    RP_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10) return fail(RP_ERR_NO_DEVICE, "the kernels are built for sm_103a (GB300)");
+    std::unique_ptr<rp_world> w(new rp_world());
+    w->device = device;
+    w->precision = precision;
+    w->num_sms = prop.multiProcessorCount;
+    RP_CUDA(precision == RP_PRECISION_FP64 ? configure_f64() : configure_f32());
+    int per_sm = precision == RP_PRECISION_FP64 ? grid_blocks_per_sm_f64() : grid_blocks_per_sm_f32();
+    if (per_sm <= 0) return fail(RP_ERR_CUDA, "step kernel cannot be resident");
+    w->grid_blocks = std::min(per_sm * w->num_sms, 4096);
+    RP_CUDA(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    w->own_stream = true;
+    RP_CUDA(cudaEventCreate(&w->ev0));
+    RP_CUDA(cudaEventCreate(&w->ev1));
+    w->scene_body.assign(2, 0);
+    *out = w.release();
+    return RP_OK;
+}
+
+void rp_world_destroy(rp_world* w) {
+    if (!w) return;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    if (w->ev0) cudaEventDestroy(w->ev0);
+    if (w->ev1) cudaEventDestroy(w->ev1);
+    if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+}
+
+rp_status rp_world_set_stream(rp_world* w, void* stream) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    if (w->own_stream) cudaStreamDestroy(w->stream);
+    w->stream = (cudaStream_t)stream;
+    w->own_stream = false;
+    return RP_OK;
+}
+
+rp_status rp_scene_create(rp_world* w, int32_t* out) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (out) *out = w->num_scenes;
+    w->num_scenes++;
+    w->static_dirty = true;
+    return RP_OK;
+}
+
+rp_status rp_hull_create(rp_world* w, const double* v, uint32_t nv, const uint32_t* idx, uint32_t ni, int32_t* out) {
+    if (check_world(w) || !v || !idx || !out) return fail(RP_ERR_INVALID, "null argument");
+    std::vector<double> key(v, v + 3 * (size_t)nv);
+    key.push_back(-1.0);
+    for (uint32_t i = 0; i < ni; ++i) key.push_back((double)idx[i]);
+    auto it = w->hull_index.find(key);
+    if (it != w->hull_index.end()) { *out = it->second; return RP_OK; }
+    std::unique_ptr<Hull> h(new Hull());
+    std::string err = build_hull(v, nv, idx, ni, *h);
+    if (!err.empty()) return fail(RP_ERR_DEGENERATE, err);
+    *out = (int32_t)w->hulls.size();
+    w->hulls.push_back(std::move(h));
+    w->hull_index.emplace(std::move(key), *out);
+    w->static_dirty = true;
+    return RP_OK;
+}
+
+rp_status rp_hull_create_from_topology(rp_world* w, const double* verts, int32_t nv, const double* normals, int32_t nf,
+                                       const int32_t* fstart, const int32_t* felem, const int32_t* v2f_start,
+                                       const int32_t* v2f, const int32_t* v2n_start, const int32_t* v2n,
+                                       const int32_t* f2n_start, const int32_t* f2n, int32_t* out) {
+    if (check_world(w) || !verts || !normals || !fstart || !felem || !v2f_start || !v2f || !v2n_start || !v2n ||
+        !f2n_start || !f2n || !out || nv <= 0 || nf <= 0)
+        return fail(RP_ERR_INVALID, "bad hull topology");
+    std::unique_ptr<Hull> h(new Hull());
+    h->verts.assign(verts, verts + 3 * (size_t)nv);
+    h->normals.assign(normals, normals + 3 * (size_t)nf);
+    auto rows = [](const int32_t* start, const int32_t* data, int32_t n, int32_t bound, std::vector<std::vector<int>>& dst) {
+        dst.assign((size_t)n, {});
+        for (int32_t r = 0; r < n; ++r) {
+            if (start[r + 1] < start[r]) return false;
+            for (int32_t k = start[r]; k < start[r + 1]; ++k) {
+                if (data[k] < 0 || data[k] >= bound) return false;
+                dst[(size_t)r].push_back(data[k]);
+            }
+        }
+        return true;
+    };
+    if (!rows(fstart, felem, nf, nv, h->faces) || !rows(v2f_start, v2f, nv, nf, h->v2f) ||
+        !rows(v2n_start, v2n, nv, nv, h->v2n) || !rows(f2n_start, f2n, nf, nf, h->f2n))
+        return fail(RP_ERR_INVALID, "hull topology index out of range");
+    *out = (int32_t)w->hulls.size();
+    w->hulls.push_back(std::move(h));
+    w->static_dirty = true;
+    return RP_OK;
+}
+
+rp_status rp_hull_info(rp_world* w, int32_t hull, int32_t* nv, int32_t* nf) {
+    if (check_world(w) || hull < 0 || hull >= (int32_t)w->hulls.size()) return fail(RP_ERR_INVALID, "bad hull");
+    if (nv) *nv = w->hulls[(size_t)hull]->nv();
+    if (nf) *nf = w->hulls[(size_t)hull]->nf();
+    return RP_OK;
+}
+
+rp_status rp_hull_face(rp_world* w, int32_t hull, int32_t face, double normal[3], int32_t* elems, int32_t cap, int32_t* ne) {
+    if (check_world(w) || hull < 0 || hull >= (int32_t)w->hulls.size()) return fail(RP_ERR_INVALID, "bad hull");
+    const Hull& H = *w->hulls[(size_t)hull];
+    if (face < 0 || face >= H.nf()) return fail(RP_ERR_INVALID, "bad face");
+    if (normal)
+        for (int k = 0; k < 3; ++k) normal[k] = H.normals[(size_t)(3 * face + k)];
+    const std::vector<int>& f = H.faces[(size_t)face];
+    if (ne) *ne = (int32_t)f.size();
+    for (int32_t i = 0; i < cap && i < (int32_t)f.size(); ++i) elems[i] = f[(size_t)i];
+    return RP_OK;
+}
+
+rp_status rp_entity_create(rp_world* w, int32_t scene, const double p[3], const double q[4], double mass, int32_t fixed,
+                           const rp_collider_desc* cols, uint32_t ncols, double mus, double mud, double rest, int32_t* out) {
+    if (check_world(w) || !p || !q || (!cols && ncols) || !out) return fail(RP_ERR_INVALID, "null argument");
+    if (scene < 0 || scene >= w->num_scenes) return fail(RP_ERR_INVALID, "bad scene");
+    if (ncols == 0) return fail(RP_ERR_INVALID, "an entity needs at least one collider");
+    if (!finite3(p) || !std::isfinite(q[0]) || !std::isfinite(q[1]) || !std::isfinite(q[2]) || !std::isfinite(q[3]))
+        return fail(RP_ERR_INVALID, "pose is not finite");
+    if (!fixed && !(mass > 0.0)) return fail(RP_ERR_INVALID, "mass must be positive");
+    if (!(mus >= 0.0 && mus <= 1.0 && mud >= 0.0 && mud <= 1.0 && rest >= 0.0 && rest <= 1.0))
+        return fail(RP_ERR_INVALID, "friction and restitution must lie in [0, 1] (entity.cpp:55-57)");
+    HostBody b;
+    b.scene = scene;
+    for (uint32_t i = 0; i < ncols; ++i) {
+        if (cols[i].type == RP_COLLIDER_HULL) {
+            if (cols[i].hull < 0 || cols[i].hull >= (int32_t)w->hulls.size()) return fail(RP_ERR_INVALID, "bad hull id");
+        } else if (cols[i].type != RP_COLLIDER_SPHERE || !(cols[i].radius > 0.0f)) {
+            return fail(RP_ERR_INVALID, "bad collider");
+        }
+        b.cols.push_back(cols[i]);
+    }
+    std::vector<ColliderDesc> d = descs(w, b.cols);
+    b.radius = bounding_radius(d);
+    if (fixed) {
+        b.invm = 0.0;
+        for (int k = 0; k < 9; ++k) b.I[k] = b.Iinv[k] = 0.0;
+    } else {
+        b.invm = 1.0 / mass;
+        std::string err = inertia(d, mass, b.I, b.Iinv);
+        if (!err.empty()) return fail(RP_ERR_DEGENERATE, err);
+    }
+    for (int k = 0; k < 3; ++k) b.pos[k] = p[k];
+    for (int k = 0; k < 4; ++k) b.rot[k] = q[k];
+    b.fixed = fixed ? 1 : 0;
+    b.mus = mus;
+    b.mud = mud;
+    b.rest = rest;
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+        w->device_state_valid = false;
+    }
+    w->bodies.push_back(b);
+    w->static_dirty = true;
+    *out = (int32_t)w->bodies.size() - 1;
+    return RP_OK;
+}
+
+rp_status rp_entity_set_velocity(rp_world* w, int32_t e, const double v[3], const double om[3]) {
+    if (check_world(w) || e < 0 || e >= (int32_t)w->bodies.size() || !v || !om) return fail(RP_ERR_INVALID, "bad entity");
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+        w->device_state_valid = false;
+    }
+    for (int k = 0; k < 3; ++k) { w->bodies[(size_t)e].v[k] = v[k]; w->bodies[(size_t)e].w[k] = om[k]; }
+    return RP_OK;
+}
+
+rp_status rp_entity_add_force(rp_world* w, int32_t e, const double pos[3], const double f[3], int32_t local) {
+    if (check_world(w) || e < 0 || e >= (int32_t)w->bodies.size() || !pos || !f) return fail(RP_ERR_INVALID, "bad entity");
+    Force x;
+    if (local) {
+        // entity_add_force with local coordinates (entity.cpp:176-191): rotate the force and the
+        // point by the entity's current orientation (unit scale)
+        if (w->device_state_valid) {
+            rp_status s = sync_state_to_host(w);
+            if (s != RP_OK) return s;
+        }
+        const double* q = w->bodies[(size_t)e].rot;
+        double ix = q[3] * f[0] + q[1] * f[2] - q[2] * f[1];
+        double iy = q[3] * f[1] + q[2] * f[0] - q[0] * f[2];
+        double iz = q[3] * f[2] + q[0] * f[1] - q[1] * f[0];
+        double iw = -q[0] * f[0] - q[1] * f[1] - q[2] * f[2];
+        x.f[0] = (ix * q[3]) + (iw * -q[0]) + (iy * -q[2]) - (iz * -q[1]);
+        x.f[1] = (iy * q[3]) + (iw * -q[1]) + (iz * -q[0]) - (ix * -q[2]);
+        x.f[2] = (iz * q[3]) + (iw * -q[2]) + (ix * -q[1]) - (iy * -q[0]);
+        double m[3][3];
+        m[0][0] = 1.0 - 2.0 * q[1] * q[1] - 2.0 * q[2] * q[2];
+        m[1][0] = 2.0 * q[0] * q[1] + 2.0 * q[3] * q[2];
+        m[2][0] = 2.0 * q[0] * q[2] - 2.0 * q[3] * q[1];
+        m[0][1] = 2.0 * q[0] * q[1] - 2.0 * q[3] * q[2];
+        m[1][1] = 1.0 - (2.0 * q[0] * q[0]) - (2.0 * q[2] * q[2]);
+        m[2][1] = 2.0 * q[1] * q[2] + 2.0 * q[3] * q[0];
+        m[0][2] = 2.0 * q[0] * q[2] + 2.0 * q[3] * q[1];
+        m[1][2] = 2.0 * q[1] * q[2] - 2.0 * q[3] * q[0];
+        m[2][2] = 1.0 - (2.0 * q[0] * q[0]) - (2.0 * q[1] * q[1]);
+        // rotation * identity scale, then the point transform with a zero translation column
+        double r[3][4];
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j) {
+                double sc[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
+                r[i][j] = m[i][0] * sc[0] + m[i][1] * sc[1] + m[i][2] * sc[2] + 0.0 * 0.0;
+            }
+            r[i][3] = m[i][0] * 0.0 + m[i][1] * 0.0 + m[i][2] * 0.0 + 0.0 * 1.0;
+        }
+        for (int i = 0; i < 3; ++i) x.pos[i] = r[i][0] * pos[0] + r[i][1] * pos[1] + r[i][2] * pos[2] + r[i][3] * 1.0;
+    } else {
+        for (int k = 0; k < 3; ++k) { x.pos[k] = pos[k]; x.f[k] = f[k]; }
+    }
+    w->bodies[(size_t)e].forces.push_back(x);
+    w->forces_dirty = true;
+    return RP_OK;
+}
+
+rp_status rp_entity_clear_forces(rp_world* w, int32_t e) {
+    if (check_world(w) || e < 0 || e >= (int32_t)w->bodies.size()) return fail(RP_ERR_INVALID, "bad entity");
+    if (!w->bodies[(size_t)e].forces.empty()) w->forces_dirty = true;
+    w->bodies[(size_t)e].forces.clear();
+    return RP_OK;
+}
+
+rp_status rp_world_set_gravity(rp_world* w, double g) {
+    if (check_world(w) || !std::isfinite(g)) return fail(RP_ERR_INVALID, "bad gravity");
+    if (g != w->gravity) w->forces_dirty = true;
+    w->gravity = g;
+    return RP_OK;
+}
+
+rp_status rp_entity_get_mass_properties(rp_world* w, int32_t e, double* invm, double I[9], double Iinv[9], double* radius) {
+    if (check_world(w) || e < 0 || e >= (int32_t)w->bodies.size()) return fail(RP_ERR_INVALID, "bad entity");
+    const HostBody& b = w->bodies[(size_t)e];
+    if (invm) *invm = b.invm;
+    if (I) std::memcpy(I, b.I, sizeof(b.I));
+    if (Iinv) std::memcpy(Iinv, b.Iinv, sizeof(b.Iinv));
+    if (radius) *radius = b.radius;
+    return RP_OK;
+}
+
+rp_status rp_entity_set_mass_properties(rp_world* w, int32_t e, double invm, const double I[9], const double Iinv[9],
+                                        double radius) {
+    if (check_world(w) || e < 0 || e >= (int32_t)w->bodies.size() || !I || !Iinv) return fail(RP_ERR_INVALID, "bad entity");
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            if (I[3 * r + c] != I[3 * c + r] || Iinv[3 * r + c] != Iinv[3 * c + r])
+                return fail(RP_ERR_INVALID, "inertia tensors must be symmetric");
+    HostBody& b = w->bodies[(size_t)e];
+    b.invm = invm;
+    std::memcpy(b.I, I, sizeof(b.I));
+    std::memcpy(b.Iinv, Iinv, sizeof(b.Iinv));
+    b.radius = radius;
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+        w->device_state_valid = false;
+    }
+    w->static_dirty = true;
+    w->forces_dirty = true;
+    return RP_OK;
+}
+
+int32_t rp_num_entities(const rp_world* w) { return w ? (int32_t)w->bodies.size() : 0; }
+
+static rp_status add_ext(rp_world* w, ExtConstraint c, int32_t* out) {
+    if (c.e1 < 0 || c.e2 < 0 || c.e1 >= (int32_t)w->bodies.size() || c.e2 >= (int32_t)w->bodies.size())
+        return fail(RP_ERR_INVALID, "bad entity");
+    if (w->bodies[(size_t)c.e1].scene != w->bodies[(size_t)c.e2].scene) return fail(RP_ERR_INVALID, "entities in different scenes");
+    if (c.e1 == c.e2) return fail(RP_ERR_INVALID, "a constraint needs two distinct entities");
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+        w->device_state_valid = false;
+    }
+    HostExt x;
+    x.c = c;
+    x.scene = w->bodies[(size_t)c.e1].scene;
+    w->exts.push_back(x);
+    w->static_dirty = true;
+    if (out) *out = (int32_t)w->exts.size() - 1;
+    return RP_OK;
+}
+
+static ExtConstraint ext_base(int32_t type, int32_t e1, int32_t e2, const double* r1, const double* r2) {
+    ExtConstraint c;
+    std::memset(&c, 0, sizeof(c));
+    c.type = type;
+    c.e1 = e1;
+    c.e2 = e2;
+    for (int k = 0; k < 3; ++k) { c.r1[k] = r1 ? r1[k] : 0.0; c.r2[k] = r2 ? r2[k] : 0.0; }
+    return c;
+}
+
+rp_status rp_constraint_positional(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3], double compliance,
+                                   const double distance[3], int32_t* out) {
+    if (check_world(w) || !r1 || !r2 || !distance) return fail(RP_ERR_INVALID, "null argument");
+    ExtConstraint c = ext_base(CON_POSITIONAL, e1, e2, r1, r2);
+    c.compliance = compliance;
+    for (int k = 0; k < 3; ++k) c.distance[k] = distance[k];
+    return add_ext(w, c, out);
+}
+
+rp_status rp_constraint_mutual_orientation(rp_world* w, int32_t e1, int32_t e2, double compliance, int32_t* out) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    ExtConstraint c = ext_base(CON_MUTUAL_ORIENTATION, e1, e2, nullptr, nullptr);
+    c.compliance = compliance;
+    return add_ext(w, c, out);
+}
+
+rp_status rp_constraint_hinge(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3], double compliance,
+                              int32_t a1, int32_t a2, int32_t limited, int32_t l1, int32_t l2, double lower, double upper,
+                              int32_t* out) {
+    if (check_world(w) || !r1 || !r2) return fail(RP_ERR_INVALID, "null argument");
+    if (a1 < 0 || a1 > 5 || a2 < 0 || a2 > 5 || (limited && (l1 < 0 || l1 > 5 || l2 < 0 || l2 > 5)))
+        return fail(RP_ERR_INVALID, "bad axis");
+    ExtConstraint c = ext_base(CON_HINGE, e1, e2, r1, r2);
+    c.compliance = compliance;
+    c.a1 = a1; c.a2 = a2; c.limited = limited ? 1 : 0;
+    c.l1 = limited ? l1 : 0; c.l2 = limited ? l2 : 0;
+    c.lo = limited ? lower : 0.0; c.hi = limited ? upper : 0.0;
+    return add_ext(w, c, out);
+}
+
+rp_status rp_constraint_spherical(rp_world* w, int32_t e1, int32_t e2, const double r1[3], const double r2[3], int32_t s1,
+                                  int32_t s2, int32_t t1, int32_t t2, double slo, double shi, double tlo, double thi,
+                                  int32_t* out) {
+    if (check_world(w) || !r1 || !r2) return fail(RP_ERR_INVALID, "null argument");
+    if (s1 < 0 || s1 > 5 || s2 < 0 || s2 > 5 || t1 < 0 || t1 > 5 || t2 < 0 || t2 > 5) return fail(RP_ERR_INVALID, "bad axis");
+    ExtConstraint c = ext_base(CON_SPHERICAL, e1, e2, r1, r2);
+    c.a1 = s1; c.a2 = s2; c.l1 = t1; c.l2 = t2;
+    c.lo = slo; c.hi = shi; c.lo2 = tlo; c.hi2 = thi;
+    return add_ext(w, c, out);
+}
+
+rp_status rp_simulate(rp_world* w, double dt, uint32_t substeps, uint32_t iters, int32_t collisions, uint32_t nsteps) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (!std::isfinite(dt) || substeps == 0) return fail(RP_ERR_INVALID, "bad dt or substep count");
+    if (w->bodies.empty() || nsteps == 0 || !(dt > 0.0)) return RP_OK;
+    RP_CUDA(cudaSetDevice(w->device));
+    rp_status s = ensure_device(w);
+    if (s != RP_OK) return s;
+    if (w->forces_dirty) {
+        s = upload_forces(w);
+        if (s != RP_OK) return s;
+    }
+    StepParams P;
+    P.dt = dt;
+    P.num_substeps = (int32_t)substeps;
+    P.num_pos_iters = (int32_t)iters;
+    P.enable_collisions = collisions ? 1 : 0;
+    P.pad = 0;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        s = snapshot(w, false);
+        if (s != RP_OK) return s;
+        if (w->timing) RP_CUDA(cudaEventRecord(w->ev0, w->stream));
+        for (uint32_t k = 0; k < nsteps; ++k) RP_CUDA(launch_step(w, P));
+        if (w->timing) RP_CUDA(cudaEventRecord(w->ev1, w->stream));
+        cudaError_t e;
+        uint32_t bits = read_status(w, e);
+        if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
+        if (w->timing) {
+            float ms = 0.f;
+            RP_CUDA(cudaEventElapsedTime(&ms, w->ev0, w->ev1));
+            w->last_ms = ms / nsteps;
+        }
+        if (bits & (ST_PAIR_OVERFLOW | ST_CONTACT_OVERFLOW)) {
+            // restore the frames' starting state, grow the scratch 4x and redo them
+            s = snapshot(w, true);
+            if (s != RP_OK) return s;
+            s = sync_state_to_host(w);
+            if (s != RP_OK) return s;
+            if (bits & ST_PAIR_OVERFLOW) w->pair_mult *= 4.0;
+            if (bits & ST_CONTACT_OVERFLOW) w->contact_mult *= 4.0;
+            w->static_dirty = true;
+            s = ensure_device(w);
+            if (s != RP_OK) return s;
+            s = upload_forces(w);
+            if (s != RP_OK) return s;
+            continue;
+        }
+        w->status_accum |= bits;
+        break;
+    }
+    w->steps += nsteps;
+    w->substeps += (uint64_t)nsteps * substeps;
+    for (HostBody& b : w->bodies)
+        if (!b.forces.empty()) { b.forces.clear(); w->forces_dirty = true; }
+    if (w->status_accum & ST_BARRIER_TIMEOUT) return fail(RP_ERR_TIMEOUT, "device barrier timed out");
+    return RP_OK;
+}
+
+rp_status rp_sync(rp_world* w) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    return RP_OK;
+}
+
+rp_status rp_last_status(rp_world* w, uint32_t* bits) {
+    if (check_world(w) || !bits) return RP_ERR_INVALID;
+    *bits = w->status_accum;
+    w->status_accum = 0;
+    return RP_OK;
+}
+
+rp_status rp_state_get(rp_world* w, double* out) {
+    if (check_world(w) || (!out && !w->bodies.empty())) return fail(RP_ERR_INVALID, "null argument");
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+    }
+    for (size_t e = 0; e < w->bodies.size(); ++e) {
+        const HostBody& b = w->bodies[e];
+        double* o = out + e * RP_STATE_DOUBLES;
+        for (int k = 0; k < 3; ++k) { o[k] = b.pos[k]; o[7 + k] = b.v[k]; o[10 + k] = b.w[k]; o[13 + k] = b.ppos[k]; o[20 + k] = b.pv[k]; o[23 + k] = b.pw[k]; }
+        for (int k = 0; k < 4; ++k) { o[3 + k] = b.rot[k]; o[16 + k] = b.prot[k]; }
+        o[26] = b.active;
+        o[27] = b.deact;
+    }
+    return RP_OK;
+}
+
+rp_status rp_state_set(rp_world* w, const double* in) {
+    if (check_world(w) || (!in && !w->bodies.empty())) return fail(RP_ERR_INVALID, "null argument");
+    for (size_t e = 0; e < w->bodies.size(); ++e) {
+        const double* o = in + e * RP_STATE_DOUBLES;
+        for (int k = 0; k < RP_STATE_DOUBLES; ++k)
+            if (!std::isfinite(o[k])) return fail(RP_ERR_INVALID, "state is not finite");
+    }
+    for (size_t e = 0; e < w->bodies.size(); ++e) {
+        HostBody& b = w->bodies[e];
+        const double* o = in + e * RP_STATE_DOUBLES;
+        for (int k = 0; k < 3; ++k) { b.pos[k] = o[k]; b.v[k] = o[7 + k]; b.w[k] = o[10 + k]; b.ppos[k] = o[13 + k]; b.pv[k] = o[20 + k]; b.pw[k] = o[23 + k]; }
+        for (int k = 0; k < 4; ++k) { b.rot[k] = o[3 + k]; b.prot[k] = o[16 + k]; }
+        b.active = o[26] != 0.0 ? 1.0 : 0.0;
+        b.deact = o[27];
+    }
+    w->device_state_valid = false;
+    if (!w->static_dirty) return upload_state(w);
+    return RP_OK;
+}
+
+rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out, uint32_t cap, uint32_t* count) {
+    if (check_world(w) || scene < 0 || scene >= w->num_scenes || (!out && cap)) return fail(RP_ERR_INVALID, "bad argument");
+    RP_CUDA(cudaSetDevice(w->device));
+    rp_status s = ensure_device(w);
+    if (s != RP_OK) return s;
+    if (w->precision == RP_PRECISION_FP64) RP_CUDA(broad_f64(make_view<double>(w), scene, w->stream));
+    else RP_CUDA(broad_f32(make_view<float>(w), scene, w->stream));
+    w->launches++;
+    int32_t n = 0;
+    RP_CUDA(cudaMemcpyAsync(&n, w->d_pair_count.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    int32_t pc = w->scene_pair_cap[(size_t)scene + 1] - w->scene_pair_cap[(size_t)scene];
+    if (count) *count = (uint32_t)n;
+    if (n > pc) return fail(RP_ERR_CAPACITY, "more pairs than the scratch holds");
+    std::vector<int2> pr((size_t)n);
+    if (n) RP_CUDA(cudaMemcpyAsync(pr.data(), w->d_pairs.as<int2>() + w->scene_pair_cap[(size_t)scene], (size_t)n * 8,
+                                   cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    for (int32_t k = 0; k < n && (uint32_t)k < cap; ++k) {
+        out[2 * k] = (uint32_t)w->slot_to_entity[(size_t)pr[(size_t)k].x];
+        out[2 * k + 1] = (uint32_t)w->slot_to_entity[(size_t)pr[(size_t)k].y];
+    }
+    return RP_OK;
+}
+
+rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count) {
+    if (check_world(w) || e1 < 0 || e2 < 0 || e1 >= (int32_t)w->bodies.size() || e2 >= (int32_t)w->bodies.size() || e1 == e2)
+        return fail(RP_ERR_INVALID, "bad entity");
+    RP_CUDA(cudaSetDevice(w->device));
+    rp_status s = ensure_device(w);
+    if (s != RP_OK) return s;
+    const int kcap = 64;
+    RP_CUDA(w->d_kat_out.ensure((size_t)kcap * 9 * 8));
+    RP_CUDA(w->d_kat_count.ensure(4));
+    int a = w->bodies[(size_t)e1].slot, b = w->bodies[(size_t)e2].slot;
+    if (w->precision == RP_PRECISION_FP64)
+        RP_CUDA(contacts_f64(make_view<double>(w), a, b, w->d_kat_out.as<double>(), kcap, w->d_kat_count.as<int>(), w->stream));
+    else
+        RP_CUDA(contacts_f32(make_view<float>(w), a, b, w->d_kat_out.as<double>(), kcap, w->d_kat_count.as<int>(), w->stream));
+    w->launches++;
+    int n = 0;
+    std::vector<double> buf((size_t)kcap * 9);
+    RP_CUDA(cudaMemcpyAsync(&n, w->d_kat_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaMemcpyAsync(buf.data(), w->d_kat_out.p, buf.size() * 8, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    if (count) *count = (uint32_t)n;
+    for (int k = 0; k < n && (uint32_t)k < cap && k < kcap; ++k)
+        for (int j = 0; j < 9; ++j) out[9 * k + j] = buf[(size_t)(9 * k + j)];
+    return RP_OK;
+}
+
+rp_status rp_counters(rp_world* w, uint64_t out[8]) {
+    if (check_world(w) || !out) return RP_ERR_INVALID;
+    for (int k = 0; k < 8; ++k) out[k] = 0;
+    if (w->d_counters.p) {
+        unsigned long long c[8];
+        RP_CUDA(cudaMemcpyAsync(c, w->d_counters.p, 64, cudaMemcpyDeviceToHost, w->stream));
+        int32_t cc = 0, pc = 0, lv = 0;
+        if (w->d_contact_count.p) RP_CUDA(cudaMemcpyAsync(&cc, w->d_contact_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
+        if (w->d_pair_count.p) RP_CUDA(cudaMemcpyAsync(&pc, w->d_pair_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
+        if (w->d_scene_levels.p) RP_CUDA(cudaMemcpyAsync(&lv, w->d_scene_levels.p, 4, cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaStreamSynchronize(w->stream));
+        out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+        out[5] = (uint64_t)cc; out[6] = (uint64_t)pc; out[7] = (uint64_t)lv;
+    }
+    out[3] = w->steps;
+    out[4] = w->substeps;
+    return RP_OK;
+}
+
+uint64_t rp_kernel_launches(const rp_world* w) { return w ? w->launches : 0; }
+
+rp_status rp_set_timing(rp_world* w, int32_t enabled) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    w->timing = enabled != 0;
+    return RP_OK;
+}
+
+rp_status rp_last_step_ms(rp_world* w, double* ms) {
+    if (check_world(w) || !ms) return RP_ERR_INVALID;
+    *ms = w->last_ms;
+    return RP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// Kernel entry points and host-side launchers of one precision build.
+// rp_kernels_f32.cu and rp_kernels_f64.cu include this file with RP_EXACT 0 / 1; the FP64 build is
+// compiled without FMA contraction so that it evaluates the reference's FP64 expressions exactly.
+#pragma once
+#include "rp_step.cuh"
+#include "rp_launch.h"
+
+namespace rp {
+
+// Broad phase of one scene with one CTA (known-answer entry point rp_broad_pairs).
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) broad_kernel(WorldView<R> W, int s) {
+    __shared__ int scan_smem[32];
+    CtaGroup g;
+    broad_phase(W, g, s, scan_smem);
+}
+
+// Narrowphase of one body pair with one warp (known-answer entry point rp_contacts): transform the
+// two bodies' hulls, then colliders_get_contacts; writes contact points in world coordinates.
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(32) contacts_kernel(WorldView<R> W, int a, int b, double* out, int cap, int* count) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    NarrowSmem<R>& sm = *reinterpret_cast<NarrowSmem<R>*>(dyn_smem);
+    const int lane = threadIdx.x;
+    for (int side = 0; side < 2; ++side) {
+        int body = side ? b : a;
+        for (int ci = W.col_start[body]; ci < W.col_start[body + 1]; ++ci) {
+            const Collider col = W.colliders[ci];
+            if (col.type != COL_HULL) continue;
+            const Shape sh = W.shapes[col.shape];
+            double4_32a p4 = W.pos[body], q4 = W.rot[body];
+            V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
+            V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
+            if (EXACT) {
+                M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
+                for (int i = lane; i < sh.nv; i += 32) {
+                    const double* v = W.shape_verts + 3 * (sh.vert_off + i);
+                    tv[i] = v3cast<R>(m4_point(M, v3<double>(v[0], v[1], v[2])));
+                }
+                for (int i = lane; i < sh.nf; i += 32) {
+                    const double* nrm = W.face_normal + 3 * (sh.face_off + i);
+                    tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
+                }
+            } else {
+                M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
+                for (int i = lane; i < sh.nv; i += 32) {
+                    const double* v = W.shape_verts + 3 * (sh.vert_off + i);
+                    tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
+                }
+                for (int i = lane; i < sh.nf; i += 32) {
+                    const double* nrm = W.face_normal + 3 * (sh.face_off + i);
+                    tn[i] = vnorm(mmulv(Rm, v3<R>((R)nrm[0], (R)nrm[1], (R)nrm[2])));
+                }
+            }
+        }
+    }
+    __syncwarp();
+    __threadfence_block();
+    pair_contacts<R, EXACT>(W, sm, a, b, true);
+    double4_32a pa = W.pos[a];
+    int nc = sm.ncontacts;
+    for (int k = lane; k < nc && k < cap; k += 32) {
+        V3<R> p1 = sm.c_r1[k], p2 = sm.c_r2[k], n = sm.c_n[k];
+        double ox = EXACT ? 0.0 : pa.x, oy = EXACT ? 0.0 : pa.y, oz = EXACT ? 0.0 : pa.z;
+        double* o = out + 9 * k;
+        o[0] = (double)p1.x + ox; o[1] = (double)p1.y + oy; o[2] = (double)p1.z + oz;
+        o[3] = (double)p2.x + ox; o[4] = (double)p2.y + oy; o[5] = (double)p2.z + oz;
+        o[6] = (double)n.x; o[7] = (double)n.y; o[8] = (double)n.z;
+    }
+    if (lane == 0) {
+        *count = nc;
+        if (sm.status) atomicOr(&W.status[0], (uint32_t)sm.status);
+    }
+}
+
+template <typename R, bool EXACT>
+struct Launcher {
+    static size_t smem_bytes() { return sizeof(NarrowSmem<R>) * WARPS_PER_BLOCK; }
+
+    static cudaError_t configure() {
+        cudaError_t e = cudaFuncSetAttribute(step_kernel_cta<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(step_kernel_grid<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(contacts_kernel<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(NarrowSmem<R>));
+    }
+
+    static int grid_blocks_per_sm() {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, step_kernel_grid<R, EXACT>, BLOCK, smem_bytes()) != cudaSuccess) return 0;
+        return nb;
+    }
+
+    static cudaError_t step(const WorldView<R>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st) {
+        if (grid) {
+            void* args[] = {(void*)&W, (void*)&P};
+            return cudaLaunchCooperativeKernel((const void*)step_kernel_grid<R, EXACT>, dim3(blocks), dim3(BLOCK), args,
+                                               smem_bytes(), st);
+        }
+        step_kernel_cta<R, EXACT><<<blocks, BLOCK, smem_bytes(), st>>>(W, P);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t broad(const WorldView<R>& W, int s, cudaStream_t st) {
+        broad_kernel<R><<<1, BLOCK, 0, st>>>(W, s);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t contacts(const WorldView<R>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st) {
+        contacts_kernel<R, EXACT><<<1, 32, sizeof(NarrowSmem<R>), st>>>(W, a, b, out, cap, count);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace rp

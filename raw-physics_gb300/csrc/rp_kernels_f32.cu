@@ -1,0 +1,15 @@
+// FP32 build of the step kernels: FP32 arithmetic with FP64 poses and EPA face test.
+#include "rp_kernels.cuh"
+
+namespace rp {
+size_t smem_bytes_f32() { return Launcher<float, false>::smem_bytes(); }
+cudaError_t configure_f32() { return Launcher<float, false>::configure(); }
+int grid_blocks_per_sm_f32() { return Launcher<float, false>::grid_blocks_per_sm(); }
+cudaError_t step_f32(const WorldView<float>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st) {
+    return Launcher<float, false>::step(W, P, grid, blocks, st);
+}
+cudaError_t broad_f32(const WorldView<float>& W, int scene, cudaStream_t st) { return Launcher<float, false>::broad(W, scene, st); }
+cudaError_t contacts_f32(const WorldView<float>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st) {
+    return Launcher<float, false>::contacts(W, a, b, out, cap, count, st);
+}
+}  // namespace rp

@@ -1,0 +1,691 @@
+// Warp-per-pair narrowphase: support mapping, GJK, EPA and contact-manifold clipping.
+//
+// One warp handles one broad-phase pair. The pair's transformed hull vertices are staged in the
+// warp's shared-memory slice; support mapping is a warp argmax; GJK's simplex logic runs
+// redundantly on all lanes; EPA keeps its polytope in shared memory, tests face visibility and
+// builds new faces lane-parallel, and replays the reference's order-dependent bookkeeping (the
+// unordered removal of faces and horizon edges) on lane 0 so that face order — and so every
+// tie-break — is the reference's. Clipping runs Sutherland–Hodgman one plane at a time with one
+// lane per polygon edge and a warp prefix sum to keep the output order.
+//
+// References (raw-physics): support.cpp:5-39, gjk.cpp:7-379, epa.cpp:8-237, clipping.cpp:12-370,
+// collider.cpp:523-571.
+#pragma once
+#include <float.h>
+#include "rp_math.cuh"
+#include "rp_world.h"
+
+namespace rp {
+
+constexpr int WARP = 32;
+constexpr int STAGE_V = 64;      // hull vertices staged per body in shared memory
+constexpr int EPA_MAXV = 104;    // 4 simplex points + at most 100 EPA iterations
+constexpr int EPA_MAXF = 192;    // faces of the EPA polytope
+constexpr int EPA_MAXE = 96;     // horizon edges of one EPA iteration
+constexpr int CLIP_MAX = 96;     // vertices of a clipped polygon
+constexpr int CMAX = 64;         // contacts of one body pair
+
+// Precision policy. R: working type of geometry and solver. EPA face normals, distances and the
+// termination test are always FP64.
+template <bool EXACT> struct Prec;
+template <> struct Prec<false> { typedef float R; static constexpr bool exact = false; };
+template <> struct Prec<true> { typedef double R; static constexpr bool exact = true; };
+
+template <typename R>
+struct NarrowSmem {
+    V3<R> va[STAGE_V];
+    V3<R> vb[STAGE_V];
+    union U {
+        struct {
+            V3<R> poly[EPA_MAXV];
+            V3<double> fn[EPA_MAXF];
+            double fd[EPA_MAXF];
+            uchar4 f[EPA_MAXF];      // x, y, z polytope indices, w = visibility
+            uchar2 e[EPA_MAXE];
+        } epa;
+        struct {
+            V3<R> buf[2][CLIP_MAX];
+            V3<R> pn[CLIP_MAX];      // clip planes: normal
+            V3<R> pp[CLIP_MAX];      // clip planes: point
+            int32_t cand[WARP * 2];  // edge-pair candidates
+        } clip;
+        __device__ U() {}
+    } u;
+    V3<R> c_r1[CMAX];   // contacts of the pair (constraint-ready local offsets)
+    V3<R> c_r2[CMAX];
+    V3<R> c_n[CMAX];
+    int ncontacts;
+    int nf, ne, npoly;
+    int status;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Warp utilities
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// argmax with the reference's "strict >, first index wins" rule (support.cpp:8-14)
+template <typename T>
+__device__ __forceinline__ void warp_argmax_first(T& v, int& idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_xor_sync(0xffffffffu, v, o);
+        int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+}
+template <typename T>
+__device__ __forceinline__ void warp_argmin_first(T& v, int& idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_xor_sync(0xffffffffu, v, o);
+        int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ov < v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+}
+__device__ __forceinline__ int warp_incl_scan(int x) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((int)lane_id() >= o) x += y;
+    }
+    return x;
+}
+
+// ---------------------------------------------------------------------------------------------
+// A collider as seen by the narrowphase: transformed vertices and normals (exact build: world
+// coordinates; FP32 build: rotated about the body origin, plus `off` for the pair-local frame).
+template <typename R>
+struct ColView {
+    int type;
+    R radius;
+    V3<R> center;            // sphere centre (pair frame)
+    V3<R> off;               // translation added to stored vertices (pair frame)
+    const V3<R>* verts;      // stored transformed vertices (shared staging or global)
+    bool staged;             // verts already include `off`
+    const V3<R>* norms;      // transformed face normals (global)
+    int nv, nf;
+    const Shape* shape;
+};
+
+template <typename R>
+__device__ __forceinline__ V3<R> cv_vertex(const ColView<R>& c, int i) {
+    V3<R> v = c.verts[i];
+    if (!c.staged) v = vadd(v, c.off);
+    return v;
+}
+
+// support_point_get_index: warp argmax over the hull's transformed vertices
+template <typename R>
+__device__ int support_index(const ColView<R>& c, V3<R> d) {
+    R best = -(R)DBL_MAX;
+    if (sizeof(R) == 4) best = -FLT_MAX;
+    int bi = 0x7fffffff;
+    for (int i = (int)lane_id(); i < c.nv; i += WARP) {
+        R dot = vdot(cv_vertex(c, i), d);
+        if (dot > best) { best = dot; bi = i; }
+    }
+    warp_argmax_first(best, bi);
+    return bi == 0x7fffffff ? 0 : bi;
+}
+
+template <typename R>
+__device__ V3<R> support_point(const ColView<R>& c, V3<R> d) {
+    if (c.type == COL_HULL) return cv_vertex(c, support_index(c, d));
+    return vadd(c.center, vscale(c.radius, vnorm(d)));
+}
+
+template <typename R>
+__device__ __forceinline__ V3<R> support_mink(const ColView<R>& a, const ColView<R>& b, V3<R> d) {
+    V3<R> s1 = support_point(a, d);
+    V3<R> s2 = support_point(b, vscale((R)-1.0, d));
+    return vsub(s1, s2);
+}
+
+// ---------------------------------------------------------------------------------------------
+// GJK (gjk.cpp:7-379); all lanes hold the same simplex.
+template <typename R>
+struct Simplex { V3<R> a, b, c, d; int num; };
+
+template <typename R>
+__device__ __forceinline__ V3<R> triple_cross(V3<R> a, V3<R> b, V3<R> c) { return vcross(vcross(a, b), c); }
+
+template <typename R>
+__device__ bool do_simplex(Simplex<R>& s, V3<R>& dir) {
+    const R zero = 0;
+    if (s.num == 2) {
+        V3<R> a = s.a, b = s.b, ao = vinv(a), ab = vsub(b, a);
+        if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+        else { s.a = a; s.num = 1; dir = ao; }
+        return false;
+    }
+    if (s.num == 3) {
+        V3<R> a = s.a, b = s.b, c = s.c;
+        V3<R> ao = vinv(a), ab = vsub(b, a), ac = vsub(c, a), abc = vcross(ab, ac);
+        if (vdot(vcross(abc, ac), ao) >= zero) {
+            if (vdot(ac, ao) >= zero) { s.a = a; s.b = c; s.num = 2; dir = triple_cross(ac, ao, ac); }
+            else if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+            else { s.a = a; dir = ao; }
+        } else {
+            if (vdot(vcross(ab, abc), ao) >= zero) {
+                if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+                else { s.a = a; dir = ao; }
+            } else {
+                if (vdot(abc, ao) >= zero) { s.a = a; s.b = b; s.c = c; s.num = 3; dir = abc; }
+                else { s.a = a; s.b = c; s.c = b; s.num = 3; dir = vinv(abc); }
+            }
+        }
+        return false;
+    }
+    V3<R> a = s.a, b = s.b, c = s.c, d = s.d;
+    V3<R> ao = vinv(a), ab = vsub(b, a), ac = vsub(c, a), ad = vsub(d, a);
+    V3<R> abc = vcross(ab, ac), acd = vcross(ac, ad), adb = vcross(ad, ab);
+    int info = 0;
+    if (vdot(abc, ao) >= zero) info |= 1;
+    if (vdot(acd, ao) >= zero) info |= 2;
+    if (vdot(adb, ao) >= zero) info |= 4;
+    switch (info) {
+    case 0: return true;
+    case 1:
+        if (vdot(vcross(abc, ac), ao) >= zero) {
+            if (vdot(ac, ao) >= zero) { s.a = a; s.b = c; s.num = 2; dir = triple_cross(ac, ao, ac); }
+            else if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+            else { s.a = a; dir = ao; }
+        } else {
+            if (vdot(vcross(ab, abc), ao) >= zero) {
+                if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+                else { s.a = a; dir = ao; }
+            } else { s.a = a; s.b = b; s.c = c; s.num = 3; dir = abc; }
+        }
+        break;
+    case 2:
+        if (vdot(vcross(acd, ad), ao) >= zero) {
+            if (vdot(ad, ao) >= zero) { s.a = a; s.b = d; s.num = 2; dir = triple_cross(ad, ao, ad); }
+            else if (vdot(ac, ao) >= zero) {
+                // the reference pairs the AC simplex with the AB search direction here (gjk.cpp:213)
+                s.a = a; s.b = c; s.num = 2; dir = triple_cross(ab, ao, ab);
+            } else { s.a = a; dir = ao; }
+        } else {
+            if (vdot(vcross(ac, acd), ao) >= zero) {
+                if (vdot(ac, ao) >= zero) { s.a = a; s.b = c; s.num = 2; dir = triple_cross(ac, ao, ac); }
+                else { s.a = a; dir = ao; }
+            } else { s.a = a; s.b = c; s.c = d; s.num = 3; dir = acd; }
+        }
+        break;
+    case 3:
+        if (vdot(ac, ao) >= zero) { s.a = a; s.b = c; s.num = 2; dir = triple_cross(ac, ao, ac); }
+        else { s.a = a; s.num = 1; dir = ao; }
+        break;
+    case 4:
+        if (vdot(vcross(adb, ab), ao) >= zero) {
+            if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+            else if (vdot(ad, ao) >= zero) { s.a = a; s.b = d; s.num = 2; dir = triple_cross(ad, ao, ad); }
+            else { s.a = a; dir = ao; }
+        } else {
+            if (vdot(vcross(ad, adb), ao) >= zero) {
+                if (vdot(ad, ao) >= zero) { s.a = a; s.b = d; s.num = 2; dir = triple_cross(ad, ao, ad); }
+                else { s.a = a; dir = ao; }
+            } else { s.a = a; s.b = d; s.c = b; s.num = 3; dir = adb; }
+        }
+        break;
+    case 5:
+        if (vdot(ab, ao) >= zero) { s.a = a; s.b = b; s.num = 2; dir = triple_cross(ab, ao, ab); }
+        else { s.a = a; s.num = 1; dir = ao; }
+        break;
+    case 6:
+        if (vdot(ad, ao) >= zero) { s.a = a; s.b = d; s.num = 2; dir = triple_cross(ad, ao, ad); }
+        else { s.a = a; s.num = 1; dir = ao; }
+        break;
+    default: s.a = a; s.num = 1; dir = ao; break;
+    }
+    return false;
+}
+
+template <typename R>
+__device__ bool gjk_collides(const ColView<R>& c1, const ColView<R>& c2, Simplex<R>& s, int& iters) {
+    s.a = support_mink(c1, c2, v3<R>(0, 0, 1));
+    s.b = s.c = s.d = v3<R>(0, 0, 0);
+    s.num = 1;
+    V3<R> dir = vscale((R)-1.0, s.a);
+    for (int i = 0; i < 100; ++i) {
+        iters = i + 1;
+        V3<R> p = support_mink(c1, c2, dir);
+        if (vdot(p, dir) < (R)0) return false;
+        if (s.num == 1) { s.b = s.a; s.a = p; }
+        else if (s.num == 2) { s.c = s.b; s.b = s.a; s.a = p; }
+        else { s.d = s.c; s.c = s.b; s.b = s.a; s.a = p; }
+        s.num++;
+        if (do_simplex(s, dir)) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------
+// EPA (epa.cpp:8-237)
+template <typename R>
+__device__ void epa_face(NarrowSmem<R>& sm, int fi, int npoly) {
+    uchar4 f = sm.u.epa.f[fi];
+    V3<double> a = v3cast<double>(sm.u.epa.poly[f.x]), b = v3cast<double>(sm.u.epa.poly[f.y]),
+               c = v3cast<double>(sm.u.epa.poly[f.z]);
+    V3<double> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
+    if (!(n.x != 0.0 || n.y != 0.0 || n.z != 0.0)) atomicOr(&sm.status, (int)ST_DEGENERATE);
+    double d = vdot(n, a);
+    if (d < -0.0) {
+        n = vinv(n);
+        d = -d;
+    } else if (d >= -0.0 && d <= 0.0) {
+        bool ok = false;
+        for (int i = 0; i < npoly; ++i) {
+            double ad = vdot(n, v3cast<double>(sm.u.epa.poly[i]));
+            if (ad < -0.0 || ad > 0.0) {
+                n = ad < -0.0 ? n : vinv(n);
+                ok = true;
+                break;
+            }
+        }
+        if (!ok) atomicOr(&sm.status, (int)ST_DEGENERATE);
+    }
+    sm.u.epa.fn[fi] = n;
+    sm.u.epa.fd[fi] = d;
+}
+
+template <typename R>
+__device__ bool epa_edge_equal(const NarrowSmem<R>& sm, uchar2 cur, uchar2 e) {
+    if ((e.x == cur.x && e.y == cur.y) || (e.x == cur.y && e.y == cur.x)) return true;
+    V3<R> c1 = sm.u.epa.poly[cur.x], c2 = sm.u.epa.poly[cur.y], e1 = sm.u.epa.poly[e.x], e2 = sm.u.epa.poly[e.y];
+    if (veq(c1, e1) && veq(c2, e2)) return true;
+    if (veq(c1, e2) && veq(c2, e1)) return true;
+    return false;
+}
+
+template <typename R>
+__device__ void epa_add_edge(NarrowSmem<R>& sm, uchar2 e) {
+    int ne = sm.ne;
+    for (int i = 0; i < ne; ++i) {
+        if (epa_edge_equal(sm, sm.u.epa.e[i], e)) {
+            ne--;
+            sm.u.epa.e[i] = sm.u.epa.e[ne];
+            sm.ne = ne;
+            return;
+        }
+    }
+    if (ne >= EPA_MAXE) { atomicOr(&sm.status, (int)ST_EPA_OVERFLOW); return; }
+    sm.u.epa.e[ne] = e;
+    sm.ne = ne + 1;
+}
+
+// Returns true when converged; normal and penetration are then set (FP64).
+template <typename R>
+__device__ bool epa(NarrowSmem<R>& sm, const ColView<R>& c1, const ColView<R>& c2, const Simplex<R>& s,
+                    V3<double>& out_n, double& out_pen, int& iters) {
+    const unsigned lane = lane_id();
+    if (lane == 0) {
+        sm.u.epa.poly[0] = s.a; sm.u.epa.poly[1] = s.b; sm.u.epa.poly[2] = s.c; sm.u.epa.poly[3] = s.d;
+        sm.u.epa.f[0] = make_uchar4(0, 1, 2, 0);
+        sm.u.epa.f[1] = make_uchar4(0, 2, 3, 0);
+        sm.u.epa.f[2] = make_uchar4(0, 3, 1, 0);
+        sm.u.epa.f[3] = make_uchar4(1, 2, 3, 0);
+        sm.nf = 4;
+        sm.npoly = 4;
+    }
+    __syncwarp();
+    if (lane < 4) epa_face(sm, (int)lane, 4);
+    __syncwarp();
+    // min over the initial faces, strict < with the first minimum kept (epa.cpp:141-144)
+    double md = DBL_MAX;
+    int mi = 0x7fffffff;
+    for (int i = (int)lane; i < sm.nf; i += WARP)
+        if (sm.u.epa.fd[i] < md) { md = sm.u.epa.fd[i]; mi = i; }
+    warp_argmin_first(md, mi);
+    V3<double> min_n = (mi == 0x7fffffff) ? v3<double>(0, 0, 0) : sm.u.epa.fn[mi];
+    double min_d = md;
+    for (int it = 0; it < 100; ++it) {
+        iters = it + 1;
+        V3<R> sp = support_mink(c1, c2, v3cast<R>(min_n));
+        V3<double> spd = v3cast<double>(sp);
+        double d = vdot(min_n, spd);
+        if (fabs(d - min_d) < 0.0001) {
+            out_n = min_n;
+            out_pen = min_d;
+            return true;
+        }
+        int np = sm.npoly;
+        if (np >= EPA_MAXV) {
+            if (lane == 0) atomicOr(&sm.status, (int)ST_EPA_OVERFLOW);
+            __syncwarp();
+            return false;
+        }
+        __syncwarp();
+        if (lane == 0) { sm.u.epa.poly[np] = sp; sm.npoly = np + 1; sm.ne = 0; }
+        // visibility of every face, lane-parallel (independent of the removal order)
+        int nf = sm.nf;
+        for (int i = (int)lane; i < nf; i += WARP) {
+            uchar4 f = sm.u.epa.f[i];
+            V3<double> cen = vadd(vadd(v3cast<double>(sm.u.epa.poly[f.y]), v3cast<double>(sm.u.epa.poly[f.z])),
+                                  v3cast<double>(sm.u.epa.poly[f.x]));
+            cen = vscale(1.0 / 3.0, cen);
+            f.w = vdot(sm.u.epa.fn[i], vsub(spd, cen)) > 0.0 ? 1 : 0;
+            sm.u.epa.f[i] = f;
+        }
+        __syncwarp();
+        // the reference's removal loop: unordered remove, re-test the moved face (epa.cpp:167-197)
+        if (lane == 0) {
+            int i = 0;
+            while (i < nf) {
+                uchar4 f = sm.u.epa.f[i];
+                if (f.w) {
+                    epa_add_edge(sm, make_uchar2(f.x, f.y));
+                    epa_add_edge(sm, make_uchar2(f.y, f.z));
+                    epa_add_edge(sm, make_uchar2(f.z, f.x));
+                    nf--;
+                    sm.u.epa.f[i] = sm.u.epa.f[nf];
+                    sm.u.epa.fd[i] = sm.u.epa.fd[nf];
+                    sm.u.epa.fn[i] = sm.u.epa.fn[nf];
+                } else {
+                    ++i;
+                }
+            }
+            if (nf + sm.ne > EPA_MAXF) atomicOr(&sm.status, (int)ST_EPA_OVERFLOW);
+            sm.nf = nf;
+        }
+        __syncwarp();
+        if (sm.status & ST_EPA_OVERFLOW) return false;
+        nf = sm.nf;
+        int ne = sm.ne;
+        for (int i = (int)lane; i < ne; i += WARP) {
+            uchar2 e = sm.u.epa.e[i];
+            sm.u.epa.f[nf + i] = make_uchar4(e.x, e.y, (unsigned char)np, 0);
+            epa_face(sm, nf + i, np + 1);
+        }
+        __syncwarp();
+        if (lane == 0) sm.nf = nf + ne;
+        nf += ne;
+        md = DBL_MAX;
+        mi = 0x7fffffff;
+        for (int i = (int)lane; i < nf; i += WARP)
+            if (sm.u.epa.fd[i] < md) { md = sm.u.epa.fd[i]; mi = i; }
+        warp_argmin_first(md, mi);
+        min_d = md;
+        if (mi != 0x7fffffff) min_n = sm.u.epa.fn[mi];
+        __syncwarp();
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Clipping (clipping.cpp)
+template <typename R>
+__device__ __forceinline__ bool in_plane(V3<R> pn, V3<R> pp, V3<R> pos) {
+    float distance = -vdot(pn, pp);
+    return !(vdot(pos, pn) + (R)distance < (R)0.0);
+}
+
+template <typename R>
+__device__ __forceinline__ bool plane_edge(V3<R> pn, V3<R> pp, V3<R> start, V3<R> end, V3<R>& out) {
+    V3<R> ab = vsub(end, start);
+    float ab_p = vdot(pn, ab);
+    if ((double)fabsf(ab_p) > 0.000001) {
+        float distance = -vdot(pn, pp);
+        V3<R> p_co = vscale((R)(-distance), pn);
+        float fac = -vdot(pn, vsub(start, p_co)) / (R)ab_p;
+        R mx = ((R)fac > (R)0.0) ? (R)fac : (R)0.0;
+        fac = (float)((mx < (R)1.0) ? mx : (R)1.0);
+        out = vadd(start, vscale((R)fac, ab));
+        return true;
+    }
+    return false;
+}
+
+// One Sutherland–Hodgman pass against one plane, one lane per polygon edge. Returns the output count.
+template <typename R>
+__device__ int sh_pass(const V3<R>* in, int n, V3<R>* out, V3<R> pn, V3<R> pp, bool remove_only, int& status) {
+    const unsigned lane = lane_id();
+    int carry = 0;
+    for (int base = 0; base < n; base += WARP) {
+        int j = base + (int)lane;
+        int cnt = 0;
+        V3<R> o0 = v3<R>(0, 0, 0), o1 = v3<R>(0, 0, 0);
+        if (j < n) {
+            V3<R> end = in[j];
+            V3<R> start = in[j == 0 ? n - 1 : j - 1];
+            bool si = in_plane(pn, pp, start), ei = in_plane(pn, pp, end);
+            if (remove_only) {
+                if (ei) { o0 = end; cnt = 1; }
+            } else if (si && ei) {
+                o0 = end; cnt = 1;
+            } else if (si && !ei) {
+                V3<R> t;
+                if (plane_edge(pn, pp, start, end, t)) { o0 = t; cnt = 1; }
+            } else if (!si && ei) {
+                V3<R> t;
+                if (plane_edge(pn, pp, start, end, t)) { o0 = t; o1 = end; cnt = 2; }
+                else { o0 = end; cnt = 1; }
+            }
+        }
+        int incl = warp_incl_scan(cnt);
+        int pos = carry + incl - cnt;
+        if (cnt >= 1) { if (pos < CLIP_MAX) out[pos] = o0; else status |= ST_CLIP_OVERFLOW; }
+        if (cnt == 2) { if (pos + 1 < CLIP_MAX) out[pos + 1] = o1; else status |= ST_CLIP_OVERFLOW; }
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+    return carry < CLIP_MAX ? carry : CLIP_MAX;
+}
+
+template <typename R, bool EXACT>
+struct PairFrame {
+    // maps a contact point pair to constraint-local offsets r1_lc, r2_lc
+    Qt<R> q1inv, q2inv;
+    V3<R> x1, x2;     // body origins in the pair frame
+    bool raw;         // keep the contact points themselves (known-answer queries)
+};
+
+template <typename R, bool EXACT>
+__device__ void push_contact(NarrowSmem<R>& sm, const PairFrame<R, EXACT>& fr, V3<R> p1, V3<R> p2, V3<R> n, bool pred) {
+    // clipping_contact_to_collision_constraint (pbd.cpp:408-424), compacted in warp order
+    unsigned m = __ballot_sync(0xffffffffu, pred);
+    int base = sm.ncontacts;
+    int pos = base + __popc(m & ((1u << lane_id()) - 1u));
+    if (pred) {
+        if (pos < CMAX) {
+            sm.c_r1[pos] = fr.raw ? p1 : qrotate(fr.q1inv, vsub(p1, fr.x1));
+            sm.c_r2[pos] = fr.raw ? p2 : qrotate(fr.q2inv, vsub(p2, fr.x2));
+            sm.c_n[pos] = n;
+        } else {
+            atomicOr(&sm.status, (int)ST_CONTACT_OVERFLOW);
+        }
+    }
+    __syncwarp();
+    if (lane_id() == 0) sm.ncontacts = min(base + __popc(m), CMAX);
+    __syncwarp();
+}
+
+template <typename R>
+__device__ __forceinline__ int csr_len(const int32_t* start, int row) { return start[row + 1] - start[row]; }
+
+// convex_convex_contact_manifold (clipping.cpp:249-341)
+template <typename R, bool EXACT>
+__device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& h1, const ColView<R>& h2,
+                                       V3<R> normal, const PairFrame<R, EXACT>& fr) {
+    const unsigned lane = lane_id();
+    V3<R> inv_n = vinv(normal);
+    int s1 = support_index(h1, normal);
+    int s2 = support_index(h2, inv_n);
+    const int32_t* cs = W.csr_start;
+    const int32_t* cd = W.csr_data;
+    // get_face_with_most_fitting_normal over vertex_to_faces (first max wins)
+    int v2f1 = h1.shape->v2f_off + s1, v2f2 = h2.shape->v2f_off + s2;
+    R best1 = sizeof(R) == 4 ? -FLT_MAX : -(R)DBL_MAX, best2 = best1;
+    int f1 = 0x7fffffff, f2 = 0x7fffffff;
+    for (int k = (int)lane; k < csr_len<R>(cs, v2f1); k += WARP) {
+        int fi = cd[cs[v2f1] + k];
+        R p = vdot(h1.norms[fi], normal);
+        if (p > best1) { best1 = p; f1 = k; }
+    }
+    for (int k = (int)lane; k < csr_len<R>(cs, v2f2); k += WARP) {
+        int fi = cd[cs[v2f2] + k];
+        R p = vdot(h2.norms[fi], inv_n);
+        if (p > best2) { best2 = p; f2 = k; }
+    }
+    warp_argmax_first(best1, f1);
+    warp_argmax_first(best2, f2);
+    f1 = cd[cs[v2f1] + (f1 == 0x7fffffff ? 0 : f1)];
+    f2 = cd[cs[v2f2] + (f2 == 0x7fffffff ? 0 : f2)];
+    V3<R> n1 = h1.norms[f1], n2 = h2.norms[f2];
+    // get_edge_with_most_fitting_normal: candidates in (i, j, normal / inverted) order
+    int v2n1 = h1.shape->v2n_off + s1, v2n2 = h2.shape->v2n_off + s2;
+    int nn1 = csr_len<R>(cs, v2n1), nn2 = csr_len<R>(cs, v2n2);
+    V3<R> sp1 = cv_vertex(h1, s1), sp2 = cv_vertex(h2, s2);
+    R bestE = sizeof(R) == 4 ? -FLT_MAX : -(R)DBL_MAX;
+    int bestK = 0x7fffffff;
+    for (int k = (int)lane; k < nn1 * nn2; k += WARP) {
+        int i = k / nn2, j = k % nn2;
+        V3<R> e1 = vsub(sp1, cv_vertex(h1, cd[cs[v2n1] + i]));
+        V3<R> e2 = vsub(sp2, cv_vertex(h2, cd[cs[v2n2] + j]));
+        V3<R> cn = vnorm(vcross(e1, e2));
+        V3<R> ci = vinv(cn);
+        R d0 = vdot(cn, normal);
+        if (d0 > bestE) { bestE = d0; bestK = 2 * k; }
+        R d1 = vdot(ci, normal);
+        if (d1 > bestE) { bestE = d1; bestK = 2 * k + 1; }
+    }
+    warp_argmax_first(bestE, bestK);
+    V3<R> edge_normal = v3<R>(0, 0, 0);
+    int ei = 0, ej = 0;
+    if (bestK != 0x7fffffff) {
+        int k = bestK >> 1;
+        ei = cd[cs[v2n1] + k / nn2];
+        ej = cd[cs[v2n2] + k % nn2];
+        V3<R> e1 = vsub(sp1, cv_vertex(h1, ei));
+        V3<R> e2 = vsub(sp2, cv_vertex(h2, ej));
+        edge_normal = vnorm(vcross(e1, e2));
+        if (bestK & 1) edge_normal = vinv(edge_normal);
+    }
+    R d1 = vdot(n1, normal), d2 = vdot(n2, inv_n), de = vdot(edge_normal, normal);
+    if (de > d1 + (R)0.0001 && de > d2 + (R)0.0001) {
+        // collision_distance_between_skew_lines (clipping.cpp:210-239)
+        V3<R> p1 = sp1, dd1 = vsub(cv_vertex(h1, ei), p1);
+        V3<R> p2 = sp2, dd2 = vsub(cv_vertex(h2, ej), p2);
+        R nA = dd1.x * dd2.x + dd1.y * dd2.y + dd1.z * dd2.z;
+        R nB = dd2.x * dd2.x + dd2.y * dd2.y + dd2.z * dd2.z;
+        R mA = -dd1.x * dd1.x - dd1.y * dd1.y - dd1.z * dd1.z;
+        R mB = -dd2.x * dd1.x - dd2.y * dd1.y - dd2.z * dd1.z;
+        R rA = -dd1.x * p2.x + dd1.x * p1.x - dd1.y * p2.y + dd1.y * p1.y - dd1.z * p2.z + dd1.z * p1.z;
+        R rB = -dd2.x * p2.x + dd2.x * p1.x - dd2.y * p2.y + dd2.y * p1.y - dd2.z * p2.z + dd2.z * p1.z;
+        R den = (nA * mB) - (nB * mA);
+        bool ok = den != (R)0;
+        if (!ok && lane == 0) atomicOr(&sm.status, (int)ST_DEGENERATE);
+        R nn = ok ? ((rA * mB) - (rB * mA)) / den : (R)0;
+        R mm = ok ? ((nA * rB) - (nB * rA)) / den : (R)0;
+        V3<R> l1 = vadd(p1, vscale(mm, dd1));
+        V3<R> l2 = vadd(p2, vscale(nn, dd2));
+        push_contact(sm, fr, l1, l2, normal, ok && lane == 0);
+        return;
+    }
+    bool ref1 = d1 > d2;
+    const ColView<R>& rh = ref1 ? h1 : h2;
+    const ColView<R>& ih = ref1 ? h2 : h1;
+    int rf = ref1 ? f1 : f2, inf = ref1 ? f2 : f1;
+    const int32_t* fes = W.face_elem_start;
+    // incident polygon and boundary planes (build_boundary_planes, clipping.cpp:121-134)
+    int fs_i = fes[ih.shape->face_off + inf];
+    int fe_i = fes[ih.shape->face_off + inf + 1];
+    int ninc = fe_i - fs_i;
+    if (ninc > CLIP_MAX) { if (lane == 0) atomicOr(&sm.status, (int)ST_CLIP_OVERFLOW); ninc = CLIP_MAX; }
+    for (int k = (int)lane; k < ninc; k += WARP) sm.u.clip.buf[0][k] = cv_vertex(ih, W.face_elem[fs_i + k]);
+    int f2n_row = rh.shape->f2n_off + rf;
+    int npl = csr_len<R>(cs, f2n_row);
+    if (npl > CLIP_MAX) { if (lane == 0) atomicOr(&sm.status, (int)ST_CLIP_OVERFLOW); npl = CLIP_MAX; }
+    for (int k = (int)lane; k < npl; k += WARP) {
+        int nf = cd[cs[f2n_row] + k];
+        sm.u.clip.pp[k] = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + nf]]);
+        sm.u.clip.pn[k] = vinv(rh.norms[nf]);
+    }
+    __syncwarp();
+    int st = 0;
+    int n = ninc, cur = 0;
+    for (int p = 0; p < npl; ++p) {
+        if (n == 0) break;
+        n = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], sm.u.clip.pn[p], sm.u.clip.pp[p], false, st);
+        cur ^= 1;
+    }
+    V3<R> ref_n = vinv(rh.norms[rf]);
+    V3<R> ref_p = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + rf]]);
+    if (n > 0) {
+        n = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], ref_n, ref_p, true, st);
+        cur ^= 1;
+    }
+    if (st && lane == 0) atomicOr(&sm.status, (int)st);
+    // contacts from the kept points (clipping.cpp:302-327)
+    for (int base = 0; base < n; base += WARP) {
+        int k = base + (int)lane;
+        bool pred = false;
+        V3<R> c1 = v3<R>(0, 0, 0), c2 = v3<R>(0, 0, 0);
+        if (k < n) {
+            V3<R> pt = sm.u.clip.buf[cur][k];
+            R dd = vdot(vscale((R)-1.0, ref_n), ref_p);
+            V3<R> cp = vsub(pt, vscale(vdot(ref_n, pt) + dd, ref_n));
+            V3<R> diff = vsub(pt, cp);
+            R pen;
+            if (ref1) {
+                pen = vdot(diff, normal);
+                c1 = vsub(pt, vscale(pen, normal));
+                c2 = pt;
+            } else {
+                pen = -vdot(diff, normal);
+                c1 = pt;
+                c2 = vadd(pt, vscale(pen, normal));
+            }
+            pred = pen < (R)0.0;
+        }
+        push_contact(sm, fr, c1, c2, normal, pred);
+    }
+}
+
+// clipping_get_contact_manifold (clipping.cpp:343-370)
+template <typename R, bool EXACT>
+__device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& c1, const ColView<R>& c2,
+                                 V3<R> normal, R pen, const PairFrame<R, EXACT>& fr) {
+    if (c1.type == COL_SPHERE) {
+        V3<R> sp = support_point(c1, normal);
+        push_contact(sm, fr, sp, vsub(sp, vscale(pen, normal)), normal, lane_id() == 0);
+    } else if (c2.type == COL_SPHERE) {
+        V3<R> sp = support_point(c2, vinv(normal));
+        push_contact(sm, fr, vadd(sp, vscale(pen, normal)), sp, normal, lane_id() == 0);
+    } else {
+        convex_convex_manifold<R, EXACT>(sm, W, c1, c2, normal, fr);
+    }
+}
+
+// collider_get_contacts (collider.cpp:523-558)
+template <typename R, bool EXACT>
+__device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& c1, const ColView<R>& c2,
+                                  const PairFrame<R, EXACT>& fr, unsigned long long* counters) {
+    if (c1.type == COL_SPHERE && c2.type == COL_SPHERE) {
+        V3<R> dv = vsub(c1.center, c2.center);
+        float dsq = vdot(dv, dv);
+        float mind = (float)c1.radius + (float)c2.radius;
+        if (dsq < (mind * mind)) {
+            V3<R> normal = vnorm(vsub(c2.center, c1.center));
+            R pen = (R)(float)(mind - sqrtf(dsq));
+            contact_manifold<R, EXACT>(sm, W, c1, c2, normal, pen, fr);
+        }
+        return;
+    }
+    Simplex<R> s;
+    int gi = 0, ei = 0;
+    bool hit = gjk_collides(c1, c2, s, gi);
+    if (counters && lane_id() == 0) atomicAdd(&counters[0], (unsigned long long)gi);
+    if (!hit) return;
+    V3<double> n;
+    double pen;
+    bool ok = epa(sm, c1, c2, s, n, pen, ei);
+    if (counters && lane_id() == 0) { atomicAdd(&counters[1], (unsigned long long)ei); atomicAdd(&counters[2], 1ull); }
+    if (!ok) {
+        if (lane_id() == 0) atomicOr(&sm.status, (int)ST_EPA_NOT_CONVERGED);
+        __syncwarp();
+        return;
+    }
+    contact_manifold<R, EXACT>(sm, W, c1, c2, v3cast<R>(n), (R)pen, fr);
+}
+
+}  // namespace rp

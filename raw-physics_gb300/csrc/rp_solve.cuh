@@ -1,0 +1,406 @@
+// XPBD constraint solves, integration and velocity passes on the device.
+//
+// Bodies touched by one solver node (a broad-phase pair with its contacts, or one external joint)
+// are loaded into registers, updated in the order the reference applies its corrections, and
+// written back once; nodes of one level never share a non-fixed body, so no two threads write the
+// same body.
+//
+// EXACT=true mirrors the reference's FP64 expressions term for term (built without FMA
+// contraction it reproduces the reference bit for bit). EXACT=false keeps positions and
+// orientations in FP64 and does the rest in FP32, forming position differences in FP64 before
+// rounding so that precision does not depend on the distance from the world origin.
+//
+// References (raw-physics): pbd.cpp:81-406 (solves), :537-577 (predict), :623-643 (velocity
+// update), :646-740 (velocity solver); pbd_base_constraints.cpp:6-227; physics_util.cpp:5-63.
+#pragma once
+#include "rp_math.cuh"
+#include "rp_world.h"
+
+namespace rp {
+
+constexpr double PI_REF = 3.14159265358979;   // PI_F of include/gm.h:8
+
+template <typename R>
+struct Body {
+    V3<double> x;
+    Qt<double> q;
+    R invm;
+    M3<R> Iinv;       // local inverse inertia
+    bool fixed;
+    int idx;
+};
+
+template <typename R>
+__device__ __forceinline__ Body<R> load_body(const WorldView<R>& W, int b) {
+    Body<R> B;
+    double4_32a p = W.pos[b], q = W.rot[b];
+    B.x = v3<double>(p.x, p.y, p.z);
+    B.q = qt<double>(q.x, q.y, q.z, q.w);
+    B.invm = W.inv_mass[b];
+    R s[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] = W.inv_inertia[6 * b + i];
+    B.Iinv = msym(s);
+    B.fixed = W.fixed[b] != 0;
+    B.idx = b;
+    return B;
+}
+
+template <typename R>
+__device__ __forceinline__ void store_pose(const WorldView<R>& W, const Body<R>& B) {
+    if (B.fixed) return;
+    W.pos[B.idx] = make_double4_32a(B.x.x, B.x.y, B.x.z, 0.0);
+    W.rot[B.idx] = make_double4_32a(B.q.x, B.q.y, B.q.z, B.q.w);
+}
+
+// Rotation used for the working-precision algebra of a body.
+template <typename R>
+__device__ __forceinline__ Qt<R> wq(const Qt<double>& q) { return qcast<R>(q); }
+
+// --------------------------------------------------------------------------------------------
+// Position_Constraint_Preprocessed_Data / positional constraint (pbd_base_constraints.cpp:6-123)
+template <typename R>
+struct Pcpd {
+    V3<R> r1, r2;      // r_wc
+    M3<R> I1, I2;      // world inverse inertia
+};
+
+template <typename R>
+__device__ __forceinline__ Pcpd<R> pcpd(const Body<R>& a, const Body<R>& b, V3<R> r1_lc, V3<R> r2_lc) {
+    Pcpd<R> p;
+    Qt<R> qa = wq<R>(a.q), qb = wq<R>(b.q);
+    p.r1 = qrotate(qa, r1_lc);
+    p.r2 = qrotate(qb, r2_lc);
+    p.I1 = world_tensor(qa, a.Iinv);
+    p.I2 = world_tensor(qb, b.Iinv);
+    return p;
+}
+
+template <typename R>
+__device__ __forceinline__ R pos_dlambda(const Body<R>& a, const Body<R>& b, const Pcpd<R>& p, R h, R compliance, R lambda,
+                                         V3<R> dx) {
+    R c = vlen(dx);
+    if (c <= Tiny<R>::v) return (R)0;
+    V3<R> n = v3<R>(dx.x / c, dx.y / c, dx.z / c);
+    R w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
+    R w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    R til = compliance / (h * h);
+    return (-c - til * lambda) / (w1 + w2 + til);
+}
+
+// q <- normalize(q + s * dq): the linearised orientation update, accumulated in FP64
+template <typename R>
+__device__ __forceinline__ void q_add_normalize(Qt<double>& q, Qt<R> d, double s) {
+    if (sizeof(R) == 8) {
+        q.x = q.x + s * (double)d.x; q.y = q.y + s * (double)d.y; q.z = q.z + s * (double)d.z; q.w = q.w + s * (double)d.w;
+    } else {
+        q.x = q.x + (double)((R)s * d.x); q.y = q.y + (double)((R)s * d.y);
+        q.z = q.z + (double)((R)s * d.z); q.w = q.w + (double)((R)s * d.w);
+    }
+    q = qnormalize(q);
+}
+
+template <typename R>
+__device__ __forceinline__ void pos_apply(Body<R>& a, Body<R>& b, const Pcpd<R>& p, R dl, V3<R> dx) {
+    R c = vlen(dx);
+    if (c <= Tiny<R>::v) return;
+    V3<R> n = v3<R>(dx.x / c, dx.y / c, dx.z / c);
+    V3<R> imp = vscale(dl, n);
+    if (!a.fixed) a.x = vadd(a.x, v3cast<double>(vscale(a.invm, imp)));
+    if (!b.fixed) b.x = vadd(b.x, v3cast<double>(vscale(-b.invm, imp)));
+    V3<R> a1 = mmulv(p.I1, vcross(p.r1, imp));
+    V3<R> a2 = mmulv(p.I2, vcross(p.r2, imp));
+    Qt<R> q1 = qmul(qt<R>(a1.x, a1.y, a1.z, (R)0), wq<R>(a.q));
+    Qt<R> q2 = qmul(qt<R>(a2.x, a2.y, a2.z, (R)0), wq<R>(b.q));
+    if (!a.fixed) q_add_normalize(a.q, q1, 0.5);
+    if (!b.fixed) q_add_normalize(b.q, q2, -0.5);
+}
+
+// Angular constraint (pbd_base_constraints.cpp:125-227)
+template <typename R>
+struct Acpd { M3<R> I1, I2; };
+
+template <typename R>
+__device__ __forceinline__ Acpd<R> acpd(const Body<R>& a, const Body<R>& b) {
+    Acpd<R> r;
+    r.I1 = world_tensor(wq<R>(a.q), a.Iinv);
+    r.I2 = world_tensor(wq<R>(b.q), b.Iinv);
+    return r;
+}
+
+template <typename R>
+__device__ __forceinline__ R ang_dlambda(const Acpd<R>& A, R h, R compliance, R lambda, V3<R> dq) {
+    R th = vlen(dq);
+    if (th <= Tiny<R>::v) return (R)0;
+    V3<R> n = v3<R>(dq.x / th, dq.y / th, dq.z / th);
+    R w1 = vdot(n, mmulv(A.I1, n));
+    R w2 = vdot(n, mmulv(A.I2, n));
+    R til = compliance / (h * h);
+    return (-th - til * lambda) / (w1 + w2 + til);
+}
+
+template <typename R>
+__device__ __forceinline__ void ang_apply(Body<R>& a, Body<R>& b, const Acpd<R>& A, R dl, V3<R> dq) {
+    R th = vlen(dq);
+    if (th <= Tiny<R>::v) return;
+    V3<R> n = v3<R>(dq.x / th, dq.y / th, dq.z / th);
+    V3<R> imp = vscale(-dl, n);
+    V3<R> a1 = mmulv(A.I1, imp);
+    V3<R> a2 = mmulv(A.I2, imp);
+    Qt<R> q1 = qmul(qt<R>(a1.x, a1.y, a1.z, (R)0), wq<R>(a.q));
+    Qt<R> q2 = qmul(qt<R>(a2.x, a2.y, a2.z, (R)0), wq<R>(b.q));
+    if (!a.fixed) q_add_normalize(a.q, q1, 0.5);
+    if (!b.fixed) q_add_normalize(b.q, q2, -0.5);
+}
+
+// x_a + r_a - (x_b + r_b), with the position difference formed in FP64 in the FP32 build
+template <typename R, bool EXACT>
+__device__ __forceinline__ V3<R> anchor_delta(const Body<R>& a, const Body<R>& b, V3<R> ra, V3<R> rb) {
+    if (EXACT) return v3cast<R>(vsub(vadd(a.x, v3cast<double>(ra)), vadd(b.x, v3cast<double>(rb))));
+    return vadd(v3cast<R>(vsub(a.x, b.x)), vsub(ra, rb));
+}
+
+// --------------------------------------------------------------------------------------------
+// collision_constraint_solve (pbd.cpp:107-154). c points at the contact record
+// {r1_lc, lambda_n, r2_lc, lambda_t, normal, -}.
+template <typename R, bool EXACT>
+__device__ void collision_solve(const WorldView<R>& W, Body<R>& a, Body<R>& b, R* c, R h, const R mus) {
+    V3<R> r1 = v3<R>(c[0], c[1], c[2]), r2 = v3<R>(c[4], c[5], c[6]), n = v3<R>(c[8], c[9], c[10]);
+    R lambda_n = c[3], lambda_t = c[7];
+    Pcpd<R> p = pcpd(a, b, r1, r2);
+    V3<R> d12 = anchor_delta<R, EXACT>(a, b, p.r1, p.r2);
+    R d = vdot(d12, n);
+    if (d > (R)0) {
+        V3<R> dx = vscale(d, n);
+        R dl = pos_dlambda(a, b, p, h, (R)0, lambda_n, dx);
+        pos_apply(a, b, p, dl, dx);
+        lambda_n += dl;
+        p = pcpd(a, b, r1, r2);
+        dl = pos_dlambda(a, b, p, h, (R)0, lambda_t, dx);
+        R lt = lambda_t + dl;
+        if (lt > mus * lambda_n) {
+            // p1 - p1_til - (p2 - p2_til) with p_til from the previous pose (pbd.cpp:142-148)
+            double4_32a pa = W.prev_pos[a.idx], qa = W.prev_rot[a.idx], pb = W.prev_pos[b.idx], qb = W.prev_rot[b.idx];
+            V3<double> xa_prev = v3<double>(pa.x, pa.y, pa.z), xb_prev = v3<double>(pb.x, pb.y, pb.z);
+            Qt<R> qa_prev = qcast<R>(qt<double>(qa.x, qa.y, qa.z, qa.w)), qb_prev = qcast<R>(qt<double>(qb.x, qb.y, qb.z, qb.w));
+            V3<R> dp;
+            if (EXACT) {
+                V3<double> p1 = vadd(a.x, v3cast<double>(p.r1)), p2 = vadd(b.x, v3cast<double>(p.r2));
+                V3<double> p1t = vadd(xa_prev, v3cast<double>(qrotate(qa_prev, r1)));
+                V3<double> p2t = vadd(xb_prev, v3cast<double>(qrotate(qb_prev, r2)));
+                dp = v3cast<R>(vsub(vsub(p1, p1t), vsub(p2, p2t)));
+            } else {
+                V3<R> da = vadd(v3cast<R>(vsub(a.x, xa_prev)), vsub(p.r1, qrotate(qa_prev, r1)));
+                V3<R> db = vadd(v3cast<R>(vsub(b.x, xb_prev)), vsub(p.r2, qrotate(qb_prev, r2)));
+                dp = vsub(da, db);
+            }
+            V3<R> dpt = vsub(dp, vscale(vdot(dp, n), n));
+            pos_apply(a, b, p, dl, dpt);
+            lambda_t += dl;
+        }
+    }
+    c[3] = lambda_n;
+    c[7] = lambda_t;
+}
+
+// limit_angle (pbd.cpp:175-217)
+template <typename R>
+__device__ bool limit_angle(V3<R> n, V3<R> n1, V3<R> n2, R alpha, R beta, V3<R>& dq) {
+    const R pi = (R)PI_REF;
+    R phi = asin(vdot(vcross(n1, n2), n));
+    if (vdot(n1, n2) < (R)0) phi = pi - phi;
+    if (phi > pi) phi = phi - (R)2.0 * pi;
+    if (phi < -pi) phi = phi + (R)2.0 * pi;
+    if (phi < alpha || phi > beta) {
+        phi = (phi > beta) ? beta : ((phi < alpha) ? alpha : phi);
+        V3<R> ax = n;
+        if (vlen(ax) != (R)0) ax = vnorm(ax);
+        R s = sin(phi / (R)2.0);
+        Qt<R> rot = qt<R>(ax.x * s, ax.y * s, ax.z * s, cos(phi / (R)2.0));
+        n1 = qrotate(rot, n1);
+        dq = vcross(n1, n2);
+        return true;
+    }
+    return false;
+}
+
+template <typename R, bool EXACT>
+__device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double* lam, R h) {
+    Body<R> a = load_body(W, C.e1), b = load_body(W, C.e2);
+    const R EPS = Tiny<R>::v;
+    V3<R> r1 = v3<R>((R)C.r1[0], (R)C.r1[1], (R)C.r1[2]), r2 = v3<R>((R)C.r2[0], (R)C.r2[1], (R)C.r2[2]);
+    switch (C.type) {
+    case CON_POSITIONAL: {  // pbd.cpp:81-97
+        V3<R> dx = vsub(v3cast<R>(vsub(a.x, b.x)), v3<R>((R)C.distance[0], (R)C.distance[1], (R)C.distance[2]));
+        if (EXACT) dx = v3cast<R>(vsub(vsub(a.x, b.x), v3<double>(C.distance[0], C.distance[1], C.distance[2])));
+        Pcpd<R> p = pcpd(a, b, r1, r2);
+        R dl = pos_dlambda(a, b, p, h, (R)C.compliance, (R)lam[0], dx);
+        pos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+    } break;
+    case CON_MUTUAL_ORIENTATION: {  // pbd.cpp:156-173
+        Acpd<R> A = acpd(a, b);
+        Qt<R> aux = qmul(wq<R>(a.q), qinverse(wq<R>(b.q)));
+        V3<R> dq = v3<R>((R)2.0 * aux.x, (R)2.0 * aux.y, (R)2.0 * aux.z);
+        R dl = ang_dlambda(A, h, (R)C.compliance, (R)lam[0], dq);
+        ang_apply(a, b, A, dl, dq);
+        lam[0] += (double)dl;
+    } break;
+    case CON_HINGE: {  // pbd.cpp:245-299
+        Acpd<R> A = acpd(a, b);
+        V3<R> dq = vcross(qaxis(wq<R>(a.q), C.a1), qaxis(wq<R>(b.q), C.a2));
+        R dl = ang_dlambda(A, h, (R)C.compliance, (R)lam[1], dq);
+        ang_apply(a, b, A, dl, dq);
+        lam[1] += (double)dl;
+        Pcpd<R> p = pcpd(a, b, r1, r2);
+        V3<R> dx = anchor_delta<R, EXACT>(a, b, p.r1, p.r2);
+        dl = pos_dlambda(a, b, p, h, (R)0, (R)lam[0], dx);
+        pos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+        if (C.limited) {
+            V3<R> n1 = qaxis(wq<R>(a.q), C.l1), n2 = qaxis(wq<R>(b.q), C.l2), n = qaxis(wq<R>(a.q), C.a1);
+            if (limit_angle(n, n1, n2, (R)C.lo, (R)C.hi, dq)) {
+                Acpd<R> B = acpd(a, b);
+                R dl2 = ang_dlambda(B, h, (R)0, (R)lam[2], dq);
+                ang_apply(a, b, B, dl2, dq);
+                lam[2] += (double)dl2;
+            }
+        }
+    } break;
+    case CON_SPHERICAL: {  // pbd.cpp:301-379
+        Pcpd<R> p = pcpd(a, b, r1, r2);
+        V3<R> dx = anchor_delta<R, EXACT>(a, b, p.r1, p.r2);
+        R dl = pos_dlambda(a, b, p, h, (R)0, (R)lam[0], dx);
+        pos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+        V3<R> n1 = qaxis(wq<R>(a.q), C.a1), n2 = qaxis(wq<R>(b.q), C.a2);
+        V3<R> n = vcross(n1, n2);
+        R nl = vlen(n);
+        if (nl > EPS) {
+            n = v3<R>(n.x / nl, n.y / nl, n.z / nl);
+            V3<R> dq;
+            if (limit_angle(n, n1, n2, (R)C.lo, (R)C.hi, dq)) {
+                Acpd<R> A = acpd(a, b);
+                R d2 = ang_dlambda(A, h, (R)0, (R)lam[1], dq);
+                ang_apply(a, b, A, d2, dq);
+                lam[1] += (double)d2;
+            }
+        }
+        V3<R> a1 = qaxis(wq<R>(a.q), C.a1), b1 = qaxis(wq<R>(a.q), C.l1);
+        V3<R> a2 = qaxis(wq<R>(b.q), C.a2), b2 = qaxis(wq<R>(b.q), C.l2);
+        n = vadd(a1, a2);
+        nl = vlen(n);
+        if (nl > EPS) {
+            n = v3<R>(n.x / nl, n.y / nl, n.z / nl);
+            n1 = vsub(b1, vscale(vdot(n, b1), n));
+            n2 = vsub(b2, vscale(vdot(n, b2), n));
+            R l1 = vlen(n1), l2 = vlen(n2);
+            if (l1 > EPS && l2 > EPS) {
+                n1 = v3<R>(n1.x / l1, n1.y / l1, n1.z / l1);
+                n2 = v3<R>(n2.x / l2, n2.y / l2, n2.z / l2);
+                V3<R> dq;
+                if (limit_angle(n, n1, n2, (R)C.lo2, (R)C.hi2, dq)) {
+                    Acpd<R> A = acpd(a, b);
+                    R d2 = ang_dlambda(A, h, (R)0, (R)lam[2], dq);
+                    ang_apply(a, b, A, d2, dq);
+                    lam[2] += (double)d2;
+                }
+            }
+        }
+    } break;
+    default: break;
+    }
+    store_pose(W, a);
+    store_pose(W, b);
+}
+
+// --------------------------------------------------------------------------------------------
+// Predict (pbd.cpp:537-577) for one body
+template <typename R, bool EXACT>
+__device__ void predict_body(const WorldView<R>& W, int b, double h) {
+    double4_32a p = W.pos[b], q4 = W.rot[b];
+    W.prev_pos[b] = p;
+    W.prev_rot[b] = q4;
+    if (W.fixed[b] || !W.active[b]) return;
+    V3<double> x = v3<double>(p.x, p.y, p.z);
+    Qt<double> q = qt<double>(q4.x, q4.y, q4.z, q4.w);
+    V3<R> v = v3<R>(W.vel[3 * b], W.vel[3 * b + 1], W.vel[3 * b + 2]);
+    V3<R> w = v3<R>(W.omega[3 * b], W.omega[3 * b + 1], W.omega[3 * b + 2]);
+    V3<R> F = v3<R>((R)W.force[3 * b], (R)W.force[3 * b + 1], (R)W.force[3 * b + 2]);
+    V3<R> T = v3<R>((R)W.torque[3 * b], (R)W.torque[3 * b + 1], (R)W.torque[3 * b + 2]);
+    R invm = W.inv_mass[b];
+    R si[6], sI[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { si[i] = W.inv_inertia[6 * b + i]; sI[i] = W.inertia[6 * b + i]; }
+    R hR = (R)h;
+    v = vadd(v, vscale(hR * invm, F));
+    if (EXACT) x = vadd(x, v3cast<double>(vscale(hR, v)));
+    else x = vadd(x, vscale(h, v3cast<double>(v)));
+    Qt<R> qw = wq<R>(q);
+    M3<R> Iinv = world_tensor(qw, msym(si)), I = world_tensor(qw, msym(sI));
+    w = vadd(w, vscale(hR, mmulv(Iinv, vsub(T, vcross(w, mmulv(I, w))))));
+    Qt<R> qd = qmul(qt<R>(w.x, w.y, w.z, (R)0), qw);
+    if (EXACT) {
+        q.x = q.x + h * 0.5 * (double)qd.x; q.y = q.y + h * 0.5 * (double)qd.y;
+        q.z = q.z + h * 0.5 * (double)qd.z; q.w = q.w + h * 0.5 * (double)qd.w;
+    } else {
+        R s = hR * (R)0.5;
+        q.x = q.x + (double)(s * qd.x); q.y = q.y + (double)(s * qd.y);
+        q.z = q.z + (double)(s * qd.z); q.w = q.w + (double)(s * qd.w);
+    }
+    q = qnormalize(q);
+    W.pos[b] = make_double4_32a(x.x, x.y, x.z, 0.0);
+    W.rot[b] = make_double4_32a(q.x, q.y, q.z, q.w);
+    W.vel[3 * b] = v.x; W.vel[3 * b + 1] = v.y; W.vel[3 * b + 2] = v.z;
+    W.omega[3 * b] = w.x; W.omega[3 * b + 1] = w.y; W.omega[3 * b + 2] = w.z;
+}
+
+// PBD velocity update (pbd.cpp:623-643) for one body
+template <typename R, bool EXACT>
+__device__ void velocity_body(const WorldView<R>& W, int b, double h) {
+    if (W.fixed[b] || !W.active[b]) return;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { W.prev_vel[3 * b + i] = W.vel[3 * b + i]; W.prev_omega[3 * b + i] = W.omega[3 * b + i]; }
+    double4_32a p = W.pos[b], pp = W.prev_pos[b], q4 = W.rot[b], pq4 = W.prev_rot[b];
+    V3<double> dx = vsub(v3<double>(p.x, p.y, p.z), v3<double>(pp.x, pp.y, pp.z));
+    V3<double> v = vscale(1.0 / h, dx);
+    Qt<double> dq = qmul(qt<double>(q4.x, q4.y, q4.z, q4.w), qinverse(qt<double>(pq4.x, pq4.y, pq4.z, pq4.w)));
+    V3<double> w = (dq.w >= 0.0) ? vscale(2.0 / h, v3<double>(dq.x, dq.y, dq.z)) : vscale(-2.0 / h, v3<double>(dq.x, dq.y, dq.z));
+    W.vel[3 * b] = (R)v.x; W.vel[3 * b + 1] = (R)v.y; W.vel[3 * b + 2] = (R)v.z;
+    W.omega[3 * b] = (R)w.x; W.omega[3 * b + 1] = (R)w.y; W.omega[3 * b + 2] = (R)w.z;
+}
+
+// Velocity solver for one contact (pbd.cpp:646-711); velocities of the two bodies are in registers.
+template <typename R, bool EXACT>
+__device__ void contact_velocity(const WorldView<R>& W, const Body<R>& a, const Body<R>& b, const R* c, R h, R mud, R e,
+                                 V3<R>& va, V3<R>& wa, V3<R>& vb, V3<R>& wb, V3<R> pva, V3<R> pwa, V3<R> pvb, V3<R> pwb) {
+    V3<R> r1 = v3<R>(c[0], c[1], c[2]), r2 = v3<R>(c[4], c[5], c[6]), n = v3<R>(c[8], c[9], c[10]);
+    R lambda_n = c[3];
+    Pcpd<R> p = pcpd(a, b, r1, r2);
+    V3<R> v = vsub(vadd(va, vcross(wa, p.r1)), vadd(vb, vcross(wb, p.r2)));
+    R vn = vdot(n, v);
+    V3<R> vt = vsub(v, vscale(vn, n));
+    V3<R> dv = v3<R>(0, 0, 0);
+    R fn = lambda_n / h;
+    R x1 = mud * fabs(fn), x2 = vlen(vt);
+    R fact = (x1 < x2) ? x1 : x2;
+    dv = vadd(dv, vscale(-fact, vnorm(vt)));
+    V3<R> vtil = vsub(vadd(pva, vcross(pwa, p.r1)), vadd(pvb, vcross(pwb, p.r2)));
+    R vntil = vdot(n, vtil);
+    R m = -e * vntil;
+    fact = -vn + ((m < (R)0.0) ? m : (R)0.0);
+    dv = vadd(dv, vscale(fact, n));
+    R w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
+    R w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    V3<R> P = vscale((R)1.0 / (w1 + w2), dv);
+    if (!a.fixed) {
+        va = vadd(va, vscale(a.invm, P));
+        wa = vadd(wa, mmulv(p.I1, vcross(p.r1, P)));
+    }
+    if (!b.fixed) {
+        vb = vadd(vb, vinv(vscale(b.invm, P)));
+        wb = vadd(wb, vinv(mmulv(p.I2, vcross(p.r2, P))));
+    }
+}
+
+}  // namespace rp

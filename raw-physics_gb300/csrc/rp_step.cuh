@@ -1,0 +1,669 @@
+// The persistent step kernel: one launch advances every scene of a batch by one
+// pbd_simulate_with_constraints call (src/physics/pbd.cpp:468-747).
+//
+// Execution groups. A scene is processed by a group of threads that synchronises between the
+// phases of the step:
+//   CtaGroup   one CTA per scene (batches of small scenes; barrier = __syncthreads)
+//   GridGroup  every CTA of a cooperative launch on one large scene (barrier = a bounded
+//              grid-wide barrier; the launch is cooperative, so all CTAs are co-resident)
+//
+// Phases of one step:
+//   broad phase   exact pair list in the reference's order (FP32 prefilter, FP64 test with
+//                 round-to-nearest intrinsics and no contraction, so it is bit-identical)
+//   islands       lock-free union-find and the sleeping update (pbd.cpp:477-506)
+//   schedule      order-preserving graph colouring of the Gauss–Seidel sweep: node k (an external
+//                 constraint or a broad-phase pair) gets level 1 + max(level of the previous node
+//                 on each of its non-fixed bodies). Nodes of one level share no non-fixed body, and
+//                 every pair of nodes that does share one keeps the reference's relative order, so
+//                 sweeping level by level reproduces the serial sweep (pbd.cpp:615-620) exactly.
+//   substeps      predict, hull transform, warp-per-pair narrowphase, level-by-level position
+//                 solve, velocity update, level-by-level velocity solve.
+#pragma once
+#include "rp_math.cuh"
+#include "rp_world.h"
+#include "rp_narrow.cuh"
+#include "rp_solve.cuh"
+
+namespace rp {
+
+constexpr int BLOCK = 256;
+constexpr int WARPS_PER_BLOCK = BLOCK / 32;
+constexpr long long BARRIER_SPIN_LIMIT = 20000000;   // ~1 s of polling, then give up with a status bit
+
+// ---------------------------------------------------------------------------------------------
+// Groups
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+static __device__ __noinline__ void grid_barrier(unsigned* bar, uint32_t* status) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned gen = ld_acquire_gpu(&bar[1]);
+        __threadfence();
+        unsigned arrived = atomicAdd(&bar[0], 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            long long spins = 0;
+            while (ld_acquire_gpu(&bar[1]) == gen) {
+                __nanosleep(40);
+                if (++spins > BARRIER_SPIN_LIMIT) { atomicOr(status, (uint32_t)ST_BARRIER_TIMEOUT); break; }
+                // after one barrier has given up, later ones do not wait again
+                if ((spins & 1023) == 0 && (*(volatile uint32_t*)status & ST_BARRIER_TIMEOUT)) break;
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+struct CtaGroup {
+    __device__ int rank() const { return (int)threadIdx.x; }
+    __device__ int size() const { return (int)blockDim.x; }
+    __device__ int nblocks() const { return 1; }
+    __device__ int block() const { return 0; }
+    __device__ void sync() const { __syncthreads(); }
+};
+
+struct GridGroup {
+    unsigned* bar;
+    uint32_t* status;
+    __device__ int rank() const { return (int)(blockIdx.x * blockDim.x + threadIdx.x); }
+    __device__ int size() const { return (int)(gridDim.x * blockDim.x); }
+    __device__ int nblocks() const { return (int)gridDim.x; }
+    __device__ int block() const { return (int)blockIdx.x; }
+    __device__ void sync() const { grid_barrier(bar, status); }
+};
+
+// Block-wide inclusive scan of one value per thread; smem must hold 32 ints.
+static __device__ int block_incl_scan(int x, int* smem, int& total) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int v = warp_incl_scan(x);
+    if (lane == 31) smem[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+        int t = lane < nw ? smem[lane] : 0;
+        t = warp_incl_scan(t);
+        if (lane < nw) smem[lane] = t;
+    }
+    __syncthreads();
+    int add = wid > 0 ? smem[wid - 1] : 0;
+    total = smem[((blockDim.x + 31) >> 5) - 1];
+    __syncthreads();
+    return v + add;
+}
+
+// Group-wide exclusive scan of data[0, n) in place; returns the total to every thread.
+// tmp: nblocks ints of global scratch (unused for a CTA group).
+template <class G>
+__device__ int group_exclusive_scan(const G& g, int* data, int n, int* tmp, int* smem) {
+    int nb = g.nblocks(), bi = g.block();
+    int chunk = (n + nb - 1) / nb;
+    int lo = min(n, bi * chunk), hi = min(n, lo + chunk);
+    int carry = 0;
+    for (int base = lo; base < hi; base += blockDim.x) {
+        int i = base + (int)threadIdx.x;
+        int x = i < hi ? data[i] : 0;
+        int tot;
+        int incl = block_incl_scan(x, smem, tot);
+        if (i < hi) data[i] = carry + incl - x;
+        carry += tot;
+    }
+    if (nb == 1) {
+        __syncthreads();
+        return carry;
+    }
+    if (threadIdx.x == 0) tmp[bi] = carry;
+    g.sync();
+    int off = 0, total = 0;
+    for (int k = (int)(threadIdx.x & 31); k < nb; k += 32) {
+        int t = tmp[k];
+        total += t;
+        if (k < bi) off += t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        off += __shfl_xor_sync(0xffffffffu, off, o);
+        total += __shfl_xor_sync(0xffffffffu, total, o);
+    }
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) data[i] += off;
+    g.sync();
+    return total;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Broad phase (broad.cpp:6-28): all i < j with |p_i - p_j| <= r_i + r_j + 0.1, in row order.
+__device__ __forceinline__ bool broad_exact(double4_32a pi, double4_32a pj, double ri, double rj) {
+    double dx = __dsub_rn(pi.x, pj.x), dy = __dsub_rn(pi.y, pj.y), dz = __dsub_rn(pi.z, pj.z);
+    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    double dist = __dsqrt_rn(d2);
+    double mx = __dadd_rn(__dadd_rn(ri, rj), 0.1);
+    return dist <= mx;
+}
+
+// Conservative FP32 rejection: true when the pair certainly fails the exact test.
+__device__ __forceinline__ bool broad_reject(float4 fi, float4 fj) {
+    // fi = (x, y, z, r + 0.05) rounded to float; w absorbs the 0.1 margin split between the two
+    float bx = 2.5e-7f * (fabsf(fi.x) + fabsf(fj.x)) + 1e-6f;
+    float by = 2.5e-7f * (fabsf(fi.y) + fabsf(fj.y)) + 1e-6f;
+    float bz = 2.5e-7f * (fabsf(fi.z) + fabsf(fj.z)) + 1e-6f;
+    float dx = fmaxf(fabsf(fi.x - fj.x) - bx, 0.f), dy = fmaxf(fabsf(fi.y - fj.y) - by, 0.f),
+          dz = fmaxf(fabsf(fi.z - fj.z) - bz, 0.f);
+    float mx = (fi.w + fj.w) * 1.00001f + 1e-6f;
+    return dx * dx + dy * dy + dz * dz > mx * mx;
+}
+
+template <typename R, class G>
+__device__ void broad_phase(const WorldView<R>& W, const G& g, int s, int* smem) {
+    const int b0 = W.scene_body[s], n = W.scene_body[s + 1] - b0;
+    const int pcap = W.scene_pair_cap[s + 1] - W.scene_pair_cap[s];
+    int2* pairs = W.pairs + W.scene_pair_cap[s];
+    const int lane = threadIdx.x & 31;
+    const int gw = g.rank() >> 5, nw = g.size() >> 5;
+    // per-row counts (warp per row)
+    for (int i = gw; i < n; i += nw) {
+        double4_32a pi = W.pos[b0 + i];
+        double ri = W.radius[b0 + i];
+        float4 fi = make_float4((float)pi.x, (float)pi.y, (float)pi.z, (float)ri + 0.05f);
+        int cnt = 0;
+        for (int jb = i + 1; jb < n; jb += 32) {
+            int j = jb + lane;
+            bool hit = false;
+            if (j < n) {
+                double4_32a pj = W.pos[b0 + j];
+                double rj = W.radius[b0 + j];
+                float4 fj = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)rj + 0.05f);
+                hit = !broad_reject(fi, fj) && broad_exact(pi, pj, ri, rj);
+            }
+            cnt += __popc(__ballot_sync(0xffffffffu, hit));
+        }
+        if (lane == 0) W.row_count[b0 + i] = cnt;
+    }
+    g.sync();
+    int total = group_exclusive_scan(g, W.row_count + b0, n, W.scan_tmp, smem);
+    if (g.rank() == 0) W.pair_count[s] = total;
+    if (total > pcap) {
+        if (g.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_PAIR_OVERFLOW);
+    }
+    for (int i = gw; i < n; i += nw) {
+        double4_32a pi = W.pos[b0 + i];
+        double ri = W.radius[b0 + i];
+        float4 fi = make_float4((float)pi.x, (float)pi.y, (float)pi.z, (float)ri + 0.05f);
+        int out = W.row_count[b0 + i];
+        for (int jb = i + 1; jb < n; jb += 32) {
+            int j = jb + lane;
+            bool hit = false;
+            if (j < n) {
+                double4_32a pj = W.pos[b0 + j];
+                double rj = W.radius[b0 + j];
+                float4 fj = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)rj + 0.05f);
+                hit = !broad_reject(fi, fj) && broad_exact(pi, pj, ri, rj);
+            }
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            int pos = out + __popc(m & ((1u << lane) - 1u));
+            if (hit && pos < pcap) pairs[pos] = make_int2(b0 + i, b0 + j);
+            out += __popc(m);
+        }
+    }
+    g.sync();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Islands and sleeping (broad.cpp:31-116, pbd.cpp:477-506)
+__device__ __forceinline__ int uf_find(int* parent_, int x) {
+    volatile int* parent = parent_;
+    int p = parent[x];
+    while (p != x) {
+        int gp = parent[p];
+        x = p;
+        p = gp;
+    }
+    return x;
+}
+__device__ __forceinline__ void uf_union(int* parent, int a, int b) {
+    for (int guard = 0; guard < (1 << 20); ++guard) {
+        int ra = uf_find(parent, a), rb = uf_find(parent, b);
+        if (ra == rb) return;
+        if (ra < rb) { int t = ra; ra = rb; rb = t; }
+        if (atomicCAS(&parent[ra], ra, rb) == ra) return;
+    }
+}
+
+template <typename R, class G>
+__device__ void islands(const WorldView<R>& W, const G& g, int s, double dt) {
+    const int b0 = W.scene_body[s], b1 = W.scene_body[s + 1];
+    const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+    const int2* pairs = W.pairs + W.scene_pair_cap[s];
+    const int e0 = W.scene_ext[s], e1 = W.scene_ext[s + 1];
+    for (int b = b0 + g.rank(); b < b1; b += g.size()) { W.uf_parent[b] = b; W.island_awake[b] = 0; }
+    g.sync();
+    for (int k = g.rank(); k < np + (e1 - e0); k += g.size()) {
+        int a, c;
+        if (k < np) { a = pairs[k].x; c = pairs[k].y; }
+        else { a = W.ext[e0 + k - np].e1; c = W.ext[e0 + k - np].e2; }
+        if (!W.fixed[a] && !W.fixed[c]) uf_union(W.uf_parent, a, c);
+    }
+    g.sync();
+    for (int b = b0 + g.rank(); b < b1; b += g.size()) {
+        if (W.fixed[b]) continue;
+        V3<R> v = v3<R>(W.vel[3 * b], W.vel[3 * b + 1], W.vel[3 * b + 2]);
+        V3<R> w = v3<R>(W.omega[3 * b], W.omega[3 * b + 1], W.omega[3 * b + 2]);
+        R lv = vlen(v), av = vlen(w);
+        double d = W.deact[b];
+        if (lv < (R)0.10 && av < (R)0.10) d += dt;
+        else d = 0.0;
+        W.deact[b] = d;
+        if (d < 1.0) W.island_awake[uf_find(W.uf_parent, b)] = 1;
+    }
+    g.sync();
+    for (int b = b0 + g.rank(); b < b1; b += g.size()) {
+        if (W.fixed[b]) continue;
+        W.active[b] = W.island_awake[uf_find(W.uf_parent, b)];
+    }
+    g.sync();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Order-preserving colouring of the Gauss–Seidel sweep.
+template <typename R, class G>
+__device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
+    const int b0 = W.scene_body[s], nb = W.scene_body[s + 1] - b0;
+    const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+    const int2* pairs = W.pairs + W.scene_pair_cap[s];
+    const int e0 = W.scene_ext[s], ne = W.scene_ext[s + 1] - e0;
+    const int nbase = W.scene_node_cap[s];
+    const int nn = ne + np;
+    int* nbody = W.node_body + 2 * nbase;
+    int* npred = W.node_pred + 2 * nbase;
+    int* nlev = W.node_level + nbase;
+    int* tl = W.body_tl + 2 * nbase;
+    int* lcount = W.level_count + s * (W.max_levels + 1);
+    int* lfill = W.level_fill + s * (W.max_levels + 1);
+    for (int b = g.rank(); b < nb; b += g.size()) W.body_tl_count[b0 + b] = 0;
+    for (int l = g.rank(); l <= W.max_levels; l += g.size()) { lcount[l] = 0; lfill[l] = 0; }
+    if (g.rank() == 0) { W.scene_levels[s] = 0; W.scene_nodes[s] = nn; }
+    g.sync();
+    for (int k = g.rank(); k < nn; k += g.size()) {
+        int a, c;
+        bool live = true;
+        if (k < ne) { a = W.ext[e0 + k].e1; c = W.ext[e0 + k].e2; }
+        else {
+            a = pairs[k - ne].x; c = pairs[k - ne].y;
+            live = !((W.fixed[a] || !W.active[a]) && (W.fixed[c] || !W.active[c]));
+        }
+        int ba = (live && !W.fixed[a]) ? a : -1;
+        int bc = (live && !W.fixed[c] && c != a) ? c : -1;
+        nbody[2 * k] = ba;
+        nbody[2 * k + 1] = bc;
+        npred[2 * k] = -1;
+        npred[2 * k + 1] = -1;
+        nlev[k] = live ? 0 : -1;
+        if (ba >= 0) atomicAdd(&W.body_tl_count[ba], 1);
+        if (bc >= 0) atomicAdd(&W.body_tl_count[bc], 1);
+    }
+    g.sync();
+    // timeline starts (relative to the scene's timeline base) live in body_tl_start
+    for (int b = g.rank(); b < nb; b += g.size()) W.body_tl_start[b0 + b] = W.body_tl_count[b0 + b];
+    g.sync();
+    group_exclusive_scan(g, W.body_tl_start + b0, nb, W.scan_tmp, smem);
+    for (int b = g.rank(); b < nb; b += g.size()) W.body_tl_count[b0 + b] = 0;
+    g.sync();
+    for (int k = g.rank(); k < nn; k += g.size()) {
+        for (int side = 0; side < 2; ++side) {
+            int b = nbody[2 * k + side];
+            if (b < 0) continue;
+            int slot = atomicAdd(&W.body_tl_count[b], 1);
+            tl[W.body_tl_start[b] + slot] = k;
+        }
+    }
+    g.sync();
+    // sort every timeline (short: a body's broad-phase degree) and link predecessors
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        int st = W.body_tl_start[b0 + b], cnt = W.body_tl_count[b0 + b];
+        int* t = tl + st;
+        for (int i = 1; i < cnt; ++i) {
+            int key = t[i], j = i - 1;
+            while (j >= 0 && t[j] > key) { t[j + 1] = t[j]; --j; }
+            t[j + 1] = key;
+        }
+        for (int i = 1; i < cnt; ++i) {
+            int k = t[i];
+            int side = (nbody[2 * k] == b0 + b) ? 0 : 1;
+            npred[2 * k + side] = t[i - 1];
+        }
+    }
+    g.sync();
+    // longest-path levels by monotone relaxation
+    // three rotating "changed" flags: the one reset in round r was last read in round r-2
+    int* flag = lfill + W.max_levels - 2;
+    if (g.rank() == 0) { flag[0] = 0; flag[1] = 0; flag[2] = 0; }
+    g.sync();
+    for (int round = 0; round < W.max_levels; ++round) {
+        if (g.rank() == 0) flag[(round + 1) % 3] = 0;
+        bool changed = false;
+        for (int k = g.rank(); k < nn; k += g.size()) {
+            int lk = nlev[k];
+            if (lk < 0) continue;
+            int p0 = npred[2 * k], p1 = npred[2 * k + 1];
+            int l0 = p0 >= 0 ? ((volatile int*)nlev)[p0] : -1;
+            int l1 = p1 >= 0 ? ((volatile int*)nlev)[p1] : -1;
+            int nl = max(l0, l1) + 1;
+            if (nl > lk) { ((volatile int*)nlev)[k] = nl; changed = true; }
+        }
+        if (changed) flag[round % 3] = 1;
+        g.sync();
+        if (((volatile int*)flag)[round % 3] == 0) break;
+        if (round == W.max_levels - 1 && g.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW);
+    }
+    g.sync();
+    // bucket nodes by level
+    int maxl = -1;
+    for (int k = g.rank(); k < nn; k += g.size()) {
+        int l = nlev[k];
+        if (l < 0) continue;
+        if (l >= W.max_levels - 3) { atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW); continue; }
+        atomicAdd(&lcount[l], 1);
+        maxl = max(maxl, l);
+    }
+    if (maxl >= 0) atomicMax(&W.scene_levels[s], maxl + 1);
+    g.sync();
+    if (g.rank() == 0) {
+        // exclusive prefix over the (few) levels; lfill doubles as the per-level fill counter
+        int L = W.scene_levels[s], acc = 0;
+        for (int l = 0; l <= L; ++l) { int c = lcount[l]; lcount[l] = acc; acc += c; }
+    }
+    g.sync();
+    for (int k = g.rank(); k < nn; k += g.size()) {
+        int l = nlev[k];
+        if (l < 0 || l >= W.max_levels - 3) continue;
+        int slot = atomicAdd(&lfill[l], 1);
+        W.level_nodes[nbase + lcount[l] + slot] = k;
+    }
+    g.sync();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Hull transform (colliders_update, collider.cpp:409-446) for every collider of the scene
+template <typename R, bool EXACT, class G>
+__device__ void transform_hulls(const WorldView<R>& W, const G& g, int s, bool include_fixed) {
+    const int b0 = W.scene_body[s], b1 = W.scene_body[s + 1];
+    const int c0 = W.col_start[b0], c1 = W.col_start[b1];
+    const int lane = threadIdx.x & 31;
+    const int gw = g.rank() >> 5, nw = g.size() >> 5;
+    // bodies are found by a short search: colliders are stored body by body
+    for (int ci = c0 + gw; ci < c1; ci += nw) {
+        const Collider col = W.colliders[ci];
+        if (col.type != COL_HULL) continue;
+        int lo = b0, hi = b1 - 1;
+        while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (W.col_start[mid] <= ci) lo = mid; else hi = mid - 1; }
+        int b = lo;
+        if (W.fixed[b] && !include_fixed) continue;
+        const Shape sh = W.shapes[col.shape];
+        double4_32a p4 = W.pos[b], q4 = W.rot[b];
+        V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
+        V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
+        if (EXACT) {
+            M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
+            for (int i = lane; i < sh.nv; i += 32) {
+                const double* v = W.shape_verts + 3 * (sh.vert_off + i);
+                tv[i] = v3cast<R>(m4_point(M, v3<double>(v[0], v[1], v[2])));
+            }
+            for (int i = lane; i < sh.nf; i += 32) {
+                const double* nrm = W.face_normal + 3 * (sh.face_off + i);
+                tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
+            }
+        } else {
+            M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
+            for (int i = lane; i < sh.nv; i += 32) {
+                const double* v = W.shape_verts + 3 * (sh.vert_off + i);
+                tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
+            }
+            for (int i = lane; i < sh.nf; i += 32) {
+                const double* nrm = W.face_normal + 3 * (sh.face_off + i);
+                tn[i] = vnorm(mmulv(Rm, v3<R>((R)nrm[0], (R)nrm[1], (R)nrm[2])));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Narrowphase: one warp per broad-phase pair
+template <typename R, bool EXACT>
+__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged) {
+    ColView<R> v;
+    const Collider col = W.colliders[ci];
+    v.type = col.type;
+    v.radius = (R)col.radius;
+    v.center = center;
+    v.off = off;
+    v.nv = 0;
+    v.nf = 0;
+    v.shape = nullptr;
+    v.verts = nullptr;
+    v.norms = nullptr;
+    v.staged = false;
+    if (col.type == COL_HULL) {
+        v.shape = W.shapes + col.shape;
+        v.nv = v.shape->nv;
+        v.nf = v.shape->nf;
+        v.verts = (const V3<R>*)(W.tverts) + col.tv_off;
+        v.norms = (const V3<R>*)(W.tnorms) + col.tn_off;
+        if (staged && v.nv <= STAGE_V) {
+            for (int i = (int)lane_id(); i < v.nv; i += 32) ((V3<R>*)staged)[i] = vadd(v.verts[i], off);
+            __syncwarp();
+            v.verts = staged;
+            v.staged = true;
+        }
+    }
+    return v;
+}
+
+// colliders_get_contacts for one body pair (collider.cpp:560-571); contacts land in sm.
+template <typename R, bool EXACT>
+__device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, int b, bool raw) {
+    if (lane_id() == 0) { sm.ncontacts = 0; sm.status = 0; }
+    __syncwarp();
+    double4_32a pa = W.pos[a], pb = W.pos[b], qa4 = W.rot[a], qb4 = W.rot[b];
+    PairFrame<R, EXACT> fr;
+    fr.raw = raw;
+    V3<R> offa, offb;
+    if (EXACT) {
+        offa = v3<R>(0, 0, 0);
+        offb = v3<R>(0, 0, 0);
+        fr.x1 = v3<R>((R)pa.x, (R)pa.y, (R)pa.z);
+        fr.x2 = v3<R>((R)pb.x, (R)pb.y, (R)pb.z);
+    } else {
+        offa = v3<R>(0, 0, 0);
+        offb = v3<R>((R)(pb.x - pa.x), (R)(pb.y - pa.y), (R)(pb.z - pa.z));
+        fr.x1 = offa;
+        fr.x2 = offb;
+    }
+    fr.q1inv = qinverse(qt<R>((R)qa4.x, (R)qa4.y, (R)qa4.z, (R)qa4.w));
+    fr.q2inv = qinverse(qt<R>((R)qb4.x, (R)qb4.y, (R)qb4.z, (R)qb4.w));
+    const int ca0 = W.col_start[a], ca1 = W.col_start[a + 1], cb0 = W.col_start[b], cb1 = W.col_start[b + 1];
+    for (int ca = ca0; ca < ca1; ++ca) {
+        // exact build: stored vertices are world coordinates, sphere centres the body positions;
+        // FP32 build: stored vertices are rotated about the body origin, the frame origin is body a
+        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va);
+        for (int cb = cb0; cb < cb1; ++cb) {
+            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb);
+            collider_contacts<R, EXACT>(sm, W, va, vb, fr, W.counters);
+            __syncwarp();
+        }
+    }
+}
+
+template <typename R, bool EXACT, class G>
+__device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem<R>& sm) {
+    const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+    const int pbase = W.scene_pair_cap[s];
+    const int cbase = W.scene_contact_cap[s];
+    const int ccap = W.scene_contact_cap[s + 1] - cbase;
+    const int lane = threadIdx.x & 31;
+    const int gw = g.rank() >> 5, nw = g.size() >> 5;
+    for (int p = gw; p < np; p += nw) {
+        int2 pr = W.pairs[pbase + p];
+        int a = pr.x, b = pr.y;
+        bool live = !((W.fixed[a] || !W.active[a]) && (W.fixed[b] || !W.active[b]));
+        if (!live) {
+            if (lane == 0) { W.pair_ccount[pbase + p] = 0; W.pair_cstart[pbase + p] = 0; }
+            continue;
+        }
+        pair_contacts<R, EXACT>(W, sm, a, b, false);
+        int nc = sm.ncontacts;
+        int start = 0;
+        if (lane == 0) {
+            start = atomicAdd(&W.contact_count[s], nc);
+            if (start + nc > ccap) {
+                atomicOr(&W.status[s], (uint32_t)ST_CONTACT_OVERFLOW);
+                nc = 0;
+            }
+            if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+            W.pair_cstart[pbase + p] = start;
+            W.pair_ccount[pbase + p] = nc;
+        }
+        start = __shfl_sync(0xffffffffu, start, 0);
+        nc = __shfl_sync(0xffffffffu, nc, 0);
+        for (int k = lane; k < nc; k += 32) {
+            R* c = W.contacts + 12 * (size_t)(cbase + start + k);
+            V3<R> r1 = sm.c_r1[k], r2 = sm.c_r2[k], n = sm.c_n[k];
+            c[0] = r1.x; c[1] = r1.y; c[2] = r1.z; c[3] = 0;
+            c[4] = r2.x; c[5] = r2.y; c[6] = r2.z; c[7] = 0;
+            c[8] = n.x; c[9] = n.y; c[10] = n.z; c[11] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Level sweeps
+template <typename R, bool EXACT>
+__device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
+    const int e0 = W.scene_ext[s], ne = W.scene_ext[s + 1] - e0;
+    if (k < ne) {
+        ext_solve<R, EXACT>(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
+        return;
+    }
+    const int p = W.scene_pair_cap[s] + (k - ne);
+    const int nc = W.pair_ccount[p];
+    if (nc == 0) return;
+    int2 pr = W.pairs[p];
+    Body<R> a = load_body(W, pr.x), b = load_body(W, pr.y);
+    const R mus = (W.material[4 * pr.x] + W.material[4 * pr.y]) / (R)2.0f;
+    R* c = W.contacts + 12 * (size_t)(W.scene_contact_cap[s] + W.pair_cstart[p]);
+    for (int i = 0; i < nc; ++i) collision_solve<R, EXACT>(W, a, b, c + 12 * i, h, mus);
+    store_pose(W, a);
+    store_pose(W, b);
+}
+
+template <typename R, bool EXACT>
+__device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
+    const int ne = W.scene_ext[s + 1] - W.scene_ext[s];
+    if (k < ne) return;
+    const int p = W.scene_pair_cap[s] + (k - ne);
+    const int nc = W.pair_ccount[p];
+    if (nc == 0) return;
+    int2 pr = W.pairs[p];
+    Body<R> a = load_body(W, pr.x), b = load_body(W, pr.y);
+    const int ia = pr.x, ib = pr.y;
+    V3<R> va = v3<R>(W.vel[3 * ia], W.vel[3 * ia + 1], W.vel[3 * ia + 2]);
+    V3<R> wa = v3<R>(W.omega[3 * ia], W.omega[3 * ia + 1], W.omega[3 * ia + 2]);
+    V3<R> vb = v3<R>(W.vel[3 * ib], W.vel[3 * ib + 1], W.vel[3 * ib + 2]);
+    V3<R> wb = v3<R>(W.omega[3 * ib], W.omega[3 * ib + 1], W.omega[3 * ib + 2]);
+    V3<R> pva = v3<R>(W.prev_vel[3 * ia], W.prev_vel[3 * ia + 1], W.prev_vel[3 * ia + 2]);
+    V3<R> pwa = v3<R>(W.prev_omega[3 * ia], W.prev_omega[3 * ia + 1], W.prev_omega[3 * ia + 2]);
+    V3<R> pvb = v3<R>(W.prev_vel[3 * ib], W.prev_vel[3 * ib + 1], W.prev_vel[3 * ib + 2]);
+    V3<R> pwb = v3<R>(W.prev_omega[3 * ib], W.prev_omega[3 * ib + 1], W.prev_omega[3 * ib + 2]);
+    const R mud = (W.material[4 * ia + 1] + W.material[4 * ib + 1]) / (R)2.0f;
+    const R e = W.material[4 * ia + 2] * W.material[4 * ib + 2];
+    const R* c = W.contacts + 12 * (size_t)(W.scene_contact_cap[s] + W.pair_cstart[p]);
+    for (int i = 0; i < nc; ++i) contact_velocity<R, EXACT>(W, a, b, c + 12 * i, h, mud, e, va, wa, vb, wb, pva, pwa, pvb, pwb);
+    if (!a.fixed) {
+        W.vel[3 * ia] = va.x; W.vel[3 * ia + 1] = va.y; W.vel[3 * ia + 2] = va.z;
+        W.omega[3 * ia] = wa.x; W.omega[3 * ia + 1] = wa.y; W.omega[3 * ia + 2] = wa.z;
+    }
+    if (!b.fixed) {
+        W.vel[3 * ib] = vb.x; W.vel[3 * ib + 1] = vb.y; W.vel[3 * ib + 2] = vb.z;
+        W.omega[3 * ib] = wb.x; W.omega[3 * ib + 1] = wb.y; W.omega[3 * ib + 2] = wb.z;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// One full step of scene s by group g
+template <typename R, bool EXACT, class G>
+__device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepParams& P, NarrowSmem<R>& sm, int* smem) {
+    if (!(P.dt > 0.0)) return;   // pbd.cpp:471
+    const double h = P.dt / P.num_substeps;
+    const R hR = (R)h;
+    const int b0 = W.scene_body[s], b1 = W.scene_body[s + 1];
+    broad_phase(W, g, s, smem);
+    islands(W, g, s, P.dt);
+    schedule(W, g, s, smem);
+    const int L = W.scene_levels[s];
+    const int nbase = W.scene_node_cap[s];
+    const int* lstart = W.level_count + s * (W.max_levels + 1);
+    const int e0 = W.scene_ext[s], e1 = W.scene_ext[s + 1];
+    for (int sub = 0; sub < P.num_substeps; ++sub) {
+        for (int b = b0 + g.rank(); b < b1; b += g.size()) predict_body<R, EXACT>(W, b, h);
+        for (int e = e0 + g.rank(); e < e1; e += g.size())
+            for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
+        if (g.rank() == 0) W.contact_count[s] = 0;
+        g.sync();
+        if (P.enable_collisions) {
+            transform_hulls<R, EXACT>(W, g, s, sub == 0);
+            g.sync();
+            narrowphase<R, EXACT>(W, g, s, sm);
+        } else {
+            const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+            for (int p = g.rank(); p < np; p += g.size()) W.pair_ccount[W.scene_pair_cap[s] + p] = 0;
+        }
+        g.sync();
+        for (int it = 0; it < P.num_pos_iters; ++it) {
+            for (int l = 0; l < L; ++l) {
+                for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size())
+                    solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                g.sync();
+            }
+        }
+        for (int b = b0 + g.rank(); b < b1; b += g.size()) velocity_body<R, EXACT>(W, b, h);
+        g.sync();
+        for (int l = 0; l < L; ++l) {
+            for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size())
+                vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+            g.sync();
+        }
+    }
+}
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(BLOCK) step_kernel_cta(WorldView<R> W, StepParams P) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ int scan_smem[32];
+    NarrowSmem<R>* sms = reinterpret_cast<NarrowSmem<R>*>(dyn_smem);
+    NarrowSmem<R>& sm = sms[threadIdx.x >> 5];
+    CtaGroup g;
+    for (int s = blockIdx.x; s < W.num_scenes; s += gridDim.x) {
+        step_scene<R, EXACT>(W, g, s, P, sm, scan_smem);
+        __syncthreads();
+    }
+}
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(BLOCK) step_kernel_grid(WorldView<R> W, StepParams P) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ int scan_smem[32];
+    NarrowSmem<R>* sms = reinterpret_cast<NarrowSmem<R>*>(dyn_smem);
+    NarrowSmem<R>& sm = sms[threadIdx.x >> 5];
+    GridGroup g;
+    g.bar = W.barrier;
+    g.status = W.status;
+    step_scene<R, EXACT>(W, g, 0, P, sm, scan_smem);
+}
+
+}  // namespace rp

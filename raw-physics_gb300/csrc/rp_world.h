@@ -1,0 +1,146 @@
+// Device-side layout of a batch of raw-physics scenes (shared by host and device code).
+//
+// A "scene" is what one pbd_simulate_with_constraints call advances: its bodies (entities), their
+// colliders, its external constraints. A batch is any number of independent scenes laid out back to
+// back; the plain single-scene form is a batch of one. All arrays live in HBM; per-scene ranges
+// are prefix offsets. Poses are FP64 (the reference's r64 world_position / world_rotation); the
+// remaining per-body quantities use the build's working type R (float for the FP32 build, double
+// for the exact all-FP64 build).
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace rp {
+
+// Status bits reported by the step kernel (rp_status values of the C ABI are built from them).
+enum : uint32_t {
+    ST_PAIR_OVERFLOW = 1u << 0,      // broad-phase pair list exceeded its capacity
+    ST_CONTACT_OVERFLOW = 1u << 1,   // contact buffer exceeded its capacity
+    ST_EPA_OVERFLOW = 1u << 2,       // EPA polytope outgrew its fixed per-warp storage
+    ST_CLIP_OVERFLOW = 1u << 3,      // clipped polygon outgrew its per-warp storage
+    ST_BARRIER_TIMEOUT = 1u << 4,    // a bounded group barrier gave up (should never happen)
+    ST_DEGENERATE = 1u << 5,         // input the reference would reject with an assert
+    ST_LEVEL_OVERFLOW = 1u << 6,     // dependency depth exceeded the level table
+    ST_EPA_NOT_CONVERGED = 1u << 8,  // informational: the reference prints "EPA did not converge."
+};
+
+// Collider kinds (Collider_Type, src/physics/collider.h:33-36)
+enum : int32_t { COL_SPHERE = 0, COL_HULL = 1 };
+
+// External constraint kinds (Constraint_Type, src/physics/pbd.h:14-20)
+enum : int32_t { CON_POSITIONAL = 0, CON_COLLISION = 1, CON_MUTUAL_ORIENTATION = 2, CON_HINGE = 3, CON_SPHERICAL = 4 };
+
+// One external constraint (the union of src/physics/pbd.h:22-77); lambdas live in the
+// per-substep scratch copy, as copy_constraints resets them every substep (pbd.cpp:426-462).
+struct ExtConstraint {
+    int32_t type, e1, e2;    // e1/e2: global body indices
+    int32_t a1, a2;          // hinge aligned axes | spherical swing axes
+    int32_t l1, l2;          // hinge limit axes | spherical twist axes
+    int32_t limited;
+    double r1[3], r2[3];
+    double compliance;
+    double distance[3];
+    double lo, hi;           // hinge limits | spherical swing limits
+    double lo2, hi2;         // spherical twist limits
+};
+
+struct Shape {               // one convex hull's topology (collider_convex_hull_create output)
+    int32_t nv, nf;
+    int32_t vert_off;        // into shape_verts (local, pre-scaled vertices, FP64)
+    int32_t face_off;        // into face_normal / face_elem_start
+    int32_t v2f_off, v2n_off;   // into csr_start for vertex -> faces, vertex -> neighbours
+    int32_t f2n_off;            // into csr_start for face -> neighbour faces
+    int32_t max_face_valence;
+    int32_t max_face_neighbours;
+};
+
+struct StepParams {          // the arguments of pbd_simulate_with_constraints
+    double dt;
+    int32_t num_substeps;
+    int32_t num_pos_iters;
+    int32_t enable_collisions;
+    int32_t pad;
+};
+
+struct Collider {
+    int32_t type;           // COL_SPHERE / COL_HULL
+    int32_t shape;           // hull: shape index
+    float radius;            // sphere radius (the reference stores r32)
+    int32_t tv_off;          // hull: offset of this collider's transformed vertices / normals
+    int32_t tn_off;
+};
+
+template <typename R>
+struct WorldView {
+    // ---- batch layout --------------------------------------------------------------------
+    int32_t num_scenes;
+    const int32_t* scene_body;     // [S+1] body ranges
+    const int32_t* scene_ext;      // [S+1] external constraint ranges
+    const int32_t* scene_pair_cap; // [S+1] pair scratch ranges (capacity)
+    const int32_t* scene_contact_cap; // [S+1] contact scratch ranges (capacity)
+    const int32_t* scene_node_cap; // [S+1] solver node scratch ranges (ext + pairs)
+    // ---- body state (mutable) ------------------------------------------------------------
+    double4_32a* pos;        // world_position (w unused)
+    double4_32a* rot;        // world_rotation (x, y, z, w)
+    double4_32a* prev_pos;
+    double4_32a* prev_rot;
+    R* vel;              // [3N] linear_velocity
+    R* omega;            // [3N] angular_velocity
+    R* prev_vel;         // [3N]
+    R* prev_omega;       // [3N]
+    uint8_t* active;
+    double* deact;       // deactivation_time
+    // ---- body constants -------------------------------------------------------------------
+    const R* inv_mass;
+    const R* inertia;       // [6N] local inertia tensor, symmetric storage
+    const R* inv_inertia;   // [6N]
+    const R* material;      // [4N] static friction, dynamic friction, restitution, (unused)
+    const double* radius;   // bounding_sphere_radius
+    const uint8_t* fixed;
+    const int32_t* col_start;   // [N+1] collider ranges
+    const double* force;     // [3N] sum of external forces (calculate_external_force)
+    const double* torque;    // [3N] sum of external torques (calculate_external_torque)
+    // ---- geometry -------------------------------------------------------------------------
+    const Collider* colliders;
+    const Shape* shapes;
+    const double* shape_verts;   // [3 * total verts] local vertices
+    const double* face_normal;   // [3 * total faces] local face normals
+    const int32_t* face_elem_start;  // [total faces + num shapes] CSR starts (per shape: nf+1 entries)
+    const int32_t* face_elem;        // vertex indices of faces
+    const int32_t* csr_start;        // shared CSR start table for v2f / v2n / f2n
+    const int32_t* csr_data;
+    R* tverts;       // [3 * total transformed verts] transformed hull vertices (per collider)
+    R* tnorms;       // [3 * total transformed normals]
+    // ---- constraints ----------------------------------------------------------------------
+    const ExtConstraint* ext;
+    // ---- scratch ---------------------------------------------------------------------------
+    int32_t* pair_count;     // [S] pairs found this step
+    int2* pairs;             // broad-phase pairs (global body indices), in reference order
+    int32_t* row_count;      // [N] broad-phase counts per row (scan workspace)
+    int32_t* uf_parent;      // [N] union-find parents (global body indices)
+    uint8_t* island_awake;   // [N] per-root flag
+    int32_t* node_body;      // [2 * nodes] the node's two bodies (-1 when fixed)
+    int32_t* node_pred;      // [2 * nodes] predecessor node on each body (-1: none)
+    int32_t* node_level;     // [nodes]
+    int32_t* body_tl_count;  // [N] timeline lengths / fill counters
+    int32_t* body_tl_start;  // [N+1] timeline CSR starts (per scene relative to node base)
+    int32_t* body_tl;        // [2 * nodes] timeline entries
+    int32_t* level_count;    // [S * (max_levels+1)] nodes per level, then prefix
+    int32_t* level_fill;     // [S * (max_levels+1)] fill counters; the last three words are flags
+    int32_t* scan_tmp;       // [grid blocks] group-scan partial sums
+    int32_t* level_nodes;    // [nodes] nodes sorted by level
+    int32_t* scene_levels;   // [S] number of levels
+    int32_t* scene_nodes;    // [S] number of live nodes (ext + pairs)
+    int32_t* pair_cstart;    // [pairs] first contact of each pair
+    int32_t* pair_ccount;    // [pairs]
+    int32_t* contact_count;  // [S] contacts allocated this substep
+    R* contacts;             // [12 * contacts] r1_lc, lambda_n, r2_lc, lambda_t, normal, (unused)
+    double* ext_lambda;      // [4 * ext] per-substep lambdas of external constraints
+    int32_t max_levels;
+    // ---- control ----------------------------------------------------------------------------
+    uint32_t* status;        // [S] status bits per scene
+    unsigned int* barrier;   // [2] grid barrier counter / generation
+    unsigned long long* counters; // [8] diagnostics: gjk/epa iterations, contacts, ...
+};
+
+}  // namespace rp

@@ -1,0 +1,293 @@
+"""Python binding of the GB300 rigid-body step (the C ABI of include/rp.h) via ctypes.
+
+The library is built in place by raw-physics_gb300/build.py; importing this package never builds
+or falls back to anything: World() raises if librawphys_gb300.so is missing or no CUDA device is
+present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "librawphys_gb300.so")
+
+STATE_DOUBLES = 28
+CONTACT_DOUBLES = 9
+PRECISION = {"fp32": 0, "fp64": 1}
+COLLIDER_SPHERE, COLLIDER_HULL = 0, 1
+ERRORS = {0: "RP_OK", -1: "RP_ERR_INVALID", -2: "RP_ERR_CUDA", -3: "RP_ERR_NO_DEVICE", -4: "RP_ERR_CAPACITY",
+          -5: "RP_ERR_DEGENERATE", -6: "RP_ERR_TIMEOUT", -7: "RP_ERR_STATE"}
+STATUS_BITS = {1 << 0: "PAIR_OVERFLOW", 1 << 1: "CONTACT_OVERFLOW", 1 << 2: "EPA_OVERFLOW", 1 << 3: "CLIP_OVERFLOW",
+               1 << 4: "BARRIER_TIMEOUT", 1 << 5: "DEGENERATE", 1 << 6: "LEVEL_OVERFLOW", 1 << 8: "EPA_NOT_CONVERGED"}
+
+# every exported symbol of include/rp.h with its ctypes signature
+_d, _i, _u, _u64 = C.c_double, C.c_int32, C.c_uint32, C.c_uint64
+_P = C.POINTER
+_W = C.c_void_p
+
+
+class ColliderDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("hull", C.c_int32), ("radius", C.c_float)]
+
+
+SIGNATURES = {
+    "rp_world_create": (_i, [_P(_W), _i, _i]),
+    "rp_world_destroy": (None, [_W]),
+    "rp_world_set_stream": (_i, [_W, C.c_void_p]),
+    "rp_last_error": (C.c_char_p, []),
+    "rp_scene_create": (_i, [_W, _P(_i)]),
+    "rp_hull_create": (_i, [_W, _P(_d), _u, _P(_u), _u, _P(_i)]),
+    "rp_hull_create_from_topology": (_i, [_W, _P(_d), _i, _P(_d), _i, _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i),
+                                          _P(_i), _P(_i), _P(_i)]),
+    "rp_hull_info": (_i, [_W, _i, _P(_i), _P(_i)]),
+    "rp_hull_face": (_i, [_W, _i, _i, _P(_d), _P(_i), _i, _P(_i)]),
+    "rp_entity_create": (_i, [_W, _i, _P(_d), _P(_d), _d, _i, _P(ColliderDesc), _u, _d, _d, _d, _P(_i)]),
+    "rp_entity_set_velocity": (_i, [_W, _i, _P(_d), _P(_d)]),
+    "rp_entity_add_force": (_i, [_W, _i, _P(_d), _P(_d), _i]),
+    "rp_entity_clear_forces": (_i, [_W, _i]),
+    "rp_world_set_gravity": (_i, [_W, _d]),
+    "rp_entity_get_mass_properties": (_i, [_W, _i, _P(_d), _P(_d), _P(_d), _P(_d)]),
+    "rp_entity_set_mass_properties": (_i, [_W, _i, _d, _P(_d), _P(_d), _d]),
+    "rp_num_entities": (_i, [_W]),
+    "rp_constraint_positional": (_i, [_W, _i, _i, _P(_d), _P(_d), _d, _P(_d), _P(_i)]),
+    "rp_constraint_mutual_orientation": (_i, [_W, _i, _i, _d, _P(_i)]),
+    "rp_constraint_hinge": (_i, [_W, _i, _i, _P(_d), _P(_d), _d, _i, _i, _i, _i, _i, _d, _d, _P(_i)]),
+    "rp_constraint_spherical": (_i, [_W, _i, _i, _P(_d), _P(_d), _i, _i, _i, _i, _d, _d, _d, _d, _P(_i)]),
+    "rp_simulate": (_i, [_W, _d, _u, _u, _i, _u]),
+    "rp_sync": (_i, [_W]),
+    "rp_last_status": (_i, [_W, _P(_u)]),
+    "rp_state_get": (_i, [_W, _P(_d)]),
+    "rp_state_set": (_i, [_W, _P(_d)]),
+    "rp_broad_pairs": (_i, [_W, _i, _P(_u), _u, _P(_u)]),
+    "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
+    "rp_counters": (_i, [_W, _P(_u64)]),
+    "rp_kernel_launches": (_u64, [_W]),
+    "rp_set_timing": (_i, [_W, _i]),
+    "rp_last_step_ms": (_i, [_W, _P(_d)]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load librawphys_gb300.so and bind every C ABI symbol (raises if the library is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("raw-physics GB300 extension not built: %s (run raw-physics_gb300/build.py)" % path)
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class RPError(RuntimeError):
+    pass
+
+
+def _dp(a):
+    return a.ctypes.data_as(_P(_d))
+
+
+def _arr(v, n=3):
+    return (C.c_double * n)(*[float(x) for x in v])
+
+
+class World:
+    """One rp_world: a set of scenes stepped together on one GPU."""
+
+    def __init__(self, device: int = 0, precision: str = "fp32"):
+        self.lib = load_library()
+        self.h = _W()
+        self._check(self.lib.rp_world_create(C.byref(self.h), device, PRECISION[precision]))
+        self.precision = precision
+        self.scene = None
+        self._hulls = {}
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.rp_last_error().decode()
+            raise RPError("%s: %s" % (ERRORS.get(rc, rc), msg))
+        return rc
+
+    def close(self):
+        if self.h:
+            self.lib.rp_world_destroy(self.h)
+            self.h = _W()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- construction ----------------------------------------------------------------------
+    def new_scene(self) -> int:
+        s = _i()
+        self._check(self.lib.rp_scene_create(self.h, C.byref(s)))
+        return s.value
+
+    def hull(self, vertices: np.ndarray, indices: np.ndarray) -> int:
+        v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        out = _i()
+        self._check(self.lib.rp_hull_create(self.h, _dp(v), v.shape[0], idx.ctypes.data_as(_P(_u)), idx.shape[0],
+                                            C.byref(out)))
+        return out.value
+
+    def hull_faces(self, hull: int):
+        nv, nf = _i(), _i()
+        self._check(self.lib.rp_hull_info(self.h, hull, C.byref(nv), C.byref(nf)))
+        faces = []
+        for f in range(nf.value):
+            n = (C.c_double * 3)()
+            el = (C.c_int32 * 256)()
+            ne = _i()
+            self._check(self.lib.rp_hull_face(self.h, hull, f, n, el, 256, C.byref(ne)))
+            faces.append((tuple(n), list(el[: ne.value])))
+        return nv.value, faces
+
+    def entity(self, scene, pos, rot, mass, fixed, colliders, mus, mud, rest) -> int:
+        arr = (ColliderDesc * len(colliders))(*colliders)
+        out = _i()
+        self._check(self.lib.rp_entity_create(self.h, scene, _arr(pos), _arr(rot, 4), float(mass), int(fixed), arr,
+                                              len(colliders), float(mus), float(mud), float(rest), C.byref(out)))
+        return out.value
+
+    def set_velocity(self, e, v, w):
+        self._check(self.lib.rp_entity_set_velocity(self.h, e, _arr(v), _arr(w)))
+
+    def add_force(self, e, position, force, local=False):
+        self._check(self.lib.rp_entity_add_force(self.h, e, _arr(position), _arr(force), int(local)))
+
+    def set_gravity(self, g: float):
+        self._check(self.lib.rp_world_set_gravity(self.h, float(g)))
+
+    def mass_properties(self, e):
+        invm = _d()
+        I, Ii = (C.c_double * 9)(), (C.c_double * 9)()
+        r = _d()
+        self._check(self.lib.rp_entity_get_mass_properties(self.h, e, C.byref(invm), I, Ii, C.byref(r)))
+        return invm.value, np.array(I[:]).reshape(3, 3), np.array(Ii[:]).reshape(3, 3), r.value
+
+    def constraint(self, c, base: int = 0):
+        o = _i()
+        e1, e2 = base + c.e1, base + c.e2
+        if c.kind == "positional":
+            rc = self.lib.rp_constraint_positional(self.h, e1, e2, _arr(c.r1), _arr(c.r2), c.compliance, _arr(c.distance), C.byref(o))
+        elif c.kind == "mutual_orientation":
+            rc = self.lib.rp_constraint_mutual_orientation(self.h, e1, e2, c.compliance, C.byref(o))
+        elif c.kind == "hinge":
+            rc = self.lib.rp_constraint_hinge(self.h, e1, e2, _arr(c.r1), _arr(c.r2), c.compliance, c.axis1, c.axis2,
+                                              int(c.limited), c.limit_axis1, c.limit_axis2, c.lower, c.upper, C.byref(o))
+        elif c.kind == "spherical":
+            rc = self.lib.rp_constraint_spherical(self.h, e1, e2, _arr(c.r1), _arr(c.r2), c.swing_axis1, c.swing_axis2,
+                                                  c.twist_axis1, c.twist_axis2, c.swing_lower, c.swing_upper,
+                                                  c.twist_lower, c.twist_upper, C.byref(o))
+        else:
+            raise ValueError(c.kind)
+        self._check(rc)
+        return o.value
+
+    def load(self, scene, scene_id: int = 0) -> int:
+        """Create every mesh hull, entity and constraint of a rawphys.scenes.Scene in scene_id.
+        Returns the index of the scene's first entity."""
+        first = None
+        for b in range(scene.num_bodies):
+            descs = []
+            for c in scene.colliders[b]:
+                if c.kind == "hull":
+                    m = scene.meshes[c.mesh]
+                    key = (id(m), tuple(c.scale))
+                    if key not in self._hulls:
+                        verts = m.positions.astype(np.float64) * np.asarray(c.scale, dtype=np.float64)
+                        self._hulls[key] = self.hull(verts, m.indices)
+                    descs.append(ColliderDesc(COLLIDER_HULL, self._hulls[key], 0.0))
+                else:
+                    descs.append(ColliderDesc(COLLIDER_SPHERE, -1, float(c.radius)))
+            e = self.entity(scene_id, scene.pos[b], scene.rot[b], scene.mass[b], scene.fixed[b], descs,
+                            scene.mus[b], scene.mud[b], scene.rest[b])
+            if first is None:
+                first = e
+            if np.any(scene.vel[b]) or np.any(scene.omega[b]):
+                self.set_velocity(e, scene.vel[b], scene.omega[b])
+        for c in scene.constraints:
+            self.constraint(c, base=first)
+        self.set_gravity(scene.gravity)
+        self.scene = scene
+        return first
+
+    # -- stepping and state ----------------------------------------------------------------
+    def simulate(self, dt, substeps, pos_iters=1, collisions=True, steps=1):
+        self._check(self.lib.rp_simulate(self.h, float(dt), int(substeps), int(pos_iters), int(bool(collisions)), int(steps)))
+
+    def step(self, n: int = 1):
+        s = self.scene
+        self.simulate(s.dt, s.substeps, s.pos_iters, s.collisions, n)
+
+    def sync(self):
+        self._check(self.lib.rp_sync(self.h))
+
+    def num_entities(self) -> int:
+        return int(self.lib.rp_num_entities(self.h))
+
+    def get_state(self) -> np.ndarray:
+        out = np.zeros((self.num_entities(), STATE_DOUBLES))
+        self._check(self.lib.rp_state_get(self.h, _dp(out)))
+        return out
+
+    def set_state(self, st: np.ndarray):
+        st = np.ascontiguousarray(st, dtype=np.float64)
+        assert st.shape == (self.num_entities(), STATE_DOUBLES)
+        self._check(self.lib.rp_state_set(self.h, _dp(st)))
+
+    def status(self) -> int:
+        b = _u()
+        self._check(self.lib.rp_last_status(self.h, C.byref(b)))
+        return b.value
+
+    def broad_pairs(self, scene: int = 0) -> np.ndarray:
+        cap = 1 << 16
+        while True:
+            out = np.zeros(2 * cap, dtype=np.uint32)
+            n = _u()
+            rc = self.lib.rp_broad_pairs(self.h, scene, out.ctypes.data_as(_P(_u)), cap, C.byref(n))
+            if rc == 0 and n.value <= cap:
+                return out[: 2 * n.value].reshape(-1, 2)
+            if rc not in (0, -4):
+                self._check(rc)
+            cap = max(2 * cap, int(n.value))
+            if cap > (1 << 26):
+                self._check(rc)
+
+    def contacts(self, e1: int, e2: int) -> np.ndarray:
+        cap = 64
+        out = np.zeros(cap * CONTACT_DOUBLES)
+        n = _u()
+        self._check(self.lib.rp_contacts(self.h, e1, e2, _dp(out), cap, C.byref(n)))
+        return out[: min(n.value, cap) * CONTACT_DOUBLES].reshape(-1, CONTACT_DOUBLES)
+
+    def counters(self):
+        out = (C.c_uint64 * 8)()
+        self._check(self.lib.rp_counters(self.h, out))
+        return list(out)
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.rp_kernel_launches(self.h))
+
+    def set_timing(self, on: bool):
+        self._check(self.lib.rp_set_timing(self.h, int(on)))
+
+    def last_step_ms(self) -> float:
+        v = _d()
+        self._check(self.lib.rp_last_step_ms(self.h, C.byref(v)))
+        return v.value
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.lib.rp_world_set_stream(self.h, C.c_void_p(stream_ptr)))
