@@ -1,0 +1,313 @@
+"""Benchmark of the GB300 rigid-body step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload large4096|stack10|batched]
+
+Workload (default): the single large scene — 4096 convex bodies (cube / icosahedron / 32-segment
+cylinder / 42-vertex icosphere, scale U(0.5,1.5), density 1) in a fixed 40x40x60 m box, dt=1/60,
+20 substeps, 1 position iteration, FP32 build with FP64 poses; seeded synthetic data. The scene is
+first advanced `--settle` frames (untimed) so the timed frames see the falling / colliding regime,
+then W warm-up frames, then K timed frames. A "step" is one pbd_simulate frame.
+
+Printed JSON line (rank 0):
+  value     body-substeps/s = dynamic bodies x substeps x K / summed device time of the K frames
+            (CUDA events on the world's stream; L2 flushed with a 256 MiB write before every frame)
+  e2e       the same metric through the C ABI with host buffers: every frame uploads the full body
+            state (rp_state_set), steps, and downloads it (rp_state_get), copies inside the timer
+  roofline  the step kernel's algorithmic bytes per launch / its average duration, against the
+            measured HBM copy bandwidth
+  cpu_baseline  the oracle port (plain-C restatement of the reference, bit-exact to it) on one host
+            core, on a bounded sample of the same workload
+--impl reference times that CPU implementation on every host core instead (one replica of the
+workload per core; the reference is single-threaded and keeps process-global state).
+Multi-GPU (torchrun): the single scene does not shard, so every rank steps its own replica
+("replicas only"); value is the sum over ranks of body-substeps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-substeps/s batched vs plain GPU at ≤1e-4 m pos err vs FP64 CPU; grad/s"
+UNIT = "body-substeps/s"
+# Algorithmic bytes of the plain form (per substep): body state read + written, the pair list, and
+# every contact record written once and read by the position and velocity solves.
+STATE_READ_B, STATE_WRITE_B, PAIR_B, CONTACT_B = 160, 84, 16, 156
+
+
+def make_scene(name):
+    from rawphys import scenes as S
+    if name == "stack10":
+        return S.stack_scene(10, seed=0)
+    return S.large_scene(4096, seed=0)
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(", ") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per step-kernel launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_large4096.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline_sample(scene, state, frames=3):
+    """The oracle port on one core: body-substeps/s over `frames` frames of the workload, started
+    from the state the timed GPU frames started from."""
+    from oracle.oracle import Oracle, build
+    build(ref=False)
+    o = Oracle("port").load(scene)
+    o.set_state(state)
+    t = time.perf_counter()
+    o.step(frames)
+    dt = time.perf_counter() - t
+    return scene.num_dynamic * scene.substeps * frames / dt, dt
+
+
+_WORKER = {}
+
+
+def _ref_init(name, state):
+    sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    scene = make_scene(name)
+    _WORKER["scene"] = scene
+    _WORKER["oracle"] = Oracle("port").load(scene)
+    _WORKER["state"] = state
+
+
+def _ref_frame(frames):
+    o, scene = _WORKER["oracle"], _WORKER["scene"]
+    o.set_state(_WORKER["state"])
+    t = time.perf_counter()
+    o.step(frames)
+    return scene.num_dynamic * scene.substeps * frames, time.perf_counter() - t
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle.oracle import Oracle, build
+    build(ref=False)
+    cores = os.cpu_count() or 1
+    scene = make_scene(args.workload)
+    # the same settled frames the GPU arm times, settled by the CPU implementation itself
+    o = Oracle("port").load(scene)
+    o.step(args.settle)
+    state = o.get_state()
+    frames = 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(args.workload, state)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_frame, [frames] * cores)
+        t = time.perf_counter()
+        total = 0
+        for _ in range(args.steps):
+            total += sum(b for b, _ in pool.map(_ref_frame, [frames] * cores))
+        wall = time.perf_counter() - t
+    value = total / wall
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": "%s: %d dynamic bodies, %d substeps, dt=1/60, 1 position iteration; frame %d "
+                                   "(after a %d-frame settle), one frame per core per step"
+                                   % (args.workload, scene.num_dynamic, scene.substeps, args.settle + 1, args.settle)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d replicas x %d frame(s) per step of the workload, oracle port (bit-exact "
+                                       "restatement of the reference, -O2 -ffp-contract=off)" % (cores, frames)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import rawphys
+    rank, world_size, local = dist_info()
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = local
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    scene = make_scene(args.workload)
+    w = rawphys.World(dev, "fp32")
+    w.set_stream(stream.cuda_stream)
+    w.load(scene)
+    nd = scene.num_dynamic
+    # untimed: settle into the colliding regime, then warm up
+    if args.settle:
+        w.step(args.settle)
+    w.step(args.warmup)
+    w.sync()
+    start_state = w.get_state()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    c0 = w.counters()
+    p0 = w.phase_times()
+    l0 = w.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)                  # evict L2 (129 MB) before each timed frame
+            ev[k][0].record(stream)
+            w.step(1)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    if world_size > 1:
+        torch.distributed.barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(ms))
+    launches = w.kernel_launches() - l0
+    c1 = w.counters()
+    p1 = w.phase_times()
+    phase_ms = {k: round((p1[k] - p0[k]) / args.steps, 4) for k in p0}
+    # slowest rank
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = nd * scene.substeps * args.steps * world_size / (total_ms / 1e3)
+    status = w.status()
+
+    # roofline of the step kernel: algorithmic bytes per launch over its measured duration
+    pairs_per_step = (c1[6] - c0[6]) / args.steps
+    contacts_per_step = (c1[5] - c0[5]) / args.steps
+    alg_bytes = scene.substeps * (STATE_READ_B + STATE_WRITE_B) * nd + scene.substeps * PAIR_B * pairs_per_step + \
+        CONTACT_B * contacts_per_step
+    launch_ms = total_ms / max(launches, 1) if world_size == 1 else total_ms / args.steps
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    traffic = profile_traffic()
+
+    # end to end through the C ABI with host buffers
+    st = w.get_state()
+    b0 = w.transfer_bytes()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        w.set_state(st)
+        w.step(1)
+        st = w.get_state()
+    e2e_wall = time.perf_counter() - t
+    b1 = w.transfer_bytes()
+    e2e = {"value": nd * scene.substeps * e2e_steps * world_size / e2e_wall, "unit": UNIT,
+           "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_steps, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_steps}
+
+    if rank == 0:
+        cpu_v, cpu_t = cpu_baseline_sample(scene, start_state, frames=args.cpu_frames)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+                "config": {"workload": "large single scene: %d dynamic bodies (cube/icosahedron/cylinder32/icosphere42, "
+                                       "scale U(0.5,1.5)) in a 40x40x60 m box, dt=1/60, %d substeps, 1 position iteration, "
+                                       "FP32 with FP64 poses; frames %d-%d after a %d-frame settle"
+                                       % (nd, scene.substeps, args.settle + args.warmup,
+                                          args.settle + args.warmup + args.steps, args.settle),
+                           "l2": "flushed (256 MiB write) before every timed frame",
+                           "parallelism": "replicas only" if world_size > 1 else "single scene, one GPU",
+                           "pairs_per_step": pairs_per_step, "contacts_per_step": contacts_per_step,
+                           "levels_per_step": (c1[7] - c0[7]) / args.steps,
+                           "phase_ms_per_step": phase_ms},
+                "gpu_launches": launches,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "peak_kind": peak_kind, "traffic": traffic,
+                             "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
+                "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
+                                 "sample": "%d frames of the same scene from the state the timed GPU frames start "
+                                           "from, oracle port (bit-exact restatement of the reference), %.1f s"
+                                           % (args.cpu_frames, cpu_t)},
+                "e2e": e2e, "clocks": clk.summary(), "device_status": status}
+        print(json.dumps(line), flush=True)
+    if world_size > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--settle", type=int, default=120)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large4096", choices=["large4096", "stack10"])
+    ap.add_argument("--cpu-frames", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -71,6 +71,9 @@ typedef struct {
 } rp_collider_desc;
 
 /* -- world ------------------------------------------------------------------------------------ */
+/* device >= 0: a world on that CUDA device (a GPU of compute capability 10.x or newer is required).
+ * device == -1: a host-only world for set-up queries (hulls, mass properties, state snapshots);
+ * any call that needs the GPU then returns RP_ERR_NO_DEVICE. */
 rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision);
 void      rp_world_destroy(rp_world* w);
 /* Use an existing cudaStream_t (passed as void*) for every launch and copy of this world. */
@@ -96,6 +99,13 @@ rp_status rp_hull_create_from_topology(rp_world* w, const double* vertices, int3
                                        int32_t* out_hull);
 /* Topology queries of a built hull (for tests): counts, then the arrays. */
 rp_status rp_hull_info(rp_world* w, int32_t hull, int32_t* num_vertices, int32_t* num_faces);
+/* One topology table of a hull in CSR form: which = 0 face boundary loops, 1 vertex->faces,
+ * 2 vertex->neighbours, 3 face->neighbours. start_out gets rows+1 entries, data_out the entries;
+ * either may be NULL to query *num_rows / *num_data first. */
+rp_status rp_hull_topology(rp_world* w, int32_t hull, int32_t which, int32_t* start_out, int32_t* data_out, int32_t cap,
+                           int32_t* num_rows, int32_t* num_data);
+/* Unique vertices (3 per vertex) and face normals (3 per face) of a hull, FP64. */
+rp_status rp_hull_geometry(rp_world* w, int32_t hull, double* vertices_out, double* normals_out);
 rp_status rp_hull_face(rp_world* w, int32_t hull, int32_t face, double normal[3], int32_t* elements, int32_t cap,
                        int32_t* num_elements);
 
@@ -106,8 +116,8 @@ rp_status rp_entity_create(rp_world* w, int32_t scene, const double position[3],
                            int32_t fixed, const rp_collider_desc* colliders, uint32_t num_colliders,
                            double static_friction, double dynamic_friction, double restitution, int32_t* out_entity);
 rp_status rp_entity_set_velocity(rp_world* w, int32_t entity, const double linear[3], const double angular[3]);
-/* entity_add_force: applies to the next rp_simulate only, as the reference's callers clear forces
- * after every frame (src/examples/stack.cpp:100-102). */
+/* entity_add_force: applies to every frame of the next rp_simulate call and is then cleared, as the
+ * reference's callers clear forces after every frame (src/examples/stack.cpp:100-102). */
 rp_status rp_entity_add_force(rp_world* w, int32_t entity, const double position[3], const double force[3],
                               int32_t local_coords);
 rp_status rp_entity_clear_forces(rp_world* w, int32_t entity);
@@ -168,10 +178,18 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out_pairs, uint32
  * the device narrowphase. out: RP_CONTACT_DOUBLES per contact. */
 rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
 /* Counters accumulated since creation: [0] GJK iterations, [1] EPA iterations, [2] EPA calls,
- * [3] steps, [4] substeps, [5] contacts generated (last step), [6] pairs (last step), [7] levels (last step). */
+ * [3] steps, [4] substeps, [5] contacts generated, [6] broad-phase pairs (summed over steps),
+ * [7] solver levels (summed over steps). */
 rp_status rp_counters(rp_world* w, uint64_t out[8]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */
 uint64_t  rp_kernel_launches(const rp_world* w);
+/* Device time per phase of the step kernel since creation, in ms, as seen by the first thread of
+ * each scene's group (summed over scenes): [0] broad phase, [1] islands and sleeping, [2] solver
+ * schedule, [3] predict, [4] hull transform, [5] narrowphase, [6] position solve, [7] velocity
+ * update, [8] velocity solve. */
+rp_status rp_phase_times(rp_world* w, double out_ms[9]);
+/* Bytes copied host->device (out[0]) and device->host (out[1]) by state and force transfers. */
+rp_status rp_transfer_bytes(rp_world* w, uint64_t out[2]);
 /* Average duration of the step kernel over the last rp_simulate, measured with CUDA events on the
  * world's stream (milliseconds per launch; 0 if timing is off). */
 rp_status rp_set_timing(rp_world* w, int32_t enabled);

@@ -49,6 +49,13 @@ double   orc_entity_get_inverse_mass(int entity);
 void     orc_entity_get_inertia(int entity, double inertia[9], double inverse_inertia[9]);
 double   orc_entity_get_radius(int entity);
 
+/* Topology of collider k of an entity (convex hulls): which = 0 face loops, 1 vertex->faces,
+ * 2 vertex->neighbours, 3 face->neighbours, as CSR (start gets rows+1 entries; data up to cap).
+ * Returns the number of rows; *ndata receives the number of entries. */
+int      orc_hull_topology(int entity, int k, int which, int32_t* start, int32_t* data, int32_t cap, int32_t* ndata);
+/* Unique vertices (3 each) and face normals (3 each) of collider k; returns nv, *nf receives nf. */
+int      orc_hull_geometry(int entity, int k, double* verts, double* normals, int32_t cap_vertices, int32_t cap_faces, int32_t* nf);
+
 /* Constraint initialisers (src/physics/pbd.h:96-102). Axis values follow PBD_Axis_Type. */
 int orc_constraint_positional(int e1, int e2, const double r1[3], const double r2[3], double compliance, const double distance[3]);
 int orc_constraint_mutual_orientation(int e1, int e2, double compliance);

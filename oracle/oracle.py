@@ -71,6 +71,8 @@ class Oracle:
                 "orc_broad_pairs": (u, [P(u), u]),
                 "orc_contacts": (u, [i, i, P(d), u]),
                 "orc_gjk_epa": (i, [i, i, P(d)]),
+                "orc_hull_topology": (i, [i, i, i, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
+                "orc_hull_geometry": (i, [i, i, P(d), P(d), C.c_int32, C.c_int32, P(C.c_int32)]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -171,6 +173,24 @@ class Oracle:
         out = np.zeros(cap * CONTACT_DOUBLES)
         n = self.lib.orc_contacts(e1, e2, out.ctypes.data_as(C.POINTER(C.c_double)), cap)
         return out[: min(n, cap) * CONTACT_DOUBLES].reshape(-1, CONTACT_DOUBLES)
+
+    def hull_topology(self, e: int, k: int = 0):
+        """(vertices (nv,3), normals (nf,3), {table: (start, data)}) of collider k of entity e."""
+        nf = C.c_int32()
+        nv = self.lib.orc_hull_geometry(e, k, None, None, 0, 0, C.byref(nf))
+        verts, normals = np.zeros((nv, 3)), np.zeros((nf.value, 3))
+        self.lib.orc_hull_geometry(e, k, verts.ctypes.data_as(C.POINTER(C.c_double)),
+                                   normals.ctypes.data_as(C.POINTER(C.c_double)), nv, nf.value, C.byref(nf))
+        tables = {}
+        for which in range(4):
+            nd = C.c_int32()
+            rows = self.lib.orc_hull_topology(e, k, which, None, None, 0, C.byref(nd))
+            start = np.zeros(rows + 1, dtype=np.int32)
+            data = np.zeros(max(nd.value, 1), dtype=np.int32)
+            self.lib.orc_hull_topology(e, k, which, start.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       data.ctypes.data_as(C.POINTER(C.c_int32)), nd.value, C.byref(nd))
+            tables[which] = (start, data[: nd.value])
+        return verts, normals, tables
 
     def gjk_epa(self, e1: int, e2: int):
         out = np.zeros(4)

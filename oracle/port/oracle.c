@@ -464,6 +464,31 @@ void orc_entity_get_inertia(int i, double I[9], double Iinv[9]) {
 }
 double orc_entity_get_radius(int i) { return g_bodies[i].radius; }
 
+int orc_hull_topology(int i, int k, int which, int32_t* start, int32_t* data, int32_t cap, int32_t* ndata) {
+    const collider_t* c = &g_bodies[i].col[k];
+    int rows = (which == 0 || which == 3) ? c->nf : c->nv;
+    int32_t n = 0;
+    for (int r = 0; r < rows; ++r) {
+        const ivec* row = which == 0 ? &c->f[r].elements : which == 1 ? &c->v2f[r] : which == 2 ? &c->v2n[r] : &c->f2n[r];
+        if (start) start[r] = n;
+        for (int q = 0; q < row->n; ++q) {
+            if (data && n < cap) data[n] = row->a[q];
+            ++n;
+        }
+    }
+    if (start) start[rows] = n;
+    if (ndata) *ndata = n;
+    return rows;
+}
+
+int orc_hull_geometry(int i, int k, double* verts, double* normals, int32_t capv, int32_t capf, int32_t* nf) {
+    const collider_t* c = &g_bodies[i].col[k];
+    for (int v = 0; v < c->nv && v < capv; ++v) { verts[3 * v] = c->v[v].x; verts[3 * v + 1] = c->v[v].y; verts[3 * v + 2] = c->v[v].z; }
+    for (int j = 0; j < c->nf && j < capf; ++j) { normals[3 * j] = c->f[j].normal.x; normals[3 * j + 1] = c->f[j].normal.y; normals[3 * j + 2] = c->f[j].normal.z; }
+    if (nf) *nf = c->nf;
+    return c->nv;
+}
+
 static constraint_t* new_constraint(int type, int e1, int e2) {
     if (g_nc == g_ccap) { g_ccap = g_ccap ? 2 * g_ccap : 8; g_cons = (constraint_t*)realloc(g_cons, sizeof(constraint_t) * (size_t)g_ccap); }
     constraint_t* c = &g_cons[g_nc++];

@@ -148,6 +148,33 @@ void orc_entity_get_inertia(int i, double inertia[9], double inverse_inertia[9])
 
 double orc_entity_get_radius(int i) { return ent(i)->bounding_sphere_radius; }
 
+int orc_hull_topology(int i, int k, int which, int32_t* start, int32_t* data, int32_t cap, int32_t* ndata) {
+    const Collider_Convex_Hull& h = ent(i)->colliders[k].convex_hull;
+    int rows = which == 0 || which == 3 ? (int)array_length(h.faces) : (int)array_length(h.vertices);
+    int32_t n = 0;
+    for (int r = 0; r < rows; ++r) {
+        const u32* row = which == 0 ? h.faces[r].elements : which == 1 ? h.vertex_to_faces[r]
+                       : which == 2 ? h.vertex_to_neighbors[r] : h.face_to_neighbors[r];
+        if (start) start[r] = n;
+        for (u32 c = 0; c < array_length(row); ++c) {
+            if (data && n < cap) data[n] = (int32_t)row[c];
+            ++n;
+        }
+    }
+    if (start) start[rows] = n;
+    if (ndata) *ndata = n;
+    return rows;
+}
+
+int orc_hull_geometry(int i, int k, double* verts, double* normals, int32_t capv, int32_t capf, int32_t* nf) {
+    const Collider_Convex_Hull& h = ent(i)->colliders[k].convex_hull;
+    int nv = (int)array_length(h.vertices), f = (int)array_length(h.faces);
+    for (int v = 0; v < nv && v < capv; ++v) { verts[3 * v] = h.vertices[v].x; verts[3 * v + 1] = h.vertices[v].y; verts[3 * v + 2] = h.vertices[v].z; }
+    for (int j = 0; j < f && j < capf; ++j) { normals[3 * j] = h.faces[j].normal.x; normals[3 * j + 1] = h.faces[j].normal.y; normals[3 * j + 2] = h.faces[j].normal.z; }
+    if (nf) *nf = f;
+    return nv;
+}
+
 static void push_constraint(const Constraint& c) {
     if (!g_constraints) g_constraints = array_new(Constraint);
     array_push(g_constraints, c);

@@ -9,7 +9,9 @@
 #include "rp_launch.h"
 #include "rp_world.h"
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -113,9 +115,10 @@ struct rp_world {
     DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_contacts, d_ext_lambda, d_status, d_barrier,
-        d_counters, d_kat_out, d_kat_count;
+        d_counters, d_phase, d_kat_out, d_kat_count;
 
     uint64_t launches = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
     uint64_t steps = 0, substeps = 0;
     uint32_t status_accum = 0;
     bool timing = false;
@@ -201,12 +204,15 @@ rp_status build_device(rp_world* w) {
     w->scene_contact_cap.assign((size_t)S + 1, 0);
     w->scene_node_cap.assign((size_t)S + 1, 0);
     int max_bodies = 0;
+    // RP_SCRATCH_SCALE (tests only) shrinks the initial scratch so the overflow-and-regrow path runs
+    const char* scale_env = std::getenv("RP_SCRATCH_SCALE");
+    const double scale = scale_env ? std::max(1e-6, std::atof(scale_env)) : 1.0;
     for (int s = 0; s < S; ++s) {
         long long n = w->scene_body[(size_t)s + 1] - w->scene_body[(size_t)s];
         max_bodies = std::max(max_bodies, (int)n);
         long long all = n * (n - 1) / 2;
-        long long pc = std::min(all, (long long)(std::max(1024.0, 48.0 * (double)n) * w->pair_mult));
-        long long cc = (long long)(std::max(256.0, 8.0 * (double)pc) * w->contact_mult);
+        long long pc = std::min(all, std::max(1LL, (long long)(std::max(1024.0, 48.0 * (double)n) * w->pair_mult * scale)));
+        long long cc = std::max(1LL, (long long)(std::max(256.0, 8.0 * (double)pc) * w->contact_mult * scale));
         if (pc > (1LL << 30) || cc > (1LL << 30)) return fail(RP_ERR_CAPACITY, "scratch sizes beyond 2^30 entries");
         w->scene_pair_cap[(size_t)s + 1] = w->scene_pair_cap[(size_t)s] + (int32_t)pc;
         w->scene_contact_cap[(size_t)s + 1] = w->scene_contact_cap[(size_t)s] + (int32_t)cc;
@@ -359,6 +365,8 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(cudaMemsetAsync(w->d_barrier.p, 0, 64, st));
         RP_CUDA(w->d_counters.ensure(8 * 8));
         RP_CUDA(cudaMemsetAsync(w->d_counters.p, 0, 64, st));
+        RP_CUDA(w->d_phase.ensure(PHASES * 8));
+        RP_CUDA(cudaMemsetAsync(w->d_phase.p, 0, PHASES * 8, st));
     }
     RP_CUDA(w->d_status.ensure((size_t)S * 4));
     RP_CUDA(cudaMemsetAsync(w->d_status.p, 0, (size_t)S * 4, st));
@@ -437,6 +445,7 @@ WorldView<R> make_view(rp_world* w) {
     V.status = w->d_status.as<uint32_t>();
     V.barrier = w->d_barrier.as<unsigned int>();
     V.counters = w->d_counters.as<unsigned long long>();
+    V.phase_ns = w->d_phase.as<unsigned long long>();
     return V;
 }
 
@@ -475,6 +484,7 @@ rp_status upload_state(rp_world* w) {
         deact[slot] = b.deact;
     }
     cudaStream_t st = w->stream;
+    w->h2d_bytes += N * (4 * 32 + 4 * 3 * R + 1 + 8);
     RP_CUDA(upload(w->d_pos, pos, st));
     RP_CUDA(upload(w->d_rot, rot, st));
     RP_CUDA(upload(w->d_ppos, ppos, st));
@@ -520,6 +530,7 @@ rp_status sync_state_to_host(rp_world* w) {
         RP_CUDA(cudaMemcpyAsync(deact.data(), w->d_deact.p, N * 8, cudaMemcpyDeviceToHost, st));
         RP_CUDA(cudaMemcpyAsync(act.data(), w->d_active.p, N, cudaMemcpyDeviceToHost, st));
     }
+    w->d2h_bytes += N * (4 * 32 + 4 * 3 * R + 1 + 8);
     std::vector<double> vel = fetch(w->d_vel, 3 * N, R, st, e);
     if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
     std::vector<double> om = fetch(w->d_omega, 3 * N, R, st, e);
@@ -545,6 +556,7 @@ rp_status sync_state_to_host(rp_world* w) {
 }
 
 rp_status ensure_device(rp_world* w) {
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world (created with device -1)");
     if (w->static_dirty) {
         rp_status s = build_device(w);
         if (s != RP_OK) return s;
@@ -574,6 +586,7 @@ rp_status upload_forces(rp_world* w) {
         }
         for (int k = 0; k < 3; ++k) { F[3 * slot + (size_t)k] = f[k]; T[3 * slot + (size_t)k] = t[k]; }
     }
+    w->h2d_bytes += 2 * F.size() * sizeof(double);
     RP_CUDA(upload(w->d_force, F, w->stream));
     RP_CUDA(upload(w->d_torque, T, w->stream));
     RP_CUDA(cudaStreamSynchronize(w->stream));
@@ -628,6 +641,14 @@ rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision) {
     if (!out) return fail(RP_ERR_INVALID, "null out");
     *out = nullptr;
     if (precision != RP_PRECISION_FP32 && precision != RP_PRECISION_FP64) return fail(RP_ERR_INVALID, "bad precision");
+    if (device == -1) {
+        rp_world* hw = new rp_world();
+        hw->device = -1;
+        hw->precision = precision;
+        hw->scene_body.assign(2, 0);
+        *out = hw;
+        return RP_OK;
+    }
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(RP_ERR_NO_DEVICE, "no CUDA device");
     if (device < 0 || device >= n) return fail(RP_ERR_INVALID, "bad device index");
@@ -654,6 +675,10 @@ rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision) {
 
 void rp_world_destroy(rp_world* w) {
     if (!w) return;
+    if (w->device < 0) {
+        delete w;
+        return;
+    }
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
     if (w->ev0) cudaEventDestroy(w->ev0);
@@ -664,6 +689,7 @@ void rp_world_destroy(rp_world* w) {
 
 rp_status rp_world_set_stream(rp_world* w, void* stream) {
     if (check_world(w)) return RP_ERR_INVALID;
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     RP_CUDA(cudaStreamSynchronize(w->stream));
     if (w->own_stream) cudaStreamDestroy(w->stream);
     w->stream = (cudaStream_t)stream;
@@ -730,6 +756,36 @@ rp_status rp_hull_info(rp_world* w, int32_t hull, int32_t* nv, int32_t* nf) {
     if (check_world(w) || hull < 0 || hull >= (int32_t)w->hulls.size()) return fail(RP_ERR_INVALID, "bad hull");
     if (nv) *nv = w->hulls[(size_t)hull]->nv();
     if (nf) *nf = w->hulls[(size_t)hull]->nf();
+    return RP_OK;
+}
+
+rp_status rp_hull_topology(rp_world* w, int32_t hull, int32_t which, int32_t* start, int32_t* data, int32_t cap, int32_t* nrows,
+                           int32_t* ndata) {
+    if (check_world(w) || hull < 0 || hull >= (int32_t)w->hulls.size() || which < 0 || which > 3)
+        return fail(RP_ERR_INVALID, "bad hull or table");
+    const Hull& H = *w->hulls[(size_t)hull];
+    const std::vector<std::vector<int>>& t = which == 0 ? H.faces : which == 1 ? H.v2f : which == 2 ? H.v2n : H.f2n;
+    int32_t total = 0;
+    for (const auto& r : t) total += (int32_t)r.size();
+    if (nrows) *nrows = (int32_t)t.size();
+    if (ndata) *ndata = total;
+    int32_t k = 0;
+    for (size_t r = 0; r < t.size(); ++r) {
+        if (start) start[r] = k;
+        for (int x : t[r]) {
+            if (data && k < cap) data[k] = x;
+            ++k;
+        }
+    }
+    if (start) start[t.size()] = k;
+    return RP_OK;
+}
+
+rp_status rp_hull_geometry(rp_world* w, int32_t hull, double* verts, double* normals) {
+    if (check_world(w) || hull < 0 || hull >= (int32_t)w->hulls.size()) return fail(RP_ERR_INVALID, "bad hull");
+    const Hull& H = *w->hulls[(size_t)hull];
+    if (verts) std::memcpy(verts, H.verts.data(), H.verts.size() * sizeof(double));
+    if (normals) std::memcpy(normals, H.normals.data(), H.normals.size() * sizeof(double));
     return RP_OK;
 }
 
@@ -970,6 +1026,7 @@ rp_status rp_constraint_spherical(rp_world* w, int32_t e1, int32_t e2, const dou
 rp_status rp_simulate(rp_world* w, double dt, uint32_t substeps, uint32_t iters, int32_t collisions, uint32_t nsteps) {
     if (check_world(w)) return RP_ERR_INVALID;
     if (!std::isfinite(dt) || substeps == 0) return fail(RP_ERR_INVALID, "bad dt or substep count");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world (created with device -1)");
     if (w->bodies.empty() || nsteps == 0 || !(dt > 0.0)) return RP_OK;
     RP_CUDA(cudaSetDevice(w->device));
     rp_status s = ensure_device(w);
@@ -1026,6 +1083,7 @@ rp_status rp_simulate(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
 
 rp_status rp_sync(rp_world* w) {
     if (check_world(w)) return RP_ERR_INVALID;
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     RP_CUDA(cudaStreamSynchronize(w->stream));
     return RP_OK;
 }
@@ -1076,6 +1134,7 @@ rp_status rp_state_set(rp_world* w, const double* in) {
 
 rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out, uint32_t cap, uint32_t* count) {
     if (check_world(w) || scene < 0 || scene >= w->num_scenes || (!out && cap)) return fail(RP_ERR_INVALID, "bad argument");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     RP_CUDA(cudaSetDevice(w->device));
     rp_status s = ensure_device(w);
     if (s != RP_OK) return s;
@@ -1102,6 +1161,7 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out, uint32_t cap
 rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count) {
     if (check_world(w) || e1 < 0 || e2 < 0 || e1 >= (int32_t)w->bodies.size() || e2 >= (int32_t)w->bodies.size() || e1 == e2)
         return fail(RP_ERR_INVALID, "bad entity");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     RP_CUDA(cudaSetDevice(w->device));
     rp_status s = ensure_device(w);
     if (s != RP_OK) return s;
@@ -1136,8 +1196,9 @@ rp_status rp_counters(rp_world* w, uint64_t out[8]) {
         if (w->d_pair_count.p) RP_CUDA(cudaMemcpyAsync(&pc, w->d_pair_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
         if (w->d_scene_levels.p) RP_CUDA(cudaMemcpyAsync(&lv, w->d_scene_levels.p, 4, cudaMemcpyDeviceToHost, w->stream));
         RP_CUDA(cudaStreamSynchronize(w->stream));
+        (void)cc; (void)pc; (void)lv;
         out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
-        out[5] = (uint64_t)cc; out[6] = (uint64_t)pc; out[7] = (uint64_t)lv;
+        out[5] = c[3]; out[6] = c[5]; out[7] = c[6];
     }
     out[3] = w->steps;
     out[4] = w->substeps;
@@ -1145,6 +1206,24 @@ rp_status rp_counters(rp_world* w, uint64_t out[8]) {
 }
 
 uint64_t rp_kernel_launches(const rp_world* w) { return w ? w->launches : 0; }
+
+rp_status rp_phase_times(rp_world* w, double out[9]) {
+    if (check_world(w) || !out) return RP_ERR_INVALID;
+    for (int k = 0; k < PHASES; ++k) out[k] = 0.0;
+    if (!w->d_phase.p) return RP_OK;
+    unsigned long long ns[PHASES];
+    RP_CUDA(cudaMemcpyAsync(ns, w->d_phase.p, sizeof(ns), cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    for (int k = 0; k < PHASES; ++k) out[k] = (double)ns[k] * 1e-6;
+    return RP_OK;
+}
+
+rp_status rp_transfer_bytes(rp_world* w, uint64_t out[2]) {
+    if (check_world(w) || !out) return RP_ERR_INVALID;
+    out[0] = w->h2d_bytes;
+    out[1] = w->d2h_bytes;
+    return RP_OK;
+}
 
 rp_status rp_set_timing(rp_world* w, int32_t enabled) {
     if (check_world(w)) return RP_ERR_INVALID;

@@ -105,7 +105,16 @@ struct ColView {
     const V3<R>* norms;      // transformed face normals (global)
     int nv, nf;
     const Shape* shape;
+    Qt<double> q64;          // the body's orientation (FP64), for decisions made in FP64
 };
+
+// A face normal of a hull rotated by the body's FP64 orientation (collider_update's normal
+// transform, collider.cpp:425-429), for the FP32 build's FP64 reference-face decision.
+template <typename R>
+__device__ __forceinline__ V3<double> face_normal64(const WorldView<R>& W, const ColView<R>& c, int f) {
+    const double* n = W.face_normal + 3 * (c.shape->face_off + f);
+    return vnorm(mmulv(qmat3(c.q64), v3<double>(n[0], n[1], n[2])));
+}
 
 template <typename R>
 __device__ __forceinline__ V3<R> cv_vertex(const ColView<R>& c, int i) {
@@ -505,7 +514,7 @@ __device__ __forceinline__ int csr_len(const int32_t* start, int row) { return s
 // convex_convex_contact_manifold (clipping.cpp:249-341)
 template <typename R, bool EXACT>
 __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& h1, const ColView<R>& h2,
-                                       V3<R> normal, const PairFrame<R, EXACT>& fr) {
+                                       V3<R> normal, V3<double> normal64, const PairFrame<R, EXACT>& fr) {
     const unsigned lane = lane_id();
     V3<R> inv_n = vinv(normal);
     int s1 = support_index(h1, normal);
@@ -582,6 +591,13 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         return;
     }
     bool ref1 = d1 > d2;
+    if (!EXACT) {
+        // The reference face is the better-aligned of the two candidates (clipping.cpp:284). For
+        // nearly parallel faces d1 and d2 differ by ~1e-11, below FP32 resolution; decide it from
+        // FP64 normals so the FP32 build picks the reference's face (and so its contact order).
+        V3<double> m1 = face_normal64(W, h1, f1), m2 = face_normal64(W, h2, f2);
+        ref1 = vdot(m1, normal64) > vdot(m2, vinv(normal64));
+    }
     const ColView<R>& rh = ref1 ? h1 : h2;
     const ColView<R>& ih = ref1 ? h2 : h1;
     int rf = ref1 ? f1 : f2, inf = ref1 ? f2 : f1;
@@ -644,7 +660,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
 // clipping_get_contact_manifold (clipping.cpp:343-370)
 template <typename R, bool EXACT>
 __device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& c1, const ColView<R>& c2,
-                                 V3<R> normal, R pen, const PairFrame<R, EXACT>& fr) {
+                                 V3<R> normal, V3<double> normal64, R pen, const PairFrame<R, EXACT>& fr) {
     if (c1.type == COL_SPHERE) {
         V3<R> sp = support_point(c1, normal);
         push_contact(sm, fr, sp, vsub(sp, vscale(pen, normal)), normal, lane_id() == 0);
@@ -652,7 +668,7 @@ __device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const
         V3<R> sp = support_point(c2, vinv(normal));
         push_contact(sm, fr, vadd(sp, vscale(pen, normal)), sp, normal, lane_id() == 0);
     } else {
-        convex_convex_manifold<R, EXACT>(sm, W, c1, c2, normal, fr);
+        convex_convex_manifold<R, EXACT>(sm, W, c1, c2, normal, normal64, fr);
     }
 }
 
@@ -667,7 +683,7 @@ __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, cons
         if (dsq < (mind * mind)) {
             V3<R> normal = vnorm(vsub(c2.center, c1.center));
             R pen = (R)(float)(mind - sqrtf(dsq));
-            contact_manifold<R, EXACT>(sm, W, c1, c2, normal, pen, fr);
+            contact_manifold<R, EXACT>(sm, W, c1, c2, normal, v3cast<double>(normal), pen, fr);
         }
         return;
     }
@@ -685,7 +701,7 @@ __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, cons
         __syncwarp();
         return;
     }
-    contact_manifold<R, EXACT>(sm, W, c1, c2, v3cast<R>(n), (R)pen, fr);
+    contact_manifold<R, EXACT>(sm, W, c1, c2, v3cast<R>(n), n, (R)pen, fr);
 }
 
 }  // namespace rp

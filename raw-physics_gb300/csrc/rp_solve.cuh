@@ -88,16 +88,27 @@ __device__ __forceinline__ R pos_dlambda(const Body<R>& a, const Body<R>& b, con
     return (-c - til * lambda) / (w1 + w2 + til);
 }
 
+// Normalisation of an FP64 quaternion in the FP32 build: an FP32 reciprocal square root refined by
+// one FP64 Newton step (relative error ~1e-14), instead of an FP64 square root and four FP64
+// divisions, which GB300 executes at a small fraction of its FP32 rate.
+__device__ __forceinline__ Qt<double> qnormalize_fast(Qt<double> q) {
+    double n2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    double r = (double)rsqrtf((float)n2);
+    r = r * (1.5 - 0.5 * n2 * r * r);
+    return qt<double>(q.x * r, q.y * r, q.z * r, q.w * r);
+}
+
 // q <- normalize(q + s * dq): the linearised orientation update, accumulated in FP64
 template <typename R>
 __device__ __forceinline__ void q_add_normalize(Qt<double>& q, Qt<R> d, double s) {
     if (sizeof(R) == 8) {
         q.x = q.x + s * (double)d.x; q.y = q.y + s * (double)d.y; q.z = q.z + s * (double)d.z; q.w = q.w + s * (double)d.w;
+        q = qnormalize(q);
     } else {
         q.x = q.x + (double)((R)s * d.x); q.y = q.y + (double)((R)s * d.y);
         q.z = q.z + (double)((R)s * d.z); q.w = q.w + (double)((R)s * d.w);
+        q = qnormalize_fast(q);
     }
-    q = qnormalize(q);
 }
 
 template <typename R>
@@ -204,6 +215,9 @@ __device__ void collision_solve(const WorldView<R>& W, Body<R>& a, Body<R>& b, R
 }
 
 // limit_angle (pbd.cpp:175-217)
+// Joint limits are evaluated in FP64 in both builds (the axes come from the FP64 orientations):
+// asin's slope diverges at |s| -> 1, so at a +-90 degree limit an FP32 s (error 1e-7) would move
+// phi by sqrt(2e-7) ~ 4.5e-4 rad; in FP64 the same amplification stays below 1e-7.
 template <typename R>
 __device__ bool limit_angle(V3<R> n, V3<R> n1, V3<R> n2, R alpha, R beta, V3<R>& dq) {
     const R pi = (R)PI_REF;
@@ -227,7 +241,6 @@ __device__ bool limit_angle(V3<R> n, V3<R> n1, V3<R> n2, R alpha, R beta, V3<R>&
 template <typename R, bool EXACT>
 __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double* lam, R h) {
     Body<R> a = load_body(W, C.e1), b = load_body(W, C.e2);
-    const R EPS = Tiny<R>::v;
     V3<R> r1 = v3<R>((R)C.r1[0], (R)C.r1[1], (R)C.r1[2]), r2 = v3<R>((R)C.r2[0], (R)C.r2[1], (R)C.r2[2]);
     switch (C.type) {
     case CON_POSITIONAL: {  // pbd.cpp:81-97
@@ -258,8 +271,9 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
         pos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
         if (C.limited) {
-            V3<R> n1 = qaxis(wq<R>(a.q), C.l1), n2 = qaxis(wq<R>(b.q), C.l2), n = qaxis(wq<R>(a.q), C.a1);
-            if (limit_angle(n, n1, n2, (R)C.lo, (R)C.hi, dq)) {
+            V3<double> n1 = qaxis(a.q, C.l1), n2 = qaxis(b.q, C.l2), n = qaxis(a.q, C.a1), dq64;
+            if (limit_angle<double>(n, n1, n2, C.lo, C.hi, dq64)) {
+                dq = v3cast<R>(dq64);
                 Acpd<R> B = acpd(a, b);
                 R dl2 = ang_dlambda(B, h, (R)0, (R)lam[2], dq);
                 ang_apply(a, b, B, dl2, dq);
@@ -273,33 +287,37 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
         R dl = pos_dlambda(a, b, p, h, (R)0, (R)lam[0], dx);
         pos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
-        V3<R> n1 = qaxis(wq<R>(a.q), C.a1), n2 = qaxis(wq<R>(b.q), C.a2);
-        V3<R> n = vcross(n1, n2);
-        R nl = vlen(n);
-        if (nl > EPS) {
-            n = v3<R>(n.x / nl, n.y / nl, n.z / nl);
-            V3<R> dq;
-            if (limit_angle(n, n1, n2, (R)C.lo, (R)C.hi, dq)) {
+        // swing and twist limits: axes and angles in FP64 (see limit_angle)
+        const double EPS64 = 1e-50;
+        V3<double> n1 = qaxis(a.q, C.a1), n2 = qaxis(b.q, C.a2);
+        V3<double> n = vcross(n1, n2);
+        double nl = vlen(n);
+        if (nl > EPS64) {
+            n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
+            V3<double> dq64;
+            if (limit_angle<double>(n, n1, n2, C.lo, C.hi, dq64)) {
+                V3<R> dq = v3cast<R>(dq64);
                 Acpd<R> A = acpd(a, b);
                 R d2 = ang_dlambda(A, h, (R)0, (R)lam[1], dq);
                 ang_apply(a, b, A, d2, dq);
                 lam[1] += (double)d2;
             }
         }
-        V3<R> a1 = qaxis(wq<R>(a.q), C.a1), b1 = qaxis(wq<R>(a.q), C.l1);
-        V3<R> a2 = qaxis(wq<R>(b.q), C.a2), b2 = qaxis(wq<R>(b.q), C.l2);
+        V3<double> a1 = qaxis(a.q, C.a1), b1 = qaxis(a.q, C.l1);
+        V3<double> a2 = qaxis(b.q, C.a2), b2 = qaxis(b.q, C.l2);
         n = vadd(a1, a2);
         nl = vlen(n);
-        if (nl > EPS) {
-            n = v3<R>(n.x / nl, n.y / nl, n.z / nl);
+        if (nl > EPS64) {
+            n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
             n1 = vsub(b1, vscale(vdot(n, b1), n));
             n2 = vsub(b2, vscale(vdot(n, b2), n));
-            R l1 = vlen(n1), l2 = vlen(n2);
-            if (l1 > EPS && l2 > EPS) {
-                n1 = v3<R>(n1.x / l1, n1.y / l1, n1.z / l1);
-                n2 = v3<R>(n2.x / l2, n2.y / l2, n2.z / l2);
-                V3<R> dq;
-                if (limit_angle(n, n1, n2, (R)C.lo2, (R)C.hi2, dq)) {
+            double l1 = vlen(n1), l2 = vlen(n2);
+            if (l1 > EPS64 && l2 > EPS64) {
+                n1 = v3<double>(n1.x / l1, n1.y / l1, n1.z / l1);
+                n2 = v3<double>(n2.x / l2, n2.y / l2, n2.z / l2);
+                V3<double> dq64;
+                if (limit_angle<double>(n, n1, n2, C.lo2, C.hi2, dq64)) {
+                    V3<R> dq = v3cast<R>(dq64);
                     Acpd<R> A = acpd(a, b);
                     R d2 = ang_dlambda(A, h, (R)0, (R)lam[2], dq);
                     ang_apply(a, b, A, d2, dq);
@@ -343,12 +361,13 @@ __device__ void predict_body(const WorldView<R>& W, int b, double h) {
     if (EXACT) {
         q.x = q.x + h * 0.5 * (double)qd.x; q.y = q.y + h * 0.5 * (double)qd.y;
         q.z = q.z + h * 0.5 * (double)qd.z; q.w = q.w + h * 0.5 * (double)qd.w;
+        q = qnormalize(q);
     } else {
         R s = hR * (R)0.5;
         q.x = q.x + (double)(s * qd.x); q.y = q.y + (double)(s * qd.y);
         q.z = q.z + (double)(s * qd.z); q.w = q.w + (double)(s * qd.w);
+        q = qnormalize_fast(q);
     }
-    q = qnormalize(q);
     W.pos[b] = make_double4_32a(x.x, x.y, x.z, 0.0);
     W.rot[b] = make_double4_32a(q.x, q.y, q.z, q.w);
     W.vel[3 * b] = v.x; W.vel[3 * b + 1] = v.y; W.vel[3 * b + 2] = v.z;
@@ -363,11 +382,24 @@ __device__ void velocity_body(const WorldView<R>& W, int b, double h) {
     for (int i = 0; i < 3; ++i) { W.prev_vel[3 * b + i] = W.vel[3 * b + i]; W.prev_omega[3 * b + i] = W.omega[3 * b + i]; }
     double4_32a p = W.pos[b], pp = W.prev_pos[b], q4 = W.rot[b], pq4 = W.prev_rot[b];
     V3<double> dx = vsub(v3<double>(p.x, p.y, p.z), v3<double>(pp.x, pp.y, pp.z));
-    V3<double> v = vscale(1.0 / h, dx);
-    Qt<double> dq = qmul(qt<double>(q4.x, q4.y, q4.z, q4.w), qinverse(qt<double>(pq4.x, pq4.y, pq4.z, pq4.w)));
-    V3<double> w = (dq.w >= 0.0) ? vscale(2.0 / h, v3<double>(dq.x, dq.y, dq.z)) : vscale(-2.0 / h, v3<double>(dq.x, dq.y, dq.z));
-    W.vel[3 * b] = (R)v.x; W.vel[3 * b + 1] = (R)v.y; W.vel[3 * b + 2] = (R)v.z;
-    W.omega[3 * b] = (R)w.x; W.omega[3 * b + 1] = (R)w.y; W.omega[3 * b + 2] = (R)w.z;
+    if (EXACT) {
+        V3<double> v = vscale(1.0 / h, dx);
+        Qt<double> dq = qmul(qt<double>(q4.x, q4.y, q4.z, q4.w), qinverse(qt<double>(pq4.x, pq4.y, pq4.z, pq4.w)));
+        V3<double> w = (dq.w >= 0.0) ? vscale(2.0 / h, v3<double>(dq.x, dq.y, dq.z)) : vscale(-2.0 / h, v3<double>(dq.x, dq.y, dq.z));
+        W.vel[3 * b] = (R)v.x; W.vel[3 * b + 1] = (R)v.y; W.vel[3 * b + 2] = (R)v.z;
+        W.omega[3 * b] = (R)w.x; W.omega[3 * b + 1] = (R)w.y; W.omega[3 * b + 2] = (R)w.z;
+        return;
+    }
+    // FP32 build: only the pose differences are formed in FP64. With q = q_prev + d,
+    // q * q_prev^-1 = (0, 0, 0, |q_prev|^2) + d * q_prev^-1, so its vector part is d * q_prev^-1.
+    const R inv_h = (R)(1.0 / h);
+    V3<R> v = vscale(inv_h, v3cast<R>(dx));
+    Qt<R> d = qt<R>((R)(q4.x - pq4.x), (R)(q4.y - pq4.y), (R)(q4.z - pq4.z), (R)(q4.w - pq4.w));
+    Qt<R> qpi = qinverse(qt<R>((R)pq4.x, (R)pq4.y, (R)pq4.z, (R)pq4.w));
+    Qt<R> dq = qmul(d, qpi);
+    R sgn = ((R)1 + dq.w >= (R)0) ? (R)2 * inv_h : (R)-2 * inv_h;
+    W.vel[3 * b] = v.x; W.vel[3 * b + 1] = v.y; W.vel[3 * b + 2] = v.z;
+    W.omega[3 * b] = sgn * dq.x; W.omega[3 * b + 1] = sgn * dq.y; W.omega[3 * b + 2] = sgn * dq.z;
 }
 
 // Velocity solver for one contact (pbd.cpp:646-711); velocities of the two bodies are in registers.

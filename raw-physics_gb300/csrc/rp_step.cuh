@@ -187,7 +187,10 @@ __device__ void broad_phase(const WorldView<R>& W, const G& g, int s, int* smem)
     }
     g.sync();
     int total = group_exclusive_scan(g, W.row_count + b0, n, W.scan_tmp, smem);
-    if (g.rank() == 0) W.pair_count[s] = total;
+    if (g.rank() == 0) {
+        W.pair_count[s] = total;
+        atomicAdd(&W.counters[5], (unsigned long long)total);
+    }
     if (total > pcap) {
         if (g.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_PAIR_OVERFLOW);
     }
@@ -376,6 +379,7 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
     if (g.rank() == 0) {
         // exclusive prefix over the (few) levels; lfill doubles as the per-level fill counter
         int L = W.scene_levels[s], acc = 0;
+        atomicAdd(&W.counters[6], (unsigned long long)L);
         for (int l = 0; l <= L; ++l) { int c = lcount[l]; lcount[l] = acc; acc += c; }
     }
     g.sync();
@@ -435,8 +439,9 @@ __device__ void transform_hulls(const WorldView<R>& W, const G& g, int s, bool i
 // ---------------------------------------------------------------------------------------------
 // Narrowphase: one warp per broad-phase pair
 template <typename R, bool EXACT>
-__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged) {
+__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged, Qt<double> q64) {
     ColView<R> v;
+    v.q64 = q64;
     const Collider col = W.colliders[ci];
     v.type = col.type;
     v.radius = (R)col.radius;
@@ -490,9 +495,9 @@ __device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, i
     for (int ca = ca0; ca < ca1; ++ca) {
         // exact build: stored vertices are world coordinates, sphere centres the body positions;
         // FP32 build: stored vertices are rotated about the body origin, the frame origin is body a
-        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va);
+        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va, qt<double>(qa4.x, qa4.y, qa4.z, qa4.w));
         for (int cb = cb0; cb < cb1; ++cb) {
-            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb);
+            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb, qt<double>(qb4.x, qb4.y, qb4.z, qb4.w));
             collider_contacts<R, EXACT>(sm, W, va, vb, fr, W.counters);
             __syncwarp();
         }
@@ -525,6 +530,7 @@ __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem
                 nc = 0;
             }
             if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+            if (nc) atomicAdd(&W.counters[3], (unsigned long long)nc);
             W.pair_cstart[pbase + p] = start;
             W.pair_ccount[pbase + p] = nc;
         }
@@ -596,15 +602,70 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
 
 // ---------------------------------------------------------------------------------------------
 // One full step of scene s by group g
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Level-by-level sweep of the Gauss–Seidel schedule. With a grid group, a run of consecutive
+// levels that each hold at most SOLO_NODES nodes is swept by CTA 0 alone, separated by
+// __syncthreads, while the other CTAs wait at one grid barrier: the dependent chain of small levels
+// then costs a block barrier per level instead of a grid barrier. Larger levels use the whole grid.
+constexpr int SOLO_NODES = 2 * BLOCK;
+
+template <typename R, bool EXACT, bool VELOCITY, class G>
+__device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, int L, const int* lstart, int nbase, R hR) {
+    int l = 0;
+    while (l < L) {
+        int cnt = lstart[l + 1] - lstart[l];
+        if (g.nblocks() == 1 || cnt > SOLO_NODES) {
+            for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size()) {
+                if (VELOCITY) vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                else solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+            }
+            g.sync();
+            ++l;
+            continue;
+        }
+        int l2 = l;
+        while (l2 < L && lstart[l2 + 1] - lstart[l2] <= SOLO_NODES) ++l2;
+        if (g.block() == 0) {
+            for (int k = l; k < l2; ++k) {
+                for (int i = lstart[k] + (int)threadIdx.x; i < lstart[k + 1]; i += blockDim.x) {
+                    if (VELOCITY) vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                    else solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                }
+                __syncthreads();
+            }
+        }
+        g.sync();
+        l = l2;
+    }
+}
+
 template <typename R, bool EXACT, class G>
 __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepParams& P, NarrowSmem<R>& sm, int* smem) {
     if (!(P.dt > 0.0)) return;   // pbd.cpp:471
     const double h = P.dt / P.num_substeps;
     const R hR = (R)h;
     const int b0 = W.scene_body[s], b1 = W.scene_body[s + 1];
+    const bool timer = W.phase_ns && g.rank() == 0;
+    unsigned long long t_last = timer ? global_ns() : 0;
+    auto mark = [&](int ph) {
+        if (timer) {
+            unsigned long long t = global_ns();
+            atomicAdd(&W.phase_ns[ph], t - t_last);
+            t_last = t;
+        }
+    };
     broad_phase(W, g, s, smem);
+    mark(PH_BROAD);
     islands(W, g, s, P.dt);
+    mark(PH_ISLANDS);
     schedule(W, g, s, smem);
+    mark(PH_SCHEDULE);
     const int L = W.scene_levels[s];
     const int nbase = W.scene_node_cap[s];
     const int* lstart = W.level_count + s * (W.max_levels + 1);
@@ -615,29 +676,25 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
             for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
         if (g.rank() == 0) W.contact_count[s] = 0;
         g.sync();
+        mark(PH_PREDICT);
         if (P.enable_collisions) {
             transform_hulls<R, EXACT>(W, g, s, sub == 0);
             g.sync();
+            mark(PH_TRANSFORM);
             narrowphase<R, EXACT>(W, g, s, sm);
         } else {
             const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
             for (int p = g.rank(); p < np; p += g.size()) W.pair_ccount[W.scene_pair_cap[s] + p] = 0;
         }
         g.sync();
-        for (int it = 0; it < P.num_pos_iters; ++it) {
-            for (int l = 0; l < L; ++l) {
-                for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size())
-                    solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
-                g.sync();
-            }
-        }
+        mark(PH_NARROW);
+        for (int it = 0; it < P.num_pos_iters; ++it) sweep_levels<R, EXACT, false>(W, g, s, L, lstart, nbase, hR);
+        mark(PH_SOLVE);
         for (int b = b0 + g.rank(); b < b1; b += g.size()) velocity_body<R, EXACT>(W, b, h);
         g.sync();
-        for (int l = 0; l < L; ++l) {
-            for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size())
-                vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
-            g.sync();
-        }
+        mark(PH_VELOCITY);
+        sweep_levels<R, EXACT, true>(W, g, s, L, lstart, nbase, hR);
+        mark(PH_VSOLVE);
     }
 }
 

@@ -54,6 +54,9 @@ struct Shape {               // one convex hull's topology (collider_convex_hull
     int32_t max_face_neighbours;
 };
 
+// Phases of the step kernel timed by group rank 0 (rp_phase_times)
+enum { PH_BROAD = 0, PH_ISLANDS, PH_SCHEDULE, PH_PREDICT, PH_TRANSFORM, PH_NARROW, PH_SOLVE, PH_VELOCITY, PH_VSOLVE, PHASES };
+
 struct StepParams {          // the arguments of pbd_simulate_with_constraints
     double dt;
     int32_t num_substeps;
@@ -141,6 +144,7 @@ struct WorldView {
     uint32_t* status;        // [S] status bits per scene
     unsigned int* barrier;   // [2] grid barrier counter / generation
     unsigned long long* counters; // [8] diagnostics: gjk/epa iterations, contacts, ...
+    unsigned long long* phase_ns; // [PHASES] time spent per phase of the step, seen by group rank 0
 };
 
 }  // namespace rp

@@ -43,6 +43,8 @@ SIGNATURES = {
     "rp_hull_create_from_topology": (_i, [_W, _P(_d), _i, _P(_d), _i, _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i),
                                           _P(_i), _P(_i), _P(_i)]),
     "rp_hull_info": (_i, [_W, _i, _P(_i), _P(_i)]),
+    "rp_hull_topology": (_i, [_W, _i, _i, _P(_i), _P(_i), _i, _P(_i), _P(_i)]),
+    "rp_hull_geometry": (_i, [_W, _i, _P(_d), _P(_d)]),
     "rp_hull_face": (_i, [_W, _i, _i, _P(_d), _P(_i), _i, _P(_i)]),
     "rp_entity_create": (_i, [_W, _i, _P(_d), _P(_d), _d, _i, _P(ColliderDesc), _u, _d, _d, _d, _P(_i)]),
     "rp_entity_set_velocity": (_i, [_W, _i, _P(_d), _P(_d)]),
@@ -65,6 +67,8 @@ SIGNATURES = {
     "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_counters": (_i, [_W, _P(_u64)]),
     "rp_kernel_launches": (_u64, [_W]),
+    "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
+    "rp_phase_times": (_i, [_W, _P(_d)]),
     "rp_set_timing": (_i, [_W, _i]),
     "rp_last_step_ms": (_i, [_W, _P(_d)]),
 }
@@ -152,6 +156,23 @@ class World:
             self._check(self.lib.rp_hull_face(self.h, hull, f, n, el, 256, C.byref(ne)))
             faces.append((tuple(n), list(el[: ne.value])))
         return nv.value, faces
+
+    def hull_topology(self, hull: int):
+        """(vertices (nv,3), normals (nf,3), {table: (start, data)}) of a hull, as built on the host."""
+        nv, nf = _i(), _i()
+        self._check(self.lib.rp_hull_info(self.h, hull, C.byref(nv), C.byref(nf)))
+        verts, normals = np.zeros((nv.value, 3)), np.zeros((nf.value, 3))
+        self._check(self.lib.rp_hull_geometry(self.h, hull, _dp(verts), _dp(normals)))
+        tables = {}
+        for which in range(4):
+            rows, nd = _i(), _i()
+            self._check(self.lib.rp_hull_topology(self.h, hull, which, None, None, 0, C.byref(rows), C.byref(nd)))
+            start = np.zeros(rows.value + 1, dtype=np.int32)
+            data = np.zeros(max(nd.value, 1), dtype=np.int32)
+            self._check(self.lib.rp_hull_topology(self.h, hull, which, start.ctypes.data_as(_P(_i)),
+                                                  data.ctypes.data_as(_P(_i)), nd.value, C.byref(rows), C.byref(nd)))
+            tables[which] = (start, data[: nd.value])
+        return verts, normals, tables
 
     def entity(self, scene, pos, rot, mass, fixed, colliders, mus, mud, rest) -> int:
         arr = (ColliderDesc * len(colliders))(*colliders)
@@ -280,6 +301,18 @@ class World:
 
     def kernel_launches(self) -> int:
         return int(self.lib.rp_kernel_launches(self.h))
+
+    PHASES = ("broad", "islands", "schedule", "predict", "transform", "narrow", "solve", "velocity", "vsolve")
+
+    def phase_times(self) -> dict:
+        out = (C.c_double * 9)()
+        self._check(self.lib.rp_phase_times(self.h, out))
+        return dict(zip(self.PHASES, out[:]))
+
+    def transfer_bytes(self):
+        out = (C.c_uint64 * 2)()
+        self._check(self.lib.rp_transfer_bytes(self.h, out))
+        return list(out)
 
     def set_timing(self, on: bool):
         self._check(self.lib.rp_set_timing(self.h, int(on)))

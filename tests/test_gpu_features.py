@@ -1,0 +1,279 @@
+"""GPU behaviour beyond single-scene parity: batched scenes, edge cases the reference defines
+(dt <= 0, collisions off, empty and all-fixed worlds, forces), sleeping islands, scratch
+overflow and regrowth, device status, and the C++-mangled pbd_simulate drop-in."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batched_scenes_equal_separate_runs(ext_built, oracle_built):
+    """Several independent scenes in one world, one launch per frame: each equals its own oracle run."""
+    from rawphys import scenes as S
+    parts = [S.stack_scene(6, seed=1), S.chain_scene(6, "spherical", seed=2), S.random_pile_scene(8, seed=3),
+             S.sphere_scene(4, seed=1)]
+    w = ext_built.World(0, "fp64")
+    firsts = []
+    for i, sc in enumerate(parts):
+        sid = 0 if i == 0 else w.new_scene()
+        firsts.append(w.load(sc, scene_id=sid))
+    w.simulate(1.0 / 60.0, 20, 1, True, 25)
+    got = w.get_state()
+    for sc, f in zip(parts, firsts):
+        o = oracle_built("port").load(sc)
+        o.step(25)
+        assert np.array_equal(got[f:f + sc.num_bodies], o.get_state()), sc.name
+    w.close()
+
+
+def test_dt_nonpositive_is_noop_and_collisions_off(ext_built, oracle_built):
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(6, seed=2)
+    w = ext_built.World(0, "fp64")
+    w.load(sc)
+    w.step(3)
+    before = w.get_state()
+    w.simulate(0.0, 20, 1, True, 1)
+    w.simulate(-1.0, 20, 1, True, 1)
+    assert np.array_equal(before, w.get_state())
+    o = oracle_built("port").load(sc)
+    o.set_state(before)
+    o.step(4, collisions=False)
+    w.simulate(sc.dt, sc.substeps, 1, False, 4)
+    assert np.array_equal(w.get_state(), o.get_state())
+    w.close()
+
+
+def test_forces_match_oracle(ext_built, oracle_built):
+    """entity_add_force in world and local frames, cleared after the frame (entity.cpp:176-195)."""
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(5, seed=7)
+    o = oracle_built("port").load(sc)
+    w = ext_built.World(0, "fp64")
+    w.load(sc)
+    for frame in range(3):
+        for tgt in (o, w):
+            tgt.add_force(2, (0.1, 0.2, 0.0), (3.0, 0.0, -1.0 - frame), False)
+            tgt.add_force(3, (0.0, 0.3, 0.1), (0.0, 5.0, 2.0), True)
+        o.step(1)
+        w.step(1)
+        assert np.array_equal(w.get_state(), o.get_state()), frame
+    o.step(2)          # forces were cleared after each frame on both sides
+    w.step(2)
+    assert np.array_equal(w.get_state(), o.get_state())
+    w.close()
+
+
+def test_empty_and_all_fixed_worlds(ext_built):
+    rp = ext_built
+    w = rp.World(0, "fp32")
+    w.simulate(1.0 / 60.0, 20, 1, True, 3)          # no entities: no-op
+    assert w.num_entities() == 0
+    from rawphys import meshes as M
+    cube = M.cube()
+    h = w.hull(cube.positions.astype(np.float64) * 0.5, cube.indices)
+    for x in range(3):
+        w.entity(0, (x * 0.9, 0.0, 0.0), (0, 0, 0, 1), 0.0, True, [rp.ColliderDesc(rp.COLLIDER_HULL, h, 0.0)], 0.5, 0.3, 0.0)
+    st = w.get_state()
+    w.set_gravity(10.0)
+    w.simulate(1.0 / 60.0, 20, 1, True, 5)
+    after = w.get_state()
+    assert np.array_equal(after[:, 0:7], st[:, 0:7])
+    assert w.broad_pairs().shape == (3, 2)          # fixed-fixed pairs are listed, then skipped
+    w.close()
+
+
+def test_sleeping_islands_match_oracle(ext_built, oracle_built):
+    """A settled stack goes to sleep after 1 s of slow motion, island by island (pbd.cpp:477-506)."""
+    from rawphys import scenes as S
+    sc = S.stack_scene(4, seed=5)
+    o = oracle_built("port").load(sc)
+    w = ext_built.World(0, "fp64")
+    w.load(sc)
+    o.step(150)
+    w.step(150)
+    a, b = o.get_state(), w.get_state()
+    assert np.array_equal(a, b)
+    assert a[1:, 26].min() == 0.0, "the stack should be asleep by now"
+    w.close()
+
+
+def test_scratch_overflow_regrows_and_redoes(ext_built, oracle_built, monkeypatch):
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(10, seed=8)
+    monkeypatch.setenv("RP_SCRATCH_SCALE", "0.0001")
+    w = ext_built.World(0, "fp64")
+    w.load(sc)
+    w.step(60)
+    o = oracle_built("port").load(sc)
+    o.step(60)
+    assert np.array_equal(w.get_state(), o.get_state())
+    w.close()
+
+
+def test_deep_overlap_and_status(ext_built):
+    """Bodies spawned inside each other (EPA from deep penetration) run without fault; the device
+    reports informational status only."""
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(12, seed=9, spread=0.2)
+    sc.pos[1:, 1] = 0.6 + 0.3 * np.arange(sc.num_bodies - 1)
+    w = ext_built.World(0, "fp32")
+    w.load(sc)
+    w.step(30)
+    st = w.get_state()
+    assert np.all(np.isfinite(st))
+    assert (w.status() & ~(1 << 8)) == 0
+    w.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# The pbd_simulate drop-in, driven through the reference's own data layout
+
+class Vec3(C.Structure):
+    _pack_ = 1
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class Quat(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("w", C.c_double)]
+
+
+class Mat3(C.Structure):
+    _pack_ = 1
+    _fields_ = [("data", C.c_double * 9)]
+
+
+class Force(C.Structure):
+    _fields_ = [("position", Vec3), ("force", Vec3), ("local_coords", C.c_int32)]
+
+
+class HullFace(C.Structure):
+    _fields_ = [("elements", C.c_void_p), ("normal", Vec3)]
+
+
+class Hull(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("transformed_vertices", C.c_void_p), ("faces", C.c_void_p),
+                ("transformed_faces", C.c_void_p), ("vertex_to_faces", C.c_void_p), ("vertex_to_neighbors", C.c_void_p),
+                ("face_to_neighbors", C.c_void_p)]
+
+
+class Collider(C.Structure):
+    _fields_ = [("type", C.c_int32), ("convex_hull", Hull)]
+
+
+class Entity(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("mesh", C.c_uint32 * 4), ("world_position", Vec3), ("world_rotation", Quat),
+                ("world_scale", Vec3), ("color", C.c_double * 4), ("colliders", C.c_void_p),
+                ("bounding_sphere_radius", C.c_double), ("forces", C.c_void_p), ("inverse_mass", C.c_double),
+                ("inertia_tensor", Mat3), ("inverse_inertia_tensor", Mat3), ("angular_velocity", Vec3),
+                ("linear_velocity", Vec3), ("fixed", C.c_int32), ("active", C.c_int32), ("deactivation_time", C.c_double),
+                ("static_friction_coefficient", C.c_double), ("dynamic_friction_coefficient", C.c_double),
+                ("restitution_coefficient", C.c_double), ("previous_world_position", Vec3), ("previous_world_rotation", Quat),
+                ("previous_linear_velocity", Vec3), ("previous_angular_velocity", Vec3)]
+
+
+class LightArrays:
+    """Builds include/light_array.h arrays: {size_t capacity, size_t length} then the elements."""
+
+    def __init__(self):
+        self.keep = []
+
+    def make(self, ctype, values):
+        n = len(values)
+        buf = (C.c_ubyte * (16 + C.sizeof(ctype) * max(n, 1)))()
+        self.keep.append(buf)
+        hdr = (C.c_size_t * 2).from_buffer(buf)
+        hdr[0] = max(n, 1)
+        hdr[1] = n
+        arr = (ctype * max(n, 1)).from_buffer(buf, 16)
+        for i, v in enumerate(values):
+            arr[i] = v
+        return C.addressof(buf) + 16
+
+    def malloc_ptrs(self, ptrs):
+        a = (C.c_void_p * max(len(ptrs), 1))(*ptrs)
+        self.keep.append(a)
+        return C.addressof(a)
+
+
+def build_entities(o, scene, la):
+    ents = []
+    st = o.get_state()
+    for e in range(scene.num_bodies):
+        verts, normals, tables = o.hull_topology(e)
+        vtx = [Vec3(*v) for v in verts]
+        faces = []
+        fs, fd = tables[0]
+        for f in range(len(normals)):
+            faces.append(HullFace(la.make(C.c_uint32, list(fd[fs[f]:fs[f + 1]])), Vec3(*normals[f])))
+        rows = lambda t: la.malloc_ptrs([la.make(C.c_uint32, list(t[1][t[0][r]:t[0][r + 1]])) for r in range(len(t[0]) - 1)])
+        hull = Hull(la.make(Vec3, vtx), la.make(Vec3, vtx), la.make(HullFace, faces), la.make(HullFace, faces),
+                    rows(tables[1]), rows(tables[2]), rows(tables[3]))
+        col = la.make(Collider, [Collider(1, hull)])
+        I, Ii = o.inertia(e)
+        ent = Entity()
+        ent.id = 1000 + e
+        ent.world_position = Vec3(*st[e, 0:3])
+        ent.world_rotation = Quat(*st[e, 3:7])
+        ent.colliders = col
+        ent.bounding_sphere_radius = o.radius(e)
+        invm = o.inverse_mass(e)
+        ent.inverse_mass = invm
+        ent.inertia_tensor = Mat3((C.c_double * 9)(*I.reshape(9)))
+        ent.inverse_inertia_tensor = Mat3((C.c_double * 9)(*Ii.reshape(9)))
+        ent.linear_velocity = Vec3(*st[e, 7:10])
+        ent.angular_velocity = Vec3(*st[e, 10:13])
+        ent.fixed = int(scene.fixed[e])
+        ent.active = 1
+        ent.static_friction_coefficient = scene.mus[e]
+        ent.dynamic_friction_coefficient = scene.mud[e]
+        ent.restitution_coefficient = scene.rest[e]
+        g = 10.0
+        ent.forces = la.make(Force, [Force(Vec3(0, 0, 0), Vec3(0.0, -g * 1.0 / invm if invm else -np.inf, 0.0), 0)])
+        ents.append(ent)
+    arr = la.make(C.POINTER(Entity), [C.pointer(x) for x in ents])
+    return ents, arr
+
+
+def test_pbd_simulate_dropin(ext_built, oracle_built, monkeypatch):
+    """A caller holding the reference's Entity / Collider / Physics_Force structs calls the mangled
+    pbd_simulate; with the FP64 kernels the result equals the oracle bit for bit."""
+    from rawphys import scenes as S
+    monkeypatch.setenv("RP_SHIM_PRECISION", "fp64")
+    lib = C.CDLL(ext_built.LIB_PATH)
+    lib.rp_compat_reset()
+    f = getattr(lib, "_Z12pbd_simulatedPP6Entityjji")
+    f.argtypes = [C.c_double, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]
+    f.restype = None
+    sc = S.stack_scene(5, seed=2)
+    o = oracle_built("port").load(sc)
+    la = LightArrays()
+    ents, arr = build_entities(o, sc, la)
+    for frame in range(3):
+        f(sc.dt, arr, 20, 1, 1)
+        o.step(1)
+        ref = o.get_state()
+        for e, ent in enumerate(ents):
+            got = [ent.world_position.x, ent.world_position.y, ent.world_position.z,
+                   ent.world_rotation.x, ent.world_rotation.y, ent.world_rotation.z, ent.world_rotation.w,
+                   ent.linear_velocity.x, ent.linear_velocity.y, ent.linear_velocity.z]
+            assert np.array_equal(np.array(got), ref[e, 0:10]), (frame, e)
+    # transformed collider vertices follow the final pose
+    ent = ents[1]
+    hull = Collider.from_address(ent.colliders).convex_hull
+    tv = (Vec3 * 8).from_address(hull.transformed_vertices)
+    v = (Vec3 * 8).from_address(hull.vertices)
+    q = np.array([ent.world_rotation.x, ent.world_rotation.y, ent.world_rotation.z, ent.world_rotation.w])
+    x, y, z, w_ = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w_ * z), 2 * (x * z + w_ * y)],
+                  [2 * (x * y + w_ * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w_ * x)],
+                  [2 * (x * z - w_ * y), 2 * (y * z + w_ * x), 1 - 2 * (x * x + y * y)]])
+    p = np.array([ent.world_position.x, ent.world_position.y, ent.world_position.z])
+    for i in range(8):
+        assert np.allclose([tv[i].x, tv[i].y, tv[i].z], R @ np.array([v[i].x, v[i].y, v[i].z]) + p, atol=1e-12)
+    lib.rp_compat_reset()

@@ -1,0 +1,139 @@
+"""CPU-side checks of the product: the C ABI library loads and exports every declared symbol; the
+host set-up (hull topology, bounding radius, point-mass inertia) reproduces the reference exactly;
+host-only worlds refuse GPU work loudly; argument validation; scene generators."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+from make_golden import SCENES
+
+
+def declared_functions():
+    names = []
+    for h in ("rp.h", "rp_compat.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(rp_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(ext_built):
+    lib = C.CDLL(ext_built.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # the drop-in: C++-mangled exactly as the reference's pbd.cpp compiles them (pbd.h:93-94)
+    for sym in ("_Z12pbd_simulatedPP6Entityjji", "_Z29pbd_simulate_with_constraintsdPP6EntityP10Constraintjji"):
+        assert hasattr(lib, sym), sym
+    # and the binding covers the whole C ABI
+    assert set(n for n in names if n != "rp_compat_reset") <= set(ext_built.SIGNATURES)
+
+
+@pytest.mark.parametrize("name", ["stack10", "spheres6", "large1024", "chain8_hinge", "domino16"])
+def test_host_mass_properties_match_reference(ext_built, name):
+    g = golden(name)
+    scene = SCENES[name][0]()
+    w = ext_built.World(-1, "fp64")
+    w.load(scene)
+    for e in range(scene.num_bodies):
+        invm, I, Ii, r = w.mass_properties(e)
+        assert invm == g["invm"][e]
+        assert r == g["radius"][e]
+        if "inertia" in g:
+            assert np.array_equal(I.reshape(9), g["inertia"][e])
+            assert np.array_equal(Ii.reshape(9), g["inverse_inertia"][e])
+    w.close()
+
+
+def test_host_hull_topology_matches_oracle(ext_built, oracle_built):
+    """Vertex order, faces, face normals, vertex->faces, vertex->neighbours, face->neighbours."""
+    from rawphys import scenes as S
+    scene = S.large_scene(40, seed=5)
+    w = ext_built.World(-1, "fp32")
+    w.load(scene)
+    o = oracle_built("port").load(scene)
+    for e in range(scene.num_bodies):
+        c = scene.colliders[e][0]
+        hid = w._hulls[(id(scene.meshes[c.mesh]), tuple(c.scale))]
+        gv, gn, gt = w.hull_topology(hid)
+        ov, on, ot = o.hull_topology(e)
+        assert np.array_equal(gv, ov) and np.array_equal(gn, on)
+        for k in range(4):
+            assert np.array_equal(gt[k][0], ot[k][0]) and np.array_equal(gt[k][1], ot[k][1]), (e, k)
+    w.close()
+
+
+def test_cylinder_and_sphere_hull_shapes(ext_built):
+    from rawphys import meshes as M
+    w = ext_built.World(-1, "fp32")
+    for mesh, nv, nf, maxval in ((M.cube(), 8, 6, 4), (M.icosahedron(), 12, 20, 3), (M.cylinder(32), 64, 34, 32),
+                                 (M.icosphere(), 42, 80, 3)):
+        h = w.hull(mesh.positions.astype(np.float64), mesh.indices)
+        got_nv, faces = w.hull_faces(h)
+        assert got_nv == nv and len(faces) == nf, mesh.name
+        assert max(len(f[1]) for f in faces) == maxval
+        # outward normals: every vertex lies behind every face plane
+        v = w.hull_topology(h)[0]
+        for n, el in faces:
+            d = v @ np.asarray(n) - v[el[0]] @ np.asarray(n)
+            assert np.all(d <= 1e-9), mesh.name
+    w.close()
+
+
+def test_host_only_world_refuses_gpu_work(ext_built):
+    from rawphys import scenes as S
+    w = ext_built.World(-1, "fp32")
+    w.load(S.stack_scene(3))
+    with pytest.raises(ext_built.RPError, match="RP_ERR_NO_DEVICE"):
+        w.step(1)
+    with pytest.raises(ext_built.RPError, match="RP_ERR_NO_DEVICE"):
+        w.broad_pairs()
+    st = w.get_state()             # snapshots still work on the host copy
+    w.set_state(st)
+    assert np.array_equal(w.get_state(), st)
+    w.close()
+
+
+def test_argument_validation(ext_built):
+    rp = ext_built
+    w = rp.World(-1, "fp32")
+    cube = w.hull(np.array([[x, y, z] for x in (-1., 1.) for y in (-1., 1.) for z in (-1., 1.)]),
+                  np.array([0, 1, 3], dtype=np.uint32))
+    desc = [rp.ColliderDesc(rp.COLLIDER_HULL, cube, 0.0)]
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.entity(0, (0, 0, 0), (0, 0, 0, 1), -1.0, False, desc, 0.5, 0.3, 0.0)     # mass <= 0
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.entity(0, (0, 0, 0), (0, 0, 0, 1), 1.0, False, desc, 1.5, 0.3, 0.0)      # friction > 1
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.entity(0, (np.nan, 0, 0), (0, 0, 0, 1), 1.0, False, desc, 0.5, 0.3, 0.0)
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.entity(3, (0, 0, 0), (0, 0, 0, 1), 1.0, False, desc, 0.5, 0.3, 0.0)      # no such scene
+    with pytest.raises(rp.RPError, match="RP_ERR_DEGENERATE"):
+        w.hull(np.zeros((3, 3)), np.array([0, 1, 2], dtype=np.uint32))            # open, degenerate "hull"
+    bad = [rp.ColliderDesc(rp.COLLIDER_SPHERE, -1, 0.5), rp.ColliderDesc(rp.COLLIDER_HULL, cube, 0.0)]
+    with pytest.raises(rp.RPError, match="RP_ERR_DEGENERATE"):                    # reference asserts
+        w.entity(0, (0, 0, 0), (0, 0, 0, 1), 1.0, False, bad, 0.5, 0.3, 0.0)
+    e = w.entity(0, (0, 0, 0), (0, 0, 0, 1), 1.0, True, [rp.ColliderDesc(rp.COLLIDER_SPHERE, -1, 0.5)], 0.5, 0.3, 0.0)
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.set_state(np.full((1, rp.STATE_DOUBLES), np.inf))
+    assert e == 0 and w.num_entities() == 1
+    w.close()
+
+
+def test_scene_generators_are_deterministic():
+    from rawphys import scenes as S
+    a, b = S.large_scene(256, seed=3), S.large_scene(256, seed=3)
+    assert np.array_equal(a.pos, b.pos) and np.array_equal(a.rot, b.rot) and np.array_equal(a.mass, b.mass)
+    # no two bounding spheres overlap at t = 0, all bodies inside the walls
+    dyn = ~a.fixed
+    p = a.pos[dyn]
+    assert np.all(np.abs(p[:, 0]) < 20) and np.all(np.abs(p[:, 2]) < 20) and np.all((p[:, 1] > 0) & (p[:, 1] < 60))
+    q = np.linalg.norm(a.rot, axis=1)
+    assert np.allclose(q, 1.0)
