@@ -177,6 +177,11 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out_pairs, uint32
 /* colliders_update + colliders_get_contacts for one entity pair on the current state, computed by
  * the device narrowphase. out: RP_CONTACT_DOUBLES per contact. */
 rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
+/* The collision constraints of the last substep of the last rp_simulate call, in the reference's
+ * constraint order (pairs in broad-phase order, contacts in manifold order): entity pairs (2 per
+ * contact) and 11 doubles per contact: r1_lc[3], r2_lc[3], normal[3], lambda_n, lambda_t
+ * (clipping_contact_to_collision_constraint, pbd.cpp:408-424). *count receives the total. */
+rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, double* out, uint32_t cap, uint32_t* count);
 /* Counters accumulated since creation: [0] GJK iterations, [1] EPA iterations, [2] EPA calls,
  * [3] steps, [4] substeps, [5] contacts generated, [6] broad-phase pairs (summed over steps),
  * [7] solver levels (summed over steps). */

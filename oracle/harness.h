@@ -70,6 +70,9 @@ int orc_constraint_spherical(int e1, int e2, const double r1[3], const double r2
  * gravity is the magnitude g of a force (0, -g/inverse_mass, 0) added to every entity. */
 void     orc_step(double dt, uint32_t num_substeps, uint32_t num_pos_iters, int enable_collisions, double gravity);
 
+/* Port only: the collision constraints of the last substep of the last orc_step, in constraint
+ * order: entity pairs (2 each) and r1_lc[3] r2_lc[3] normal[3] lambda_n lambda_t (11 each). */
+uint32_t orc_last_contacts(int32_t* pairs, double* out, uint32_t cap);
 uint32_t orc_num_entities(void);
 void     orc_get_state(double* out);
 void     orc_set_state(const double* in);

@@ -73,8 +73,11 @@ class Oracle:
                 "orc_gjk_epa": (i, [i, i, P(d)]),
                 "orc_hull_topology": (i, [i, i, i, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
                 "orc_hull_geometry": (i, [i, i, P(d), P(d), C.c_int32, C.c_int32, P(C.c_int32)]),
+                "orc_last_contacts": (u, [P(C.c_int32), P(d), u]),
             }
             for name, (res, args) in sig.items():
+                if not hasattr(lib, name):   # orc_last_contacts exists in the port only
+                    continue
                 f = getattr(lib, name)
                 f.restype = res
                 f.argtypes = args
@@ -191,6 +194,15 @@ class Oracle:
                                        data.ctypes.data_as(C.POINTER(C.c_int32)), nd.value, C.byref(nd))
             tables[which] = (start, data[: nd.value])
         return verts, normals, tables
+
+    def last_contacts(self):
+        """(pairs (k,2), constraints (k,11)) of the last substep of the last step (port only)."""
+        cap = 1 << 16
+        pairs = np.zeros(2 * cap, dtype=np.int32)
+        out = np.zeros(11 * cap)
+        n = self.lib.orc_last_contacts(pairs.ctypes.data_as(C.POINTER(C.c_int32)), out.ctypes.data_as(C.POINTER(C.c_double)), cap)
+        n = min(n, cap)
+        return pairs[: 2 * n].reshape(-1, 2), out[: 11 * n].reshape(-1, 11)
 
     def gjk_epa(self, e1: int, e2: int):
         out = np.zeros(4)

@@ -286,6 +286,8 @@ static collider_t* g_pending = NULL;
 static int g_np = 0, g_pcap = 0;
 static constraint_t* g_cons = NULL;
 static int g_nc = 0, g_ccap = 0;
+static constraint_t* g_last = NULL;   /* collision constraints of the last substep */
+static int g_nlast = 0, g_lastcap = 0;
 
 void orc_reset(void) {
     for (int i = 0; i < g_nb; ++i) {
@@ -1438,10 +1440,31 @@ static void simulate(double dt, unsigned substeps, unsigned iters, int collision
                 e2->w = v_add(e2->w, v_inv(m3_mulv(p.I2, v_cross(p.r2, P))));
             }
         }
+        if (s + 1 == substeps) {
+            /* keep the last substep's collision constraints for orc_last_contacts */
+            g_nlast = 0;
+            for (int k = 0; k < nc; ++k)
+                if (cons[k].type == C_COL) {
+                    if (g_nlast == g_lastcap) { g_lastcap = g_lastcap ? 2 * g_lastcap : 64; g_last = (constraint_t*)realloc(g_last, sizeof(constraint_t) * (size_t)g_lastcap); }
+                    g_last[g_nlast++] = cons[k];
+                }
+        }
     }
     free(contacts.a);
     free(cons);
     free(pairs);
+}
+
+uint32_t orc_last_contacts(int32_t* pairs, double* out, uint32_t cap) {
+    for (int k = 0; k < g_nlast && (uint32_t)k < cap; ++k) {
+        const constraint_t* c = &g_last[k];
+        pairs[2 * k] = c->e1;
+        pairs[2 * k + 1] = c->e2;
+        double v[11] = {c->r1.x, c->r1.y, c->r1.z, c->r2.x, c->r2.y, c->r2.z, c->normal.x, c->normal.y, c->normal.z,
+                        c->lambda_n, c->lambda_t};
+        for (int j = 0; j < 11; ++j) out[11 * k + j] = v[j];
+    }
+    return (uint32_t)g_nlast;
 }
 
 void orc_step(double dt, uint32_t substeps, uint32_t iters, int collisions, double gravity) {

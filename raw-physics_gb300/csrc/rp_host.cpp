@@ -1185,6 +1185,45 @@ rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t
     return RP_OK;
 }
 
+rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, double* out, uint32_t cap, uint32_t* count) {
+    if (check_world(w) || scene < 0 || scene >= w->num_scenes) return fail(RP_ERR_INVALID, "bad argument");
+    if (w->device < 0 || !w->d_pair_count.p || w->static_dirty) return fail(RP_ERR_STATE, "no step has run");
+    int32_t np = 0;
+    RP_CUDA(cudaMemcpyAsync(&np, w->d_pair_count.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    const int32_t pbase = w->scene_pair_cap[(size_t)scene], cbase = w->scene_contact_cap[(size_t)scene];
+    np = std::min(np, w->scene_pair_cap[(size_t)scene + 1] - pbase);
+    std::vector<int2> pr((size_t)np);
+    std::vector<int32_t> cs((size_t)np), cc((size_t)np);
+    const int32_t ncap = w->scene_contact_cap[(size_t)scene + 1] - cbase;
+    const size_t R = w->rsize();
+    std::vector<unsigned char> con((size_t)ncap * 12 * R);
+    if (np) {
+        RP_CUDA(cudaMemcpyAsync(pr.data(), w->d_pairs.as<int2>() + pbase, (size_t)np * 8, cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaMemcpyAsync(cs.data(), w->d_pair_cstart.as<int32_t>() + pbase, (size_t)np * 4, cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaMemcpyAsync(cc.data(), w->d_pair_ccount.as<int32_t>() + pbase, (size_t)np * 4, cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaMemcpyAsync(con.data(), (char*)w->d_contacts.p + (size_t)cbase * 12 * R, con.size(), cudaMemcpyDeviceToHost, w->stream));
+    }
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    uint32_t k = 0;
+    const int map[11] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 3, 7};
+    for (int32_t p = 0; p < np; ++p) {
+        for (int32_t c = 0; c < cc[(size_t)p]; ++c, ++k) {
+            if (k >= cap) continue;
+            size_t base = (size_t)(cs[(size_t)p] + c) * 12;
+            pairs_out[2 * k] = w->slot_to_entity[(size_t)pr[(size_t)p].x];
+            pairs_out[2 * k + 1] = w->slot_to_entity[(size_t)pr[(size_t)p].y];
+            for (int j = 0; j < 11; ++j) {
+                size_t at = base + (size_t)map[j];
+                if (R == 8) std::memcpy(&out[11 * k + j], &con[at * 8], 8);
+                else { float f; std::memcpy(&f, &con[at * 4], 4); out[11 * k + j] = f; }
+            }
+        }
+    }
+    if (count) *count = k;
+    return RP_OK;
+}
+
 rp_status rp_counters(rp_world* w, uint64_t out[8]) {
     if (check_world(w) || !out) return RP_ERR_INVALID;
     for (int k = 0; k < 8; ++k) out[k] = 0;

@@ -21,7 +21,7 @@ constexpr int WARP = 32;
 constexpr int STAGE_V = 64;      // hull vertices staged per body in shared memory
 constexpr int EPA_MAXV = 104;    // 4 simplex points + at most 100 EPA iterations
 constexpr int EPA_MAXF = 192;    // faces of the EPA polytope
-constexpr int EPA_MAXE = 96;     // horizon edges of one EPA iteration
+constexpr int EPA_MAXE = 64;     // horizon edges of one EPA iteration (two register slots per lane)
 constexpr int CLIP_MAX = 96;     // vertices of a clipped polygon
 constexpr int CMAX = 64;         // contacts of one body pair
 
@@ -41,7 +41,6 @@ struct NarrowSmem {
             V3<double> fn[EPA_MAXF];
             double fd[EPA_MAXF];
             uchar4 f[EPA_MAXF];      // x, y, z polytope indices, w = visibility
-            uchar2 e[EPA_MAXE];
         } epa;
         struct {
             V3<R> buf[2][CLIP_MAX];
@@ -297,29 +296,55 @@ __device__ void epa_face(NarrowSmem<R>& sm, int fi, int npoly) {
     sm.u.epa.fd[fi] = d;
 }
 
+// The horizon edge list of one EPA iteration, held in registers across the warp: slot s lives in
+// lane s % 32, register s / 32 (up to 64 edges), with its endpoint positions for the reference's
+// position-equality test (epa.cpp:92-106).
 template <typename R>
-__device__ bool epa_edge_equal(const NarrowSmem<R>& sm, uchar2 cur, uchar2 e) {
-    if ((e.x == cur.x && e.y == cur.y) || (e.x == cur.y && e.y == cur.x)) return true;
-    V3<R> c1 = sm.u.epa.poly[cur.x], c2 = sm.u.epa.poly[cur.y], e1 = sm.u.epa.poly[e.x], e2 = sm.u.epa.poly[e.y];
-    if (veq(c1, e1) && veq(c2, e2)) return true;
-    if (veq(c1, e2) && veq(c2, e1)) return true;
-    return false;
-}
+struct EdgeRegs {
+    int ex[2], ey[2];
+    V3<R> p1[2], p2[2];
+};
 
+// add_edge (epa.cpp:79-110): remove the first edge equal to (x, y) in either orientation — by index
+// or by endpoint positions — moving the last edge into its slot; otherwise append. Every lane takes
+// part; ne is warp-uniform.
 template <typename R>
-__device__ void epa_add_edge(NarrowSmem<R>& sm, uchar2 e) {
-    int ne = sm.ne;
-    for (int i = 0; i < ne; ++i) {
-        if (epa_edge_equal(sm, sm.u.epa.e[i], e)) {
-            ne--;
-            sm.u.epa.e[i] = sm.u.epa.e[ne];
-            sm.ne = ne;
-            return;
-        }
+__device__ __forceinline__ void epa_add_edge_warp(EdgeRegs<R>& E, int& ne, int x, int y, V3<R> px, V3<R> py, bool& overflow) {
+    const unsigned lane = lane_id();
+    int found = -1;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int slot = k * 32 + (int)lane;
+        bool m = slot < ne && ((E.ex[k] == x && E.ey[k] == y) || (E.ex[k] == y && E.ey[k] == x) ||
+                               (veq(E.p1[k], px) && veq(E.p2[k], py)) || (veq(E.p1[k], py) && veq(E.p2[k], px)));
+        unsigned b = __ballot_sync(0xffffffffu, m);
+        if (found < 0 && b) found = k * 32 + __ffs(b) - 1;
     }
-    if (ne >= EPA_MAXE) { atomicOr(&sm.status, (int)ST_EPA_OVERFLOW); return; }
-    sm.u.epa.e[ne] = e;
-    sm.ne = ne + 1;
+    if (found >= 0) {
+        const int last = ne - 1, lk = last >> 5, ll = last & 31;
+        int lx = __shfl_sync(0xffffffffu, lk ? E.ex[1] : E.ex[0], ll);
+        int ly = __shfl_sync(0xffffffffu, lk ? E.ey[1] : E.ey[0], ll);
+        V3<R> q1, q2;
+        q1.x = __shfl_sync(0xffffffffu, lk ? E.p1[1].x : E.p1[0].x, ll);
+        q1.y = __shfl_sync(0xffffffffu, lk ? E.p1[1].y : E.p1[0].y, ll);
+        q1.z = __shfl_sync(0xffffffffu, lk ? E.p1[1].z : E.p1[0].z, ll);
+        q2.x = __shfl_sync(0xffffffffu, lk ? E.p2[1].x : E.p2[0].x, ll);
+        q2.y = __shfl_sync(0xffffffffu, lk ? E.p2[1].y : E.p2[0].y, ll);
+        q2.z = __shfl_sync(0xffffffffu, lk ? E.p2[1].z : E.p2[0].z, ll);
+        if ((int)lane == (found & 31)) {
+            const int fk = found >> 5;
+            if (fk) { E.ex[1] = lx; E.ey[1] = ly; E.p1[1] = q1; E.p2[1] = q2; }
+            else { E.ex[0] = lx; E.ey[0] = ly; E.p1[0] = q1; E.p2[0] = q2; }
+        }
+        ne = last;
+    } else {
+        if (ne >= EPA_MAXE) { overflow = true; return; }
+        if ((int)lane == (ne & 31)) {
+            if (ne >> 5) { E.ex[1] = x; E.ey[1] = y; E.p1[1] = px; E.p2[1] = py; }
+            else { E.ex[0] = x; E.ey[0] = y; E.p1[0] = px; E.p2[0] = py; }
+        }
+        ne = ne + 1;
+    }
 }
 
 // Returns true when converged; normal and penetration are then set (FP64).
@@ -376,35 +401,48 @@ __device__ bool epa(NarrowSmem<R>& sm, const ColView<R>& c1, const ColView<R>& c
             sm.u.epa.f[i] = f;
         }
         __syncwarp();
-        // the reference's removal loop: unordered remove, re-test the moved face (epa.cpp:167-197)
-        if (lane == 0) {
+        // the reference's removal loop: unordered remove, re-test the moved face (epa.cpp:167-197),
+        // run by the whole warp with the horizon edges in registers
+        EdgeRegs<R> E;
+        int ne = 0;
+        bool overflow = false;
+        {
             int i = 0;
             while (i < nf) {
                 uchar4 f = sm.u.epa.f[i];
                 if (f.w) {
-                    epa_add_edge(sm, make_uchar2(f.x, f.y));
-                    epa_add_edge(sm, make_uchar2(f.y, f.z));
-                    epa_add_edge(sm, make_uchar2(f.z, f.x));
+                    V3<R> px = sm.u.epa.poly[f.x], py = sm.u.epa.poly[f.y], pz = sm.u.epa.poly[f.z];
+                    epa_add_edge_warp(E, ne, f.x, f.y, px, py, overflow);
+                    epa_add_edge_warp(E, ne, f.y, f.z, py, pz, overflow);
+                    epa_add_edge_warp(E, ne, f.z, f.x, pz, px, overflow);
                     nf--;
-                    sm.u.epa.f[i] = sm.u.epa.f[nf];
-                    sm.u.epa.fd[i] = sm.u.epa.fd[nf];
-                    sm.u.epa.fn[i] = sm.u.epa.fn[nf];
+                    __syncwarp();
+                    if (lane == 0) {
+                        sm.u.epa.f[i] = sm.u.epa.f[nf];
+                        sm.u.epa.fd[i] = sm.u.epa.fd[nf];
+                        sm.u.epa.fn[i] = sm.u.epa.fn[nf];
+                    }
+                    __syncwarp();
                 } else {
                     ++i;
                 }
             }
-            if (nf + sm.ne > EPA_MAXF) atomicOr(&sm.status, (int)ST_EPA_OVERFLOW);
-            sm.nf = nf;
+        }
+        if (overflow || nf + ne > EPA_MAXF) {
+            if (lane == 0) atomicOr(&sm.status, (int)ST_EPA_OVERFLOW);
+            __syncwarp();
+            return false;
+        }
+        // new faces (edge, new point) in edge-slot order, normals lane-parallel
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            int slot = k * 32 + (int)lane;
+            if (slot < ne) {
+                sm.u.epa.f[nf + slot] = make_uchar4((unsigned char)E.ex[k], (unsigned char)E.ey[k], (unsigned char)np, 0);
+            }
         }
         __syncwarp();
-        if (sm.status & ST_EPA_OVERFLOW) return false;
-        nf = sm.nf;
-        int ne = sm.ne;
-        for (int i = (int)lane; i < ne; i += WARP) {
-            uchar2 e = sm.u.epa.e[i];
-            sm.u.epa.f[nf + i] = make_uchar4(e.x, e.y, (unsigned char)np, 0);
-            epa_face(sm, nf + i, np + 1);
-        }
+        for (int i = (int)lane; i < ne; i += WARP) epa_face(sm, nf + i, np + 1);
         __syncwarp();
         if (lane == 0) sm.nf = nf + ne;
         nf += ne;

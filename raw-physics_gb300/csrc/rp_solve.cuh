@@ -333,6 +333,130 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
 }
 
 // --------------------------------------------------------------------------------------------
+// FP32 build: a node's bodies as an FP64 base pose plus FP32 deltas.
+//
+// A solver node applies a handful of small corrections to its two bodies. Each body's pose is read
+// once in FP64 (x0, q0); corrections accumulate in FP32 deltas (dx, dq) relative to it, and the FP64
+// pose is written back once: x = x0 + dx, q = normalize(q0 + dq). The renormalisation after every
+// orientation update (pbd_base_constraints.cpp:83-103) is carried out exactly in delta form:
+// with u = dq + increment and e = |q0 + u|^2 - 1 = 2 q0.u + u.u, the normalised quaternion is
+// q0 + q0 (r - 1) + u r with r - 1 = -e / (s (1 + s)), s = sqrt(1 + e), all of which are small,
+// well-conditioned FP32 quantities. Per contact the solve then needs no FP64 arithmetic at all.
+struct FBody {
+    V3<double> x0;
+    Qt<double> q0;
+    V3<float> dx;
+    Qt<float> q0f, dq;
+    float invm;
+    M3<float> Iinv;
+    bool fixed;
+    int idx;
+    __device__ __forceinline__ Qt<float> q() const { return qt<float>(q0f.x + dq.x, q0f.y + dq.y, q0f.z + dq.z, q0f.w + dq.w); }
+};
+
+__device__ __forceinline__ FBody load_fbody(const WorldView<float>& W, int b) {
+    FBody B;
+    double4_32a p = W.pos[b], q = W.rot[b];
+    B.x0 = v3<double>(p.x, p.y, p.z);
+    B.q0 = qt<double>(q.x, q.y, q.z, q.w);
+    B.q0f = qcast<float>(B.q0);
+    B.dx = v3<float>(0.f, 0.f, 0.f);
+    B.dq = qt<float>(0.f, 0.f, 0.f, 0.f);
+    B.invm = W.inv_mass[b];
+    float s[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] = W.inv_inertia[6 * b + i];
+    B.Iinv = msym(s);
+    B.fixed = W.fixed[b] != 0;
+    B.idx = b;
+    return B;
+}
+
+__device__ __forceinline__ void store_fbody(const WorldView<float>& W, const FBody& B) {
+    if (B.fixed) return;
+    V3<double> x = vadd(B.x0, v3cast<double>(B.dx));
+    Qt<double> q = qnormalize_fast(qt<double>(B.q0.x + (double)B.dq.x, B.q0.y + (double)B.dq.y, B.q0.z + (double)B.dq.z,
+                                              B.q0.w + (double)B.dq.w));
+    W.pos[B.idx] = make_double4_32a(x.x, x.y, x.z, 0.0);
+    W.rot[B.idx] = make_double4_32a(q.x, q.y, q.z, q.w);
+}
+
+// q <- normalize(q + inc), in delta form
+__device__ __forceinline__ void frot_update(FBody& B, Qt<float> inc) {
+    Qt<float> u = qt<float>(B.dq.x + inc.x, B.dq.y + inc.y, B.dq.z + inc.z, B.dq.w + inc.w);
+    float e = 2.f * (B.q0f.x * u.x + B.q0f.y * u.y + B.q0f.z * u.z + B.q0f.w * u.w) + (u.x * u.x + u.y * u.y + u.z * u.z + u.w * u.w);
+    float s = sqrtf(1.f + e);
+    float rm1 = -e / (s * (1.f + s));
+    float r = 1.f + rm1;
+    B.dq = qt<float>(B.q0f.x * rm1 + u.x * r, B.q0f.y * rm1 + u.y * r, B.q0f.z * rm1 + u.z * r, B.q0f.w * rm1 + u.w * r);
+}
+
+__device__ __forceinline__ Pcpd<float> fpcpd(const FBody& a, const FBody& b, V3<float> r1_lc, V3<float> r2_lc) {
+    Pcpd<float> p;
+    Qt<float> qa = a.q(), qb = b.q();
+    p.r1 = qrotate(qa, r1_lc);
+    p.r2 = qrotate(qb, r2_lc);
+    p.I1 = world_tensor(qa, a.Iinv);
+    p.I2 = world_tensor(qb, b.Iinv);
+    return p;
+}
+
+__device__ __forceinline__ float fpos_dlambda(const FBody& a, const FBody& b, const Pcpd<float>& p, float lambda_til_free, V3<float> dx) {
+    (void)lambda_til_free;
+    float c = vlen(dx);
+    if (c <= 0.f) return 0.f;
+    V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
+    float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
+    float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    return -c / (w1 + w2);   // contacts carry zero compliance (pbd.cpp:123,133)
+}
+
+__device__ __forceinline__ void fpos_apply(FBody& a, FBody& b, const Pcpd<float>& p, float dl, V3<float> dx) {
+    float c = vlen(dx);
+    if (c <= 0.f) return;
+    V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
+    V3<float> imp = vscale(dl, n);
+    if (!a.fixed) a.dx = vadd(a.dx, vscale(a.invm, imp));
+    if (!b.fixed) b.dx = vadd(b.dx, vscale(-b.invm, imp));
+    V3<float> a1 = mmulv(p.I1, vcross(p.r1, imp));
+    V3<float> a2 = mmulv(p.I2, vcross(p.r2, imp));
+    Qt<float> q1 = qmul(qt<float>(a1.x, a1.y, a1.z, 0.f), a.q());
+    Qt<float> q2 = qmul(qt<float>(a2.x, a2.y, a2.z, 0.f), b.q());
+    if (!a.fixed) frot_update(a, qt<float>(0.5f * q1.x, 0.5f * q1.y, 0.5f * q1.z, 0.5f * q1.w));
+    if (!b.fixed) frot_update(b, qt<float>(-0.5f * q2.x, -0.5f * q2.y, -0.5f * q2.z, -0.5f * q2.w));
+}
+
+// collision_constraint_solve (pbd.cpp:107-154) on FP32 deltas; base_ab = (float)(x0_a - x0_b)
+static __device__ void fcollision_solve(const WorldView<float>& W, FBody& a, FBody& b, V3<float> base_ab, float* c, float mus) {
+    V3<float> r1 = v3<float>(c[0], c[1], c[2]), r2 = v3<float>(c[4], c[5], c[6]), n = v3<float>(c[8], c[9], c[10]);
+    float lambda_n = c[3], lambda_t = c[7];
+    Pcpd<float> p = fpcpd(a, b, r1, r2);
+    V3<float> d12 = vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2));
+    float d = vdot(d12, n);
+    if (d > 0.f) {
+        V3<float> dx = vscale(d, n);
+        float dl = fpos_dlambda(a, b, p, 0.f, dx);
+        fpos_apply(a, b, p, dl, dx);
+        lambda_n += dl;
+        p = fpcpd(a, b, r1, r2);
+        dl = fpos_dlambda(a, b, p, 0.f, dx);
+        float lt = lambda_t + dl;
+        if (lt > mus * lambda_n) {
+            double4_32a pa = W.prev_pos[a.idx], qa = W.prev_rot[a.idx], pb = W.prev_pos[b.idx], qb = W.prev_rot[b.idx];
+            Qt<float> qa_prev = qcast<float>(qt<double>(qa.x, qa.y, qa.z, qa.w)), qb_prev = qcast<float>(qt<double>(qb.x, qb.y, qb.z, qb.w));
+            V3<float> da = vadd(vadd(v3cast<float>(vsub(a.x0, v3<double>(pa.x, pa.y, pa.z))), a.dx), vsub(p.r1, qrotate(qa_prev, r1)));
+            V3<float> db = vadd(vadd(v3cast<float>(vsub(b.x0, v3<double>(pb.x, pb.y, pb.z))), b.dx), vsub(p.r2, qrotate(qb_prev, r2)));
+            V3<float> dp = vsub(da, db);
+            V3<float> dpt = vsub(dp, vscale(vdot(dp, n), n));
+            fpos_apply(a, b, p, dl, dpt);
+            lambda_t += dl;
+        }
+    }
+    c[3] = lambda_n;
+    c[7] = lambda_t;
+}
+
+// --------------------------------------------------------------------------------------------
 // Predict (pbd.cpp:537-577) for one body
 template <typename R, bool EXACT>
 __device__ void predict_body(const WorldView<R>& W, int b, double h) {
@@ -403,12 +527,16 @@ __device__ void velocity_body(const WorldView<R>& W, int b, double h) {
 }
 
 // Velocity solver for one contact (pbd.cpp:646-711); velocities of the two bodies are in registers.
+// p: the contact's preprocessed data from the current poses (anchors in world orientation, world
+// inverse inertias); a / b: inverse mass and fixed flag of the two bodies.
+template <typename R>
+struct VelBody { R invm; bool fixed; };
+
 template <typename R, bool EXACT>
-__device__ void contact_velocity(const WorldView<R>& W, const Body<R>& a, const Body<R>& b, const R* c, R h, R mud, R e,
+__device__ void contact_velocity(const Pcpd<R>& p, VelBody<R> a, VelBody<R> b, const R* c, R h, R mud, R e,
                                  V3<R>& va, V3<R>& wa, V3<R>& vb, V3<R>& wb, V3<R> pva, V3<R> pwa, V3<R> pvb, V3<R> pwb) {
-    V3<R> r1 = v3<R>(c[0], c[1], c[2]), r2 = v3<R>(c[4], c[5], c[6]), n = v3<R>(c[8], c[9], c[10]);
+    V3<R> n = v3<R>(c[8], c[9], c[10]);
     R lambda_n = c[3];
-    Pcpd<R> p = pcpd(a, b, r1, r2);
     V3<R> v = vsub(vadd(va, vcross(wa, p.r1)), vadd(vb, vcross(wb, p.r2)));
     R vn = vdot(n, v);
     V3<R> vt = vsub(v, vscale(vn, n));

@@ -560,12 +560,20 @@ __device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
     const int nc = W.pair_ccount[p];
     if (nc == 0) return;
     int2 pr = W.pairs[p];
-    Body<R> a = load_body(W, pr.x), b = load_body(W, pr.y);
     const R mus = (W.material[4 * pr.x] + W.material[4 * pr.y]) / (R)2.0f;
     R* c = W.contacts + 12 * (size_t)(W.scene_contact_cap[s] + W.pair_cstart[p]);
-    for (int i = 0; i < nc; ++i) collision_solve<R, EXACT>(W, a, b, c + 12 * i, h, mus);
-    store_pose(W, a);
-    store_pose(W, b);
+    if constexpr (EXACT) {
+        Body<R> a = load_body(W, pr.x), b = load_body(W, pr.y);
+        for (int i = 0; i < nc; ++i) collision_solve<R, EXACT>(W, a, b, c + 12 * i, h, mus);
+        store_pose(W, a);
+        store_pose(W, b);
+    } else {
+        FBody a = load_fbody(W, pr.x), b = load_fbody(W, pr.y);
+        const V3<float> base_ab = v3cast<float>(vsub(a.x0, b.x0));
+        for (int i = 0; i < nc; ++i) fcollision_solve(W, a, b, base_ab, c + 12 * i, mus);
+        store_fbody(W, a);
+        store_fbody(W, b);
+    }
 }
 
 template <typename R, bool EXACT>
@@ -576,8 +584,25 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
     const int nc = W.pair_ccount[p];
     if (nc == 0) return;
     int2 pr = W.pairs[p];
-    Body<R> a = load_body(W, pr.x), b = load_body(W, pr.y);
     const int ia = pr.x, ib = pr.y;
+    // anchors rotated by the current orientations (the FP32 build converts each orientation once)
+    Qt<R> qa, qb;
+    M3<R> Ia, Ib;
+    VelBody<R> a, b;
+    {
+        double4_32a q4a = W.rot[ia], q4b = W.rot[ib];
+        qa = qcast<R>(qt<double>(q4a.x, q4a.y, q4a.z, q4a.w));
+        qb = qcast<R>(qt<double>(q4b.x, q4b.y, q4b.z, q4b.w));
+        R sa[6], sb[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) { sa[i] = W.inv_inertia[6 * ia + i]; sb[i] = W.inv_inertia[6 * ib + i]; }
+        Ia = world_tensor(qa, msym(sa));
+        Ib = world_tensor(qb, msym(sb));
+        a.invm = W.inv_mass[ia];
+        b.invm = W.inv_mass[ib];
+        a.fixed = W.fixed[ia] != 0;
+        b.fixed = W.fixed[ib] != 0;
+    }
     V3<R> va = v3<R>(W.vel[3 * ia], W.vel[3 * ia + 1], W.vel[3 * ia + 2]);
     V3<R> wa = v3<R>(W.omega[3 * ia], W.omega[3 * ia + 1], W.omega[3 * ia + 2]);
     V3<R> vb = v3<R>(W.vel[3 * ib], W.vel[3 * ib + 1], W.vel[3 * ib + 2]);
@@ -589,7 +614,15 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
     const R mud = (W.material[4 * ia + 1] + W.material[4 * ib + 1]) / (R)2.0f;
     const R e = W.material[4 * ia + 2] * W.material[4 * ib + 2];
     const R* c = W.contacts + 12 * (size_t)(W.scene_contact_cap[s] + W.pair_cstart[p]);
-    for (int i = 0; i < nc; ++i) contact_velocity<R, EXACT>(W, a, b, c + 12 * i, h, mud, e, va, wa, vb, wb, pva, pwa, pvb, pwb);
+    for (int i = 0; i < nc; ++i) {
+        const R* ci = c + 12 * i;
+        Pcpd<R> pc;   // calculate_positional_constraint_preprocessed_data (the poses do not change here)
+        pc.r1 = qrotate(qa, v3<R>(ci[0], ci[1], ci[2]));
+        pc.r2 = qrotate(qb, v3<R>(ci[4], ci[5], ci[6]));
+        pc.I1 = Ia;
+        pc.I2 = Ib;
+        contact_velocity<R, EXACT>(pc, a, b, ci, h, mud, e, va, wa, vb, wb, pva, pwa, pvb, pwb);
+    }
     if (!a.fixed) {
         W.vel[3 * ia] = va.x; W.vel[3 * ia + 1] = va.y; W.vel[3 * ia + 2] = va.z;
         W.omega[3 * ia] = wa.x; W.omega[3 * ia + 1] = wa.y; W.omega[3 * ia + 2] = wa.z;

@@ -69,6 +69,7 @@ SIGNATURES = {
     "rp_kernel_launches": (_u64, [_W]),
     "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
     "rp_phase_times": (_i, [_W, _P(_d)]),
+    "rp_last_contacts": (_i, [_W, _i, _P(_i), _P(_d), _u, _P(_u)]),
     "rp_set_timing": (_i, [_W, _i]),
     "rp_last_step_ms": (_i, [_W, _P(_d)]),
 }
@@ -293,6 +294,16 @@ class World:
         n = _u()
         self._check(self.lib.rp_contacts(self.h, e1, e2, _dp(out), cap, C.byref(n)))
         return out[: min(n.value, cap) * CONTACT_DOUBLES].reshape(-1, CONTACT_DOUBLES)
+
+    def last_contacts(self, scene: int = 0):
+        """(pairs (k,2), constraints (k,11)) of the last substep of the last simulate call."""
+        cap = 1 << 16
+        pairs = np.zeros(2 * cap, dtype=np.int32)
+        out = np.zeros(11 * cap)
+        n = _u()
+        self._check(self.lib.rp_last_contacts(self.h, scene, pairs.ctypes.data_as(_P(_i)), _dp(out), cap, C.byref(n)))
+        k = min(n.value, cap)
+        return pairs[: 2 * k].reshape(-1, 2), out[: 11 * k].reshape(-1, 11)
 
     def counters(self):
         out = (C.c_uint64 * 8)()
