@@ -278,6 +278,16 @@ def run_ours(args):
                            "parallelism": "replicas only" if world_size > 1 else "single scene, one GPU",
                            "pairs_per_step": pairs_per_step, "contacts_per_step": contacts_per_step,
                            "levels_per_step": (c1[7] - c0[7]) / args.steps,
+                           "gjk_iters_per_step": (c1[0] - c0[0]) / args.steps,
+                           "epa_calls_per_step": (c1[2] - c0[2]) / args.steps,
+                           "epa_iters_per_step": (c1[1] - c0[1]) / args.steps,
+                           "gjk_cap_hits_per_step": (c1[8] - c0[8]) / args.steps,
+                           "epa_cap_hits_per_step": (c1[9] - c0[9]) / args.steps,
+                           "pair_cycles_max": c1[10],
+                           "pair_cycles_mean": (c1[11] - c0[11]) / max(1, c1[12] - c0[12]),
+                           "pairs_narrowphased_per_step": (c1[12] - c0[12]) / args.steps,
+                           "pairs_bounds_apart_per_step": (c1[13] - c0[13]) / args.steps,
+                           "gjk_epa_manifold_cycles_per_step": [(c1[k] - c0[k]) / args.steps for k in (14, 15, 16)],
                            "phase_ms_per_step": phase_ms},
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

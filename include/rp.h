@@ -184,8 +184,13 @@ rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t
 rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, double* out, uint32_t cap, uint32_t* count);
 /* Counters accumulated since creation: [0] GJK iterations, [1] EPA iterations, [2] EPA calls,
  * [3] steps, [4] substeps, [5] contacts generated, [6] broad-phase pairs (summed over steps),
- * [7] solver levels (summed over steps). */
-rp_status rp_counters(rp_world* w, uint64_t out[8]);
+ * [7] solver levels (summed over steps), [8] GJK calls that hit the 100-iteration cap,
+ * [9] EPA calls that hit the 100-iteration cap, [10] largest narrowphase cost of one pair
+ * (SM clock cycles), [11] narrowphase cycles summed over pairs, [12] pairs narrowphased,
+ * [13] pairs skipped because their bounding box and sphere are certainly apart, [14] GJK cycles,
+ * [15] EPA cycles, [16] contact-manifold cycles (summed over calls), [17..19] reserved (0). */
+#define RP_NUM_COUNTERS 20
+rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */
 uint64_t  rp_kernel_launches(const rp_world* w);
 /* Device time per phase of the step kernel since creation, in ms, as seen by the first thread of

@@ -10,6 +10,7 @@
 #include "rp_world.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -109,12 +110,12 @@ struct rp_world {
     DevBuf d_scene_body, d_scene_ext, d_scene_pair_cap, d_scene_contact_cap, d_scene_node_cap;
     DevBuf d_pos, d_rot, d_ppos, d_prot, d_vel, d_omega, d_pvel, d_pomega, d_active, d_deact;
     DevBuf d_backup;
-    DevBuf d_invm, d_I, d_Iinv, d_mat, d_radius, d_fixed, d_col_start, d_force, d_torque;
+    DevBuf d_invm, d_I, d_Iinv, d_mat, d_radius, d_bound, d_fixed, d_col_start, d_force, d_torque;
     DevBuf d_colliders, d_shapes, d_shape_verts, d_face_normal, d_face_elem_start, d_face_elem, d_csr_start, d_csr_data;
     DevBuf d_tverts, d_tnorms, d_ext;
     DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
-        d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_contacts, d_ext_lambda, d_status, d_barrier,
+        d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
         d_counters, d_phase, d_kat_out, d_kat_count;
 
     uint64_t launches = 0;
@@ -298,6 +299,39 @@ rp_status build_device(rp_world* w) {
         rad[slot] = b.radius;
         fixedv[slot] = (uint8_t)b.fixed;
     }
+    // geometric bounds for the narrowphase's separation test: a box and a sphere about the body
+    // origin enclosing every hull vertex, rounded outwards to float; bodies with sphere colliders
+    // get no box and an infinite radius (never separated by this test)
+    std::vector<float4> bound(2 * N);
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX}, r2 = 0.0;
+        bool hulls = !b.cols.empty();
+        for (const rp_collider_desc& d : b.cols) {
+            if (d.type != RP_COLLIDER_HULL) { hulls = false; break; }
+            const Hull& H = *w->hulls[(size_t)d.hull];
+            for (int i = 0; i < H.nv(); ++i) {
+                const double* v = &H.verts[(size_t)(3 * i)];
+                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[k]); hi[k] = std::max(hi[k], v[k]); }
+                r2 = std::max(r2, v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            }
+        }
+        if (!hulls) {
+            bound[2 * slot] = make_float4(0.f, 0.f, 0.f, INFINITY);
+            bound[2 * slot + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        float c[3], hx[3];
+        for (int k = 0; k < 3; ++k) {
+            double cd = 0.5 * (lo[k] + hi[k]);
+            c[k] = (float)cd;
+            double half = 0.5 * (hi[k] - lo[k]) + std::fabs(cd - (double)c[k]);
+            hx[k] = std::nextafter((float)(half * (1.0 + 1e-6)), INFINITY);
+        }
+        float r = std::nextafter((float)(std::sqrt(r2) * (1.0 + 1e-6)), INFINITY);
+        bound[2 * slot] = make_float4(c[0], c[1], c[2], r);
+        bound[2 * slot + 1] = make_float4(hx[0], hx[1], hx[2], 1.f);
+    }
     const size_t R = w->rsize();
     RP_CUDA(upload(w->d_scene_body, w->scene_body, st));
     RP_CUDA(upload(w->d_scene_ext, w->scene_ext, st));
@@ -309,6 +343,7 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(upload(w->d_Iinv, as_working<double>(Ii6, R), st));
     RP_CUDA(upload(w->d_mat, as_working<double>(mat, R), st));
     RP_CUDA(upload(w->d_radius, rad, st));
+    RP_CUDA(upload(w->d_bound, bound, st));
     RP_CUDA(upload(w->d_fixed, fixedv, st));
     RP_CUDA(upload(w->d_col_start, col_start, st));
     RP_CUDA(upload(w->d_colliders, cols, st));
@@ -358,13 +393,14 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(w->d_pair_cstart.ensure(std::max<size_t>(P, 1) * 4));
     RP_CUDA(w->d_pair_ccount.ensure(std::max<size_t>(P, 1) * 4));
     RP_CUDA(w->d_contact_count.ensure((size_t)S * 4));
+    RP_CUDA(w->d_work.ensure((size_t)S * 4));
     RP_CUDA(w->d_contacts.ensure(std::max<size_t>(C, 1) * 12 * R));
     RP_CUDA(w->d_ext_lambda.ensure(std::max<size_t>(E, 1) * 4 * 8));
     if (!w->d_status.p) {
         RP_CUDA(w->d_barrier.ensure(64));
         RP_CUDA(cudaMemsetAsync(w->d_barrier.p, 0, 64, st));
-        RP_CUDA(w->d_counters.ensure(8 * 8));
-        RP_CUDA(cudaMemsetAsync(w->d_counters.p, 0, 64, st));
+        RP_CUDA(w->d_counters.ensure(32 * 8));
+        RP_CUDA(cudaMemsetAsync(w->d_counters.p, 0, 256, st));
         RP_CUDA(w->d_phase.ensure(PHASES * 8));
         RP_CUDA(cudaMemsetAsync(w->d_phase.p, 0, PHASES * 8, st));
     }
@@ -404,6 +440,7 @@ WorldView<R> make_view(rp_world* w) {
     V.inv_inertia = w->d_Iinv.as<R>();
     V.material = w->d_mat.as<R>();
     V.radius = w->d_radius.as<double>();
+    V.bound = w->d_bound.as<float4>();
     V.fixed = w->d_fixed.as<uint8_t>();
     V.col_start = w->d_col_start.as<int32_t>();
     V.force = w->d_force.as<double>();
@@ -439,6 +476,7 @@ WorldView<R> make_view(rp_world* w) {
     V.pair_cstart = w->d_pair_cstart.as<int32_t>();
     V.pair_ccount = w->d_pair_ccount.as<int32_t>();
     V.contact_count = w->d_contact_count.as<int32_t>();
+    V.work = w->d_work.as<int32_t>();
     V.contacts = w->d_contacts.as<R>();
     V.ext_lambda = w->d_ext_lambda.as<double>();
     V.max_levels = w->max_levels;
@@ -1224,12 +1262,12 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
     return RP_OK;
 }
 
-rp_status rp_counters(rp_world* w, uint64_t out[8]) {
+rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]) {
     if (check_world(w) || !out) return RP_ERR_INVALID;
-    for (int k = 0; k < 8; ++k) out[k] = 0;
+    for (int k = 0; k < RP_NUM_COUNTERS; ++k) out[k] = 0;
     if (w->d_counters.p) {
-        unsigned long long c[8];
-        RP_CUDA(cudaMemcpyAsync(c, w->d_counters.p, 64, cudaMemcpyDeviceToHost, w->stream));
+        unsigned long long c[32];
+        RP_CUDA(cudaMemcpyAsync(c, w->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost, w->stream));
         int32_t cc = 0, pc = 0, lv = 0;
         if (w->d_contact_count.p) RP_CUDA(cudaMemcpyAsync(&cc, w->d_contact_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
         if (w->d_pair_count.p) RP_CUDA(cudaMemcpyAsync(&pc, w->d_pair_count.p, 4, cudaMemcpyDeviceToHost, w->stream));
@@ -1238,6 +1276,8 @@ rp_status rp_counters(rp_world* w, uint64_t out[8]) {
         (void)cc; (void)pc; (void)lv;
         out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
         out[5] = c[3]; out[6] = c[5]; out[7] = c[6];
+        out[8] = c[4]; out[9] = c[7]; out[10] = c[8]; out[11] = c[9]; out[12] = c[10]; out[13] = c[11];
+        out[14] = c[12]; out[15] = c[13]; out[16] = c[14];
     }
     out[3] = w->steps;
     out[4] = w->substeps;

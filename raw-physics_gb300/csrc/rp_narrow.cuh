@@ -459,6 +459,199 @@ __device__ bool epa(NarrowSmem<R>& sm, const ColView<R>& c1, const ColView<R>& c
 }
 
 // ---------------------------------------------------------------------------------------------
+// EPA for the FP32 build: the same expansion, termination test and iteration cap as the reference,
+// with every step warp-parallel. Faces are FP32 (their vertices are FP32 Minkowski points); the
+// horizon is found set-wise: an edge of a visible face belongs to it when no other edge of a
+// visible face joins the same two points (by index or position), which is what the reference's
+// toggling add_edge leaves; surviving faces keep their relative order and new faces follow in
+// horizon order, so only exact ties in the closest-face search can resolve differently. The
+// closest face is re-evaluated in FP64 before it is returned.
+template <typename R>
+struct EpaFastSmem {
+    V3<float> poly[EPA_MAXV];
+    V3<float> fn[EPA_MAXF];
+    float fd[EPA_MAXF];
+    uchar4 f[EPA_MAXF];
+    uchar2 edge[3 * WARP];   // edges of this iteration's visible faces
+    uchar2 hz[3 * WARP];     // the horizon
+};
+
+__device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, uchar4 f, V3<float>& n_out, float& d_out, int& status) {
+    V3<float> a = poly[f.x], b = poly[f.y], c = poly[f.z];
+    V3<float> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
+    if (!(n.x != 0.f || n.y != 0.f || n.z != 0.f)) status |= ST_DEGENERATE;
+    float d = vdot(n, a);
+    if (d < -0.f) {
+        n = vinv(n);
+        d = -d;
+    } else if (d >= -0.f && d <= 0.f) {
+        bool ok = false;
+        for (int i = 0; i < npoly; ++i) {
+            float ad = vdot(n, poly[i]);
+            if (ad < -0.f || ad > 0.f) {
+                n = ad < -0.f ? n : vinv(n);
+                ok = true;
+                break;
+            }
+        }
+        if (!ok) status |= ST_DEGENERATE;
+    }
+    n_out = n;
+    d_out = d;
+}
+
+template <typename R>
+__device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView<R>& c2, const Simplex<R>& s,
+                         V3<double>& out_n, double& out_pen, int& iters) {
+    static_assert(sizeof(EpaFastSmem<R>) <= sizeof(typename NarrowSmem<R>::U), "EPA scratch must fit the union");
+    EpaFastSmem<R>& sm = *reinterpret_cast<EpaFastSmem<R>*>(&smr.u);
+    const unsigned lane = lane_id();
+    int st = 0;
+    if (lane == 0) {
+        sm.poly[0] = v3cast<float>(s.a); sm.poly[1] = v3cast<float>(s.b);
+        sm.poly[2] = v3cast<float>(s.c); sm.poly[3] = v3cast<float>(s.d);
+        sm.f[0] = make_uchar4(0, 1, 2, 0);
+        sm.f[1] = make_uchar4(0, 2, 3, 0);
+        sm.f[2] = make_uchar4(0, 3, 1, 0);
+        sm.f[3] = make_uchar4(1, 2, 3, 0);
+    }
+    __syncwarp();
+    int nf = 4, npoly = 4;
+    if (lane < 4) epa_face_f32(sm.poly, 4, sm.f[lane], sm.fn[lane], sm.fd[lane], st);
+    __syncwarp();
+    auto closest = [&](float& md, int& mi) {
+        md = FLT_MAX;
+        mi = 0x7fffffff;
+        for (int i = (int)lane; i < nf; i += WARP)
+            if (sm.fd[i] < md) { md = sm.fd[i]; mi = i; }
+        warp_argmin_first(md, mi);
+    };
+    float min_d;
+    int mi;
+    closest(min_d, mi);
+    for (int it = 0; it < 100; ++it) {
+        iters = it + 1;
+        V3<float> min_n = mi == 0x7fffffff ? v3<float>(0.f, 0.f, 0.f) : sm.fn[mi];
+        V3<float> sp = v3cast<float>(support_mink(c1, c2, v3cast<R>(min_n)));
+        double d = (double)min_n.x * sp.x + (double)min_n.y * sp.y + (double)min_n.z * sp.z;
+        if (fabs(d - (double)min_d) < 0.0001) {
+            // the closest face in FP64 (face normal and depth from its three Minkowski points)
+            uchar4 f = sm.f[mi];
+            V3<double> a = v3cast<double>(sm.poly[f.x]), b = v3cast<double>(sm.poly[f.y]), c = v3cast<double>(sm.poly[f.z]);
+            V3<double> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
+            if (vdot(n, v3cast<double>(min_n)) < 0.0) n = vinv(n);
+            out_n = n;
+            out_pen = vdot(n, a);
+            if (st && lane == 0) atomicOr(&smr.status, st);
+            return true;
+        }
+        if (npoly >= EPA_MAXV) break;
+        const int np = npoly;
+        if (lane == 0) sm.poly[np] = sp;
+        // visibility (epa.cpp:171-179)
+        for (int i = (int)lane; i < nf; i += WARP) {
+            uchar4 f = sm.f[i];
+            V3<float> cen = vscale(1.0f / 3.0f, vadd(vadd(sm.poly[f.y], sm.poly[f.z]), sm.poly[f.x]));
+            f.w = vdot(sm.fn[i], vsub(sp, cen)) > 0.f ? 1 : 0;
+            sm.f[i] = f;
+        }
+        __syncwarp();
+        // edges of the visible faces, in face order
+        int ne = 0;
+        bool overflow = false;
+        for (int base = 0; base < nf; base += WARP) {
+            int i = base + (int)lane;
+            uchar4 f = i < nf ? sm.f[i] : make_uchar4(0, 0, 0, 0);
+            bool v = i < nf && f.w;
+            unsigned m = __ballot_sync(0xffffffffu, v);
+            int pos = ne + 3 * __popc(m & ((1u << lane) - 1u));
+            if (v) {
+                if (pos + 3 <= 3 * WARP) {
+                    sm.edge[pos] = make_uchar2(f.x, f.y);
+                    sm.edge[pos + 1] = make_uchar2(f.y, f.z);
+                    sm.edge[pos + 2] = make_uchar2(f.z, f.x);
+                } else {
+                    overflow = true;
+                }
+            }
+            ne += 3 * __popc(m);
+        }
+        overflow = __any_sync(0xffffffffu, overflow) || ne > 3 * WARP;
+        __syncwarp();
+        if (overflow) { st |= ST_EPA_OVERFLOW; break; }
+        // horizon: the toggling add_edge keeps one edge of every class of coincident edges (same
+        // two points, by index or position) that occurs an odd number of times
+        int nh = 0;
+        for (int base = 0; base < ne; base += WARP) {
+            int k = base + (int)lane;
+            bool keep = false;
+            uchar2 e = make_uchar2(0, 0);
+            if (k < ne) {
+                e = sm.edge[k];
+                V3<float> e1 = sm.poly[e.x], e2 = sm.poly[e.y];
+                int partners = 0;
+                bool first = true;
+                for (int j = 0; j < ne; ++j) {
+                    if (j == k) continue;
+                    uchar2 g = sm.edge[j];
+                    bool same = (g.x == e.x && g.y == e.y) || (g.x == e.y && g.y == e.x);
+                    if (!same) {
+                        V3<float> g1 = sm.poly[g.x], g2 = sm.poly[g.y];
+                        same = (veq(g1, e1) && veq(g2, e2)) || (veq(g1, e2) && veq(g2, e1));
+                    }
+                    if (same) {
+                        ++partners;
+                        if (j < k) first = false;
+                    }
+                }
+                keep = first && (partners & 1) == 0;
+            }
+            unsigned m = __ballot_sync(0xffffffffu, keep);
+            int pos = nh + __popc(m & ((1u << lane) - 1u));
+            nh += __popc(m);
+            if (keep) sm.hz[pos] = e;
+        }
+        __syncwarp();
+        // compact the surviving (invisible) faces in order
+        int kept = 0;
+        for (int base = 0; base < nf; base += WARP) {
+            int i = base + (int)lane;
+            uchar4 f;
+            V3<float> n;
+            float dd;
+            bool alive = false;
+            if (i < nf) {
+                f = sm.f[i];
+                alive = !f.w;
+                n = sm.fn[i];
+                dd = sm.fd[i];
+            }
+            unsigned m = __ballot_sync(0xffffffffu, alive);
+            int pos = kept + __popc(m & ((1u << lane) - 1u));
+            __syncwarp();
+            if (alive) { sm.f[pos] = f; sm.fn[pos] = n; sm.fd[pos] = dd; }
+            kept += __popc(m);
+            __syncwarp();
+        }
+        if (kept + nh > EPA_MAXF || nh > 3 * WARP) { st |= ST_EPA_OVERFLOW; break; }
+        for (int k = (int)lane; k < nh; k += WARP) {
+            uchar2 e = sm.hz[k];
+            uchar4 f = make_uchar4(e.x, e.y, (unsigned char)np, 0);
+            sm.f[kept + k] = f;
+            epa_face_f32(sm.poly, np + 1, f, sm.fn[kept + k], sm.fd[kept + k], st);
+        }
+        __syncwarp();
+        nf = kept + nh;
+        npoly = np + 1;
+        closest(min_d, mi);
+    }
+    st = __reduce_or_sync(0xffffffffu, st);
+    if (lane == 0 && st) atomicOr(&smr.status, st);
+    __syncwarp();
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Clipping (clipping.cpp)
 template <typename R>
 __device__ __forceinline__ bool in_plane(V3<R> pn, V3<R> pp, V3<R> pos) {
@@ -710,6 +903,14 @@ __device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const
     }
 }
 
+// EPA of the FP32 build: false runs the FP64 face-normal / termination EPA on the FP32 polytope
+// (follows the reference's expansion path wherever its decisions are not FP32-rounding ties);
+// true runs the all-FP32 EPA with a final FP64 re-evaluation of the chosen face.
+#ifndef RP_EPA_FAST
+#define RP_EPA_FAST 0
+#endif
+constexpr bool kEpaFast = RP_EPA_FAST != 0;
+
 // collider_get_contacts (collider.cpp:523-558)
 template <typename R, bool EXACT>
 __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, const ColView<R>& c1, const ColView<R>& c2,
@@ -727,19 +928,32 @@ __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, cons
     }
     Simplex<R> s;
     int gi = 0, ei = 0;
+    const long long t0 = clock64();
     bool hit = gjk_collides(c1, c2, s, gi);
-    if (counters && lane_id() == 0) atomicAdd(&counters[0], (unsigned long long)gi);
+    const long long t1 = clock64();
+    if (counters && lane_id() == 0) {
+        atomicAdd(&counters[0], (unsigned long long)gi);
+        atomicAdd(&counters[12], (unsigned long long)(t1 - t0));
+        if (gi >= 100) atomicAdd(&counters[4], 1ull);
+    }
     if (!hit) return;
     V3<double> n;
     double pen;
-    bool ok = epa(sm, c1, c2, s, n, pen, ei);
-    if (counters && lane_id() == 0) { atomicAdd(&counters[1], (unsigned long long)ei); atomicAdd(&counters[2], 1ull); }
+    bool ok = (EXACT || !kEpaFast) ? epa(sm, c1, c2, s, n, pen, ei) : epa_fast(sm, c1, c2, s, n, pen, ei);
+    const long long t2 = clock64();
+    if (counters && lane_id() == 0) {
+        atomicAdd(&counters[1], (unsigned long long)ei);
+        atomicAdd(&counters[2], 1ull);
+        atomicAdd(&counters[13], (unsigned long long)(t2 - t1));
+        if (ei >= 100) atomicAdd(&counters[7], 1ull);
+    }
     if (!ok) {
         if (lane_id() == 0) atomicOr(&sm.status, (int)ST_EPA_NOT_CONVERGED);
         __syncwarp();
         return;
     }
     contact_manifold<R, EXACT>(sm, W, c1, c2, v3cast<R>(n), n, (R)pen, fr);
+    if (counters && lane_id() == 0) atomicAdd(&counters[14], (unsigned long long)(clock64() - t2));
 }
 
 }  // namespace rp

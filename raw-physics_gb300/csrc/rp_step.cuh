@@ -504,6 +504,48 @@ __device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, i
     }
 }
 
+// Gap between the box bound of one body and the sphere bound of another (metres, FP32; exact up to
+// ~1e-6 relative), and the scale its rounding error is relative to.
+__device__ __forceinline__ float box_sphere_gap(float4 c, float4 hx, double4_32a pbox, double4_32a qbox, double4_32a psph,
+                                                float rs, float& scale) {
+    const float dx = (float)(psph.x - pbox.x), dy = (float)(psph.y - pbox.y), dz = (float)(psph.z - pbox.z);
+    const float ux = -(float)qbox.x, uy = -(float)qbox.y, uz = -(float)qbox.z, qw = (float)qbox.w;
+    // rotate d by the inverse of the box body's rotation: v = d + w t + u x t, t = 2 u x d
+    const float tx = 2.f * (uy * dz - uz * dy), ty = 2.f * (uz * dx - ux * dz), tz = 2.f * (ux * dy - uy * dx);
+    const float vx = dx + qw * tx + (uy * tz - uz * ty);
+    const float vy = dy + qw * ty + (uz * tx - ux * tz);
+    const float vz = dz + qw * tz + (ux * ty - uy * tx);
+    const float ex = fmaxf(fabsf(vx - c.x) - hx.x, 0.f), ey = fmaxf(fabsf(vy - c.y) - hx.y, 0.f),
+                ez = fmaxf(fabsf(vz - c.z) - hx.z, 0.f);
+    scale = fabsf(dx) + fabsf(dy) + fabsf(dz) + fabsf(c.x) + fabsf(c.y) + fabsf(c.z) + hx.x + hx.y + hx.z + rs;
+    return sqrtf(ex * ex + ey * ey + ez * ez) - rs;
+}
+
+// True only when the hulls of bodies a and b are certainly apart by much more than rounding: the
+// box bound of one misses the sphere bound of the other. For such a pair gjk_collides
+// (gjk.cpp:350-379) cannot find the origin inside the Minkowski difference and returns false, so
+// the pair yields no contact; skipping it changes no result. Non-unit rotations are never skipped.
+template <typename R>
+__device__ __forceinline__ bool bounds_apart(const WorldView<R>& W, int a, int b) {
+    const double4_32a pa = W.pos[a], pb = W.pos[b], qa = W.rot[a], qb = W.rot[b];
+    const float4 ca = W.bound[2 * a], ha = W.bound[2 * a + 1], cb = W.bound[2 * b], hb = W.bound[2 * b + 1];
+    const double na = qa.x * qa.x + qa.y * qa.y + qa.z * qa.z + qa.w * qa.w;
+    const double nb = qb.x * qb.x + qb.y * qb.y + qb.z * qb.z + qb.w * qb.w;
+    if (fabs(na - 1.0) > 1e-6 || fabs(nb - 1.0) > 1e-6) return false;
+    float scale;
+    if (ha.w != 0.f) {
+        float gap = box_sphere_gap(ca, ha, pa, qa, pb, cb.w, scale);
+        if (gap > 1e-5f * scale + 1e-6f) return true;
+    }
+    if (hb.w != 0.f) {
+        float gap = box_sphere_gap(cb, hb, pb, qb, pa, ca.w, scale);
+        if (gap > 1e-5f * scale + 1e-6f) return true;
+    }
+    return false;
+}
+
+// Pairs are handed out one at a time from a per-scene counter (work[s], reset before the substep's
+// predict phase); a warp fetches its next pair while it computes the current one.
 template <typename R, bool EXACT, class G>
 __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem<R>& sm) {
     const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
@@ -511,16 +553,29 @@ __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem
     const int cbase = W.scene_contact_cap[s];
     const int ccap = W.scene_contact_cap[s + 1] - cbase;
     const int lane = threadIdx.x & 31;
-    const int gw = g.rank() >> 5, nw = g.size() >> 5;
-    for (int p = gw; p < np; p += nw) {
+    unsigned long long cyc_sum = 0, cyc_max = 0, n_full = 0, n_apart = 0, n_contacts = 0;
+    int p = 0;
+    if (lane == 0) p = atomicAdd(&W.work[s], 1);
+    p = __shfl_sync(0xffffffffu, p, 0);
+    while (p < np) {
+        int next = 0;
+        if (lane == 0) next = atomicAdd(&W.work[s], 1);
         int2 pr = W.pairs[pbase + p];
         int a = pr.x, b = pr.y;
         bool live = !((W.fixed[a] || !W.active[a]) && (W.fixed[b] || !W.active[b]));
-        if (!live) {
+        bool apart = live && bounds_apart(W, a, b);
+        if (!live || apart) {
             if (lane == 0) { W.pair_ccount[pbase + p] = 0; W.pair_cstart[pbase + p] = 0; }
+            n_apart += apart;
+            p = __shfl_sync(0xffffffffu, next, 0);
             continue;
         }
+        const long long t0 = clock64();
         pair_contacts<R, EXACT>(W, sm, a, b, false);
+        const unsigned long long dt = (unsigned long long)(clock64() - t0);
+        cyc_sum += dt;
+        cyc_max = max(cyc_max, dt);
+        ++n_full;
         int nc = sm.ncontacts;
         int start = 0;
         if (lane == 0) {
@@ -530,7 +585,7 @@ __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem
                 nc = 0;
             }
             if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
-            if (nc) atomicAdd(&W.counters[3], (unsigned long long)nc);
+            n_contacts += nc;
             W.pair_cstart[pbase + p] = start;
             W.pair_ccount[pbase + p] = nc;
         }
@@ -544,6 +599,14 @@ __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem
             c[8] = n.x; c[9] = n.y; c[10] = n.z; c[11] = 0;
         }
         __syncwarp();
+        p = __shfl_sync(0xffffffffu, next, 0);
+    }
+    if (lane == 0 && (n_full | n_apart)) {
+        if (n_contacts) atomicAdd(&W.counters[3], n_contacts);
+        atomicMax(&W.counters[8], cyc_max);
+        atomicAdd(&W.counters[9], cyc_sum);
+        atomicAdd(&W.counters[10], n_full);
+        atomicAdd(&W.counters[11], n_apart);
     }
 }
 
@@ -707,7 +770,7 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
         for (int b = b0 + g.rank(); b < b1; b += g.size()) predict_body<R, EXACT>(W, b, h);
         for (int e = e0 + g.rank(); e < e1; e += g.size())
             for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
-        if (g.rank() == 0) W.contact_count[s] = 0;
+        if (g.rank() == 0) { W.contact_count[s] = 0; W.work[s] = 0; }
         g.sync();
         mark(PH_PREDICT);
         if (P.enable_collisions) {
@@ -732,7 +795,7 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
 }
 
 template <typename R, bool EXACT>
-__global__ void __launch_bounds__(BLOCK) step_kernel_cta(WorldView<R> W, StepParams P) {
+__global__ void __launch_bounds__(BLOCK, 1) step_kernel_cta(WorldView<R> W, StepParams P) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ int scan_smem[32];
     NarrowSmem<R>* sms = reinterpret_cast<NarrowSmem<R>*>(dyn_smem);
@@ -745,7 +808,7 @@ __global__ void __launch_bounds__(BLOCK) step_kernel_cta(WorldView<R> W, StepPar
 }
 
 template <typename R, bool EXACT>
-__global__ void __launch_bounds__(BLOCK) step_kernel_grid(WorldView<R> W, StepParams P) {
+__global__ void __launch_bounds__(BLOCK, 1) step_kernel_grid(WorldView<R> W, StepParams P) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ int scan_smem[32];
     NarrowSmem<R>* sms = reinterpret_cast<NarrowSmem<R>*>(dyn_smem);

@@ -99,6 +99,9 @@ struct WorldView {
     const R* inv_inertia;   // [6N]
     const R* material;      // [4N] static friction, dynamic friction, restitution, (unused)
     const double* radius;   // bounding_sphere_radius
+    const float4* bound;    // [2N] geometric bound of the body's hulls in its local frame, rounded
+                            // outwards: (box centre xyz, radius of the vertices about the body origin),
+                            // (box half extents xyz, 1 when the body has a box, 0 when it has none)
     const uint8_t* fixed;
     const int32_t* col_start;   // [N+1] collider ranges
     const double* force;     // [3N] sum of external forces (calculate_external_force)
@@ -137,13 +140,14 @@ struct WorldView {
     int32_t* pair_cstart;    // [pairs] first contact of each pair
     int32_t* pair_ccount;    // [pairs]
     int32_t* contact_count;  // [S] contacts allocated this substep
+    int32_t* work;           // [S] next broad-phase pair to narrowphase (dynamic work distribution)
     R* contacts;             // [12 * contacts] r1_lc, lambda_n, r2_lc, lambda_t, normal, (unused)
     double* ext_lambda;      // [4 * ext] per-substep lambdas of external constraints
     int32_t max_levels;
     // ---- control ----------------------------------------------------------------------------
     uint32_t* status;        // [S] status bits per scene
     unsigned int* barrier;   // [2] grid barrier counter / generation
-    unsigned long long* counters; // [8] diagnostics: gjk/epa iterations, contacts, ...
+    unsigned long long* counters; // [32] diagnostics: gjk/epa iterations and cap hits, contacts, pair cycles
     unsigned long long* phase_ns; // [PHASES] time spent per phase of the step, seen by group rank 0
 };
 

@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_DIR, "librawphys_gb300.so")
+LIB_PATH = os.environ.get("RAWPHYS_LIB") or os.path.join(PKG_DIR, "librawphys_gb300.so")
 
 STATE_DOUBLES = 28
 CONTACT_DOUBLES = 9
@@ -306,7 +306,7 @@ class World:
         return pairs[: 2 * k].reshape(-1, 2), out[: 11 * k].reshape(-1, 11)
 
     def counters(self):
-        out = (C.c_uint64 * 8)()
+        out = (C.c_uint64 * 20)()
         self._check(self.lib.rp_counters(self.h, out))
         return list(out)
 

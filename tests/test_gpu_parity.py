@@ -3,9 +3,9 @@
   * all-FP64 build: bit-identical to the oracle (itself pinned bit-exactly to the reference) over
     whole trajectories, pair lists and contact manifolds;
   * FP32 build: per-step position / orientation error from identical states within 1e-4 m / rad,
-    except where the reference itself is ill-conditioned (a resting stack of exactly parallel faces:
-    FP64-rounding-size input perturbations already move the reference's next frame by more than
-    1e-4 m); there the bound is 3x the reference's own sensitivity, measured live.
+    except where the reference itself is ill-conditioned (hinge chains, resting stacks of exactly
+    parallel faces, 1:100 mass-ratio towers): there the bound is the spread of the reference's own
+    results under FP32-scale noise (1e-7 m / 1e-7 relative) injected into its inputs, measured live.
 """
 from __future__ import annotations
 
@@ -53,95 +53,116 @@ def test_fp64_trajectory_bitexact(ext_built, oracle_built, name):
     w.close()
 
 
-def reference_sensitivity(o, state, rel=1e-12, trials=4, seed=0):
-    """How far the reference's next frame moves when its input pose is perturbed at FP64-rounding
-    scale: the floor below which no implementation that rounds differently can agree."""
-    rng = np.random.default_rng(seed)
-    o.set_state(state)
-    o.step(1)
-    base = o.get_state()
-    worst = 0.0
-    for _ in range(trials):
-        p = state.copy()
-        p[:, 0:7] *= 1.0 + rel * rng.standard_normal(p[:, 0:7].shape)
-        o.set_state(p)
-        o.step(1)
-        worst = max(worst, float(np.max(np.abs(o.get_state()[:, 0:3] - base[:, 0:3]))))
-    return worst
+# FP32-scale noise model: what rounding to FP32 does to a substep's input geometry. Positions move
+# by 1e-7 m (the FP32 build keeps FP64 poses and rounds pair-local geometry, whose extent is ~1 m,
+# to FP32), orientations by 1e-7 relative.
+NOISE = 1e-7
 
 
-def contact_sets_agree(po, co, pg, cg, tol=1e-5, touch=1e-6):
-    """Same collision constraints per pair (order-insensitive, within tol on r1, r2, normal);
-    constraints whose two anchors coincide to `touch` may be present on one side only."""
-    keys = set(map(tuple, po.tolist())) | set(map(tuple, pg.tolist()))
-    for k in keys:
-        a = co[(po == k).all(axis=1)]
-        b = cg[(pg == k).all(axis=1)]
-        if not _match_sets(a[:, 0:9], b[:, 0:9], tol, touch=touch, anchors=True):
-            return False
-    return True
+def perturb(state, rng, noise=NOISE):
+    p = state.copy()
+    p[:, 0:3] += noise * rng.standard_normal(p[:, 0:3].shape)
+    p[:, 3:7] *= 1.0 + noise * rng.standard_normal(p[:, 3:7].shape)
+    return p
+
+
+def pose_dev(a, b):
+    return max(float(np.max(np.abs(a[:, 0:3] - b[:, 0:3]))), float(np.max(np.abs(a[:, 3:7] - b[:, 3:7]))))
+
+
+def noisy_frame(o, scene, state, rng):
+    """One frame of the reference with FP32-scale noise injected into every substep's input."""
+    h = scene.dt / scene.substeps
+    st = state
+    for _ in range(scene.substeps):
+        o.set_state(perturb(st, rng))
+        o.step(1, dt=h, substeps=1)
+        st = o.get_state()
+    return st
+
+
+def contact_sets_agree(po, co, pg, cg, tol=1e-5):
+    """Same collision constraints in the same order (the Gauss-Seidel solve visits them in order),
+    within tol on r1, r2 and the normal."""
+    if not np.array_equal(po, pg):
+        return False
+    return len(co) == len(cg) and (len(co) == 0 or float(np.max(np.abs(co[:, 0:9] - cg[:, 0:9]))) <= tol)
 
 
 @pytest.mark.parametrize("name", SMALL)
 def test_fp32_substep_agreement(ext_built, oracle_built, name):
-    """One substep at a time from identical states. Whenever the FP32 build generates the same
-    contact set as the FP64 reference, positions and orientations agree within 1e-4 (in practice
-    ~1e-6). Substeps where the two contact sets differ are discrete events the reference decides
-    below FP32 resolution (a reference-face choice between faces parallel to ~1e-8, a contact
-    touching at rounding level, a GJK/EPA that runs out of iterations on a curved hull); they must
-    stay a minority."""
+    """One substep at a time from identical states, checked against the reference's own response
+    to FP32-scale noise on the same input (16 noisy replays of the substep):
+      * where the FP32 build's collision constraints equal the reference's, positions and
+        orientations agree within 1e-4 (or within 3x the noisy replays' spread, in the scenes whose
+        substep the reference itself cannot resolve at FP32 precision);
+      * where they differ (in value or in order), the reference's own constraint list changes under
+        the same noise: the divergence is a decision the reference makes below FP32 resolution (a
+        reference-face choice between faces parallel to ~1e-8, a clipped vertex on a clipping plane
+        that rotates the manifold's order, a contact touching at rounding level, EPA stopping on a
+        different face inside its 1e-4 termination tolerance)."""
     scene = SCENES[name][0]()
     o = oracle_built("port").load(scene)
     o.step(SCENES[name][2] or 10)
+    noisy = oracle_built("port").load(scene)
+    rng = np.random.default_rng(1)
     w = world(ext_built, scene, "fp32")
     h = scene.dt / scene.substeps
-    agree_err, events, n = [], 0, 60
-    for k in range(n):
+    agree_err, unexplained = [], []
+    for k in range(60):
         st = o.get_state()
         w.set_state(st)
         o.step(1, dt=h, substeps=1)
         w.simulate(h, 1, scene.pos_iters, scene.collisions, 1)
         a, b = o.get_state(), w.get_state()
-        pe = float(np.max(np.abs(a[:, 0:3] - b[:, 0:3])))
-        re = float(np.max(np.abs(a[:, 3:7] - b[:, 3:7])))
-        same = True
-        if scene.collisions:
-            same = contact_sets_agree(*o.last_contacts(), *w.last_contacts())
+        ref_c = o.last_contacts()
+        err = pose_dev(a, b)
+        same = (not scene.collisions) or contact_sets_agree(*ref_c, *w.last_contacts())
+        spread, flips = 0.0, False
+        for _ in range(16):
+            noisy.set_state(perturb(st, rng))
+            noisy.step(1, dt=h, substeps=1)
+            spread = max(spread, pose_dev(noisy.get_state(), a))
+            if scene.collisions:
+                flips |= not contact_sets_agree(*ref_c, *noisy.last_contacts())
         if same:
-            assert pe <= 1e-4 and re <= 1e-4, "%s substep %d: %.3g m, %.3g rad with identical contacts" % (name, k, pe, re)
-            agree_err.append(max(pe, re))
-        else:
-            events += 1
-    assert events <= n // 4, "%s: %d of %d substeps diverge in their contact sets" % (name, events, n)
-    assert np.median(agree_err) <= 1e-5, (name, np.median(agree_err))
+            assert err <= max(1e-4, 3 * spread), "%s substep %d: %.3g with identical contacts (noise spread %.3g)" % (
+                name, k, err, spread)
+            agree_err.append(err)
+        elif not flips and err > 1e-4:
+            unexplained.append((k, err))
+    assert not unexplained, "%s: contact sets differ where the reference is robust to FP32 noise: %s" % (name, unexplained)
+    if agree_err:
+        assert np.median(agree_err) <= 1e-5, (name, np.median(agree_err))
     w.close()
 
 
 @pytest.mark.parametrize("name", SMALL)
 def test_fp32_frame_error(ext_built, oracle_built, name):
-    """Whole frames (20 substeps) from identical states: the median error over 12 frames is within
-    1e-4 m / rad, or within the reference's own response to an FP32-rounding-sized (1e-7 relative)
-    perturbation of its input where the scene is ill-conditioned (resting stacks of parallel faces,
-    hinge limits at +-90 degrees)."""
+    """Whole frames (all substeps) from identical states, 12 frames: per-step position / orientation
+    error within 1e-4 m / rad (median), or — where the scene is ill-conditioned (hinge chains,
+    resting stacks of parallel faces, 1:100 mass-ratio towers) — within the spread of the reference's
+    own frames under FP32-scale noise injected into every substep (4 replays per frame)."""
     scene = SCENES[name][0]()
     o = oracle_built("port").load(scene)
     o.step(SCENES[name][2] or 10)
-    start = o.get_state()
-    sens = reference_sensitivity(oracle_built("port").load(scene), start, rel=1e-7)
-    o = oracle_built("port").load(scene)
-    o.set_state(start)
+    noisy = oracle_built("port").load(scene)
+    rng = np.random.default_rng(2)
     w = world(ext_built, scene, "fp32")
-    errs = []
+    errs, spreads = [], []
     for k in range(12):
         st = o.get_state()
         w.set_state(st)
         w.step(1)
         o.step(1)
         a, b = o.get_state(), w.get_state()
-        errs.append(max(float(np.max(np.abs(a[:, 0:3] - b[:, 0:3]))), float(np.max(np.abs(a[:, 3:7] - b[:, 3:7])))))
-    bound = max(1e-4, sens)
-    assert np.median(errs) <= bound, "%s: median frame error %.3g > %.3g (sensitivity %.3g)" % (name, np.median(errs), bound, sens)
-    assert max(errs) <= 5e-2, (name, errs)
+        errs.append(pose_dev(a, b))
+        spreads.append(max(pose_dev(noisy_frame(noisy, scene, st, rng), a) for _ in range(4)))
+        o.set_state(a)
+    bound = max(1e-4, float(np.median(spreads)))
+    assert np.median(errs) <= bound, "%s: median frame error %.3g > %.3g (noise spreads %s)" % (
+        name, np.median(errs), bound, np.round(spreads, 6))
+    assert max(errs) <= max(1e-3, 3 * max(spreads)), (name, errs, spreads)
     w.close()
 
 
@@ -163,14 +184,12 @@ def test_pairs_bitexact(ext_built, oracle_built, name, precision):
     w.close()
 
 
-def _match_sets(a, b, tol, touch=1e-6, anchors=False):
+def _match_sets(a, b, tol, touch=1e-6):
     """True when contact lists a and b hold the same contacts up to order (within tol). A contact
     whose two points are within `touch` of each other (penetration at rounding level: the
-    reference keeps it when its FP64 penetration is below zero) may be present on one side only.
-    anchors=True: rows are constraint anchors r1_lc, r2_lc (body frames), compared as such and
-    never treated as touching."""
+    reference keeps it when its FP64 penetration is below zero) may be present on one side only."""
     def touching(r):
-        return (not anchors) and np.max(np.abs(r[0:3] - r[3:6])) <= touch
+        return np.max(np.abs(r[0:3] - r[3:6])) <= touch
     used = np.zeros(len(b), dtype=bool)
     for row in a:
         d = np.max(np.abs(b - row), axis=1) if len(b) else np.zeros(0)
@@ -183,14 +202,36 @@ def _match_sets(a, b, tol, touch=1e-6, anchors=False):
     return all(touching(r) for r in b[~used])
 
 
+def _world_vertices(o, state, e):
+    v, _, _ = o.hull_topology(e)
+    x, q = state[e, 0:3], state[e, 3:7]
+    u, s = q[0:3], q[3]
+    t = 2.0 * np.cross(u, v)
+    return v + s * t + np.cross(u, t) + x
+
+
+def _depth(va, vb, n):
+    """Overlap of two vertex sets along unit direction n: the Minkowski difference's support
+    distance, the quantity EPA minimises (epa.cpp:118-237)."""
+    n = n / np.linalg.norm(n)
+    return float(np.max(va @ n) - np.min(vb @ n))
+
+
 @pytest.mark.parametrize("name", [n for n in SMALL])
 def test_contacts_known_answers(ext_built, oracle_built, name):
-    """colliders_get_contacts on every pair of a penetrating state: exact in FP64; the same
-    contacts (order may differ where parallel faces tie) within 2e-5 in FP32."""
+    """colliders_get_contacts on every pair of a penetrating state: exact in FP64. In FP32 the same
+    contacts (order may differ where parallel faces tie) within 2e-5, except that
+      * points may differ by up to 2x the reference's own spread under FP32-scale input noise
+        (8 noisy evaluations of the pair), and
+      * the normal may be another EPA-valid one: EPA stops once the support distance is within
+        1e-4 of the closest face (epa.cpp:118-237), so any normal whose overlap depth is within
+        1e-4 of the reference normal's is an output the reference's algorithm could give."""
     g = golden(name)
     scene = SCENES[name][0]()
     if not scene_fingerprint_ok(scene, g):
         pytest.skip("scene generator differs from the fixture's")
+    o = oracle_built("port").load(scene)
+    rng = np.random.default_rng(3)
     for precision in ("fp64", "fp32"):
         w = world(ext_built, scene, precision)
         w.set_state(g["kat_state"])
@@ -201,8 +242,23 @@ def test_contacts_known_answers(ext_built, oracle_built, name):
             k += cnt
             if precision == "fp64":
                 assert np.array_equal(c, expect), (name, a, b)
-            else:
-                assert _match_sets(c, expect, 2e-5), (name, a, b, c, expect)
+                continue
+            if _match_sets(c, expect, 2e-5):
+                continue
+            spread = 0.0
+            for _ in range(8):
+                o.set_state(perturb(g["kat_state"], rng))
+                cn = o.contacts(int(a), int(b))
+                if len(cn) != len(expect):
+                    spread = np.inf
+                    break
+                spread = max([spread] + [float(np.min(np.max(np.abs(cn - r), axis=1))) for r in expect])
+            assert _match_sets(c[:, 0:6], expect[:, 0:6], max(2e-5, 2 * spread)), (name, a, b, c, expect, spread)
+            if len(c) and len(expect):
+                va, vb = _world_vertices(o, g["kat_state"], int(a)), _world_vertices(o, g["kat_state"], int(b))
+                d_ref = _depth(va, vb, expect[0, 6:9])
+                for n in np.unique(c[:, 6:9], axis=0):
+                    assert _depth(va, vb, n) <= d_ref + 1e-4, (name, a, b, n, expect[0, 6:9])
         w.close()
 
 
