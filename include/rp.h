@@ -53,6 +53,15 @@ enum { RP_PRECISION_FP32 = 0, RP_PRECISION_FP64 = 1 };
  * RP_PRECISION_FP64: every quantity in FP64, evaluated in the reference's operation order without
  *                    FMA contraction (reproduces the reference's FP64 results). */
 
+/* How a frame is launched (rp_world_set_mode). Both give identical results.
+ * RP_MODE_PHASED:     one small kernel per phase (setup, predict, hull transform, GJK, EPA, contact
+ *                     manifold, position and velocity sweeps) over every scene, the frame replayed
+ *                     from a captured CUDA graph. The default.
+ * RP_MODE_PERSISTENT: one persistent kernel per frame (a CTA per scene, or a cooperative grid on a
+ *                     single large scene).
+ * RP_MODE_AUTO:       RP_MODE_PHASED unless the environment variable RP_MODE is "persistent". */
+enum { RP_MODE_AUTO = 0, RP_MODE_PERSISTENT = 1, RP_MODE_PHASED = 2 };
+
 enum { RP_COLLIDER_SPHERE = 0, RP_COLLIDER_HULL = 1 };        /* Collider_Type, collider.h:33-36 */
 enum { RP_AXIS_POS_X = 0, RP_AXIS_NEG_X, RP_AXIS_POS_Y, RP_AXIS_NEG_Y, RP_AXIS_POS_Z, RP_AXIS_NEG_Z }; /* PBD_Axis_Type */
 
@@ -78,6 +87,8 @@ rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision);
 void      rp_world_destroy(rp_world* w);
 /* Use an existing cudaStream_t (passed as void*) for every launch and copy of this world. */
 rp_status rp_world_set_stream(rp_world* w, void* cuda_stream);
+/* Selects the launch mode (RP_MODE_*); no counterpart in the reference. */
+rp_status rp_world_set_mode(rp_world* w, int32_t mode);
 const char* rp_last_error(void);
 /* Adds a new empty scene; scene 0 exists from creation. */
 rp_status rp_scene_create(rp_world* w, int32_t* out_scene);
@@ -116,6 +127,14 @@ rp_status rp_entity_create(rp_world* w, int32_t scene, const double position[3],
                            int32_t fixed, const rp_collider_desc* colliders, uint32_t num_colliders,
                            double static_friction, double dynamic_friction, double restitution, int32_t* out_entity);
 rp_status rp_entity_set_velocity(rp_world* w, int32_t entity, const double linear[3], const double angular[3]);
+/* n calls of rp_entity_create with one collider each (cols[i]), plus optional initial velocities
+ * (vel / omega: 3 doubles per entity, or NULL for zero); arrays hold one entry per entity (pos: 3,
+ * rot: 4). All or nothing: on error no entity is added. *out_first receives the first new entity.
+ * Bulk form for batches of many scenes; no counterpart in the reference. */
+rp_status rp_entities_create(rp_world* w, uint32_t n, const int32_t* scene, const double* pos, const double* rot,
+                             const double* mass, const int32_t* fixed, const rp_collider_desc* cols, const double* mus,
+                             const double* mud, const double* rest, const double* vel, const double* omega,
+                             int32_t* out_first);
 /* entity_add_force: applies to every frame of the next rp_simulate call and is then cleared, as the
  * reference's callers clear forces after every frame (src/examples/stack.cpp:100-102). */
 rp_status rp_entity_add_force(rp_world* w, int32_t entity, const double position[3], const double force[3],
@@ -188,7 +207,9 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
  * [9] EPA calls that hit the 100-iteration cap, [10] largest narrowphase cost of one pair
  * (SM clock cycles), [11] narrowphase cycles summed over pairs, [12] pairs narrowphased,
  * [13] pairs skipped because their bounding box and sphere are certainly apart, [14] GJK cycles,
- * [15] EPA cycles, [16] contact-manifold cycles (summed over calls), [17..19] reserved (0). */
+ * [15] EPA cycles, [16] contact-manifold cycles (summed over calls), [17] GJK cycles spent in
+ * support mapping, [18] GJK runs ended early on a repeated state (they would have reached the
+ * iteration cap and returned no collision), [19] reserved (0). */
 #define RP_NUM_COUNTERS 20
 rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */

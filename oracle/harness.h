@@ -86,6 +86,11 @@ uint32_t orc_contacts(int e1, int e2, double* out, uint32_t cap);
  * Returns 0 = no collision, 1 = collision and EPA converged, 2 = collision and EPA failed.
  * out = normal[3], penetration. */
 int      orc_gjk_epa(int e1, int e2, double* out);
+/* colliders_update on both entities, then clipping_get_contact_manifold (src/physics/clipping.cpp:
+ * 343-370) of their first colliders for a given normal (pointing from e1 to e2) and penetration:
+ * the manifold the reference builds once EPA has returned that normal. out: ORC_CONTACT_DOUBLES per
+ * contact; returns the count. */
+uint32_t orc_manifold(int e1, int e2, const double* normal, double penetration, double* out, uint32_t cap);
 
 #ifdef __cplusplus
 }

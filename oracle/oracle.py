@@ -71,6 +71,7 @@ class Oracle:
                 "orc_broad_pairs": (u, [P(u), u]),
                 "orc_contacts": (u, [i, i, P(d), u]),
                 "orc_gjk_epa": (i, [i, i, P(d)]),
+                "orc_manifold": (u, [i, i, P(d), d, P(d), u]),
                 "orc_hull_topology": (i, [i, i, i, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
                 "orc_hull_geometry": (i, [i, i, P(d), P(d), C.c_int32, C.c_int32, P(C.c_int32)]),
                 "orc_last_contacts": (u, [P(C.c_int32), P(d), u]),
@@ -208,3 +209,13 @@ class Oracle:
         out = np.zeros(4)
         r = self.lib.orc_gjk_epa(e1, e2, out.ctypes.data_as(C.POINTER(C.c_double)))
         return int(r), out
+
+    def manifold(self, e1: int, e2: int, normal, penetration: float) -> np.ndarray:
+        """clipping_get_contact_manifold of the two entities' first colliders for the given EPA
+        result (normal from e1 to e2, penetration)."""
+        cap = 256
+        n = np.ascontiguousarray(normal, dtype=np.float64)
+        out = np.zeros(cap * CONTACT_DOUBLES)
+        k = self.lib.orc_manifold(e1, e2, n.ctypes.data_as(C.POINTER(C.c_double)), float(penetration),
+                                  out.ctypes.data_as(C.POINTER(C.c_double)), cap)
+        return out[: min(k, cap) * CONTACT_DOUBLES].reshape(-1, CONTACT_DOUBLES)

@@ -1546,4 +1546,21 @@ int orc_gjk_epa(int e1, int e2, double* out) {
     return 1;
 }
 
+uint32_t orc_manifold(int e1, int e2, const double* normal, double penetration, double* out, uint32_t cap) {
+    body_colliders_update(&g_bodies[e1]);
+    body_colliders_update(&g_bodies[e2]);
+    cvec c = {0, 0, NULL};
+    v3 n = {normal[0], normal[1], normal[2]};
+    contact_manifold(&g_bodies[e1].col[0], &g_bodies[e2].col[0], n, penetration, &c);
+    for (int k = 0; k < c.n && (uint32_t)k < cap; ++k) {
+        double* o = out + (size_t)k * ORC_CONTACT_DOUBLES;
+        o[0] = c.a[k].p1.x; o[1] = c.a[k].p1.y; o[2] = c.a[k].p1.z;
+        o[3] = c.a[k].p2.x; o[4] = c.a[k].p2.y; o[5] = c.a[k].p2.z;
+        o[6] = c.a[k].n.x; o[7] = c.a[k].n.y; o[8] = c.a[k].n.z;
+    }
+    uint32_t cnt = (uint32_t)c.n;
+    free(c.a);
+    return cnt;
+}
+
 int orc_last_error(void) { return g_error; }

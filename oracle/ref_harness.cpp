@@ -17,6 +17,7 @@
 #include "physics/collider.h"
 #include "physics/gjk.h"
 #include "physics/epa.h"
+#include "physics/clipping.h"
 #include <vector>
 #include <string.h>
 #include "harness.h"
@@ -315,6 +316,28 @@ uint32_t orc_contacts(int e1, int e2, double* out, uint32_t cap) {
     }
     array_free(contacts);
     return n;
+}
+
+uint32_t orc_manifold(int e1, int e2, const double* normal, double penetration, double* out, uint32_t cap) {
+    Entity* a = ent(e1);
+    Entity* b = ent(e2);
+    colliders_update(a->colliders, a->world_position, &a->world_rotation);
+    colliders_update(b->colliders, b->world_position, &b->world_rotation);
+    Collider_Contact* contacts = array_new(Collider_Contact);
+    vec3 n;
+    n.x = normal[0];
+    n.y = normal[1];
+    n.z = normal[2];
+    clipping_get_contact_manifold(&a->colliders[0], &b->colliders[0], n, penetration, &contacts);
+    uint32_t cnt = (uint32_t)array_length(contacts);
+    for (uint32_t k = 0; k < cnt && k < cap; ++k) {
+        double* o = out + (size_t)k * ORC_CONTACT_DOUBLES;
+        o[0] = contacts[k].collision_point1.x; o[1] = contacts[k].collision_point1.y; o[2] = contacts[k].collision_point1.z;
+        o[3] = contacts[k].collision_point2.x; o[4] = contacts[k].collision_point2.y; o[5] = contacts[k].collision_point2.z;
+        o[6] = contacts[k].normal.x; o[7] = contacts[k].normal.y; o[8] = contacts[k].normal.z;
+    }
+    array_free(contacts);
+    return cnt;
 }
 
 int orc_gjk_epa(int e1, int e2, double* out) {

@@ -1,8 +1,10 @@
 """Build the GB300 extension in place: raw-physics_gb300/librawphys_gb300.so.
 
-Four translation units, compiled in parallel:
-  csrc/rp_kernels_f32.cu   FP32 build of the step kernels            (nvcc, sm_103a)
+Seven translation units, compiled in parallel:
+  csrc/rp_kernels_f32.cu   FP32 build of the persistent step kernels (nvcc, sm_103a)
   csrc/rp_kernels_f64.cu   all-FP64 build, no FMA contraction        (nvcc, sm_103a, -fmad=false)
+  csrc/rp_pipe_f32.cu      FP32 build of the phase-major kernels     (nvcc, sm_103a)
+  csrc/rp_pipe_f64.cu      all-FP64 phase-major kernels              (nvcc, sm_103a, -fmad=false)
   csrc/rp_host.cpp         runtime + C ABI (include/rp.h)            (host compiler)
   csrc/rp_hull.cpp         hull topology and mass properties        (host compiler)
   csrc/rp_shim.cpp         C++-mangled pbd_simulate drop-in          (host compiler)
@@ -38,6 +40,8 @@ def _units():
     return [
         ("rp_kernels_f32.cu", cu_common),
         ("rp_kernels_f64.cu", cu_common + ["-fmad=false"]),
+        ("rp_pipe_f32.cu", cu_common),
+        ("rp_pipe_f64.cu", cu_common + ["-fmad=false"]),
         ("rp_host.cpp", cxx),
         ("rp_hull.cpp", cxx),
         ("rp_shim.cpp", cxx),

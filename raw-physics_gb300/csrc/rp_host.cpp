@@ -111,12 +111,26 @@ struct rp_world {
     DevBuf d_pos, d_rot, d_ppos, d_prot, d_vel, d_omega, d_pvel, d_pomega, d_active, d_deact;
     DevBuf d_backup;
     DevBuf d_invm, d_I, d_Iinv, d_mat, d_radius, d_bound, d_fixed, d_col_start, d_force, d_torque;
-    DevBuf d_colliders, d_shapes, d_shape_verts, d_face_normal, d_face_elem_start, d_face_elem, d_csr_start, d_csr_data;
+    DevBuf d_colliders, d_shapes, d_shape_verts, d_face_normal, d_shape_verts_f, d_face_normal_f, d_face_elem_start, d_face_elem, d_csr_start, d_csr_data;
     DevBuf d_tverts, d_tnorms, d_ext;
     DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
         d_counters, d_phase, d_kat_out, d_kat_count;
+
+    // phase-major pipeline
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
+    int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
+    bool pipe_ready = false;
+    PipeConfig pipe;
+    PipeDims dims;
+    uint64_t layout_gen = 0;          // bumped whenever device buffers are (re)allocated
+    cudaGraphExec_t graph = nullptr;  // one captured frame of the pipeline
+    uint64_t graph_gen = ~0ull;
+    StepParams graph_params = {};
+    std::vector<cudaEvent_t> marks;   // phase events of a timed frame
+    std::vector<int> mark_phase;
+    double phase_ms[PHASES] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 
     uint64_t launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
@@ -212,8 +226,8 @@ rp_status build_device(rp_world* w) {
         long long n = w->scene_body[(size_t)s + 1] - w->scene_body[(size_t)s];
         max_bodies = std::max(max_bodies, (int)n);
         long long all = n * (n - 1) / 2;
-        long long pc = std::min(all, std::max(1LL, (long long)(std::max(1024.0, 48.0 * (double)n) * w->pair_mult * scale)));
-        long long cc = std::max(1LL, (long long)(std::max(256.0, 8.0 * (double)pc) * w->contact_mult * scale));
+        long long pc = std::min(all, std::max(1LL, (long long)(std::max(256.0, 16.0 * (double)n) * w->pair_mult * scale)));
+        long long cc = std::max(1LL, (long long)(std::max(256.0, 2.0 * (double)pc) * w->contact_mult * scale));
         if (pc > (1LL << 30) || cc > (1LL << 30)) return fail(RP_ERR_CAPACITY, "scratch sizes beyond 2^30 entries");
         w->scene_pair_cap[(size_t)s + 1] = w->scene_pair_cap[(size_t)s] + (int32_t)pc;
         w->scene_contact_cap[(size_t)s + 1] = w->scene_contact_cap[(size_t)s] + (int32_t)cc;
@@ -350,6 +364,11 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(upload(w->d_shapes, shapes, st));
     RP_CUDA(upload(w->d_shape_verts, sverts, st));
     RP_CUDA(upload(w->d_face_normal, snorm, st));
+    {
+        std::vector<float> fv(sverts.begin(), sverts.end()), fn(snorm.begin(), snorm.end());
+        RP_CUDA(upload(w->d_shape_verts_f, fv, st));
+        RP_CUDA(upload(w->d_face_normal_f, fn, st));
+    }
     RP_CUDA(upload(w->d_face_elem_start, fstart, st));
     RP_CUDA(upload(w->d_face_elem, felem, st));
     RP_CUDA(upload(w->d_csr_start, cstart, st));
@@ -396,6 +415,39 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(w->d_work.ensure((size_t)S * 4));
     RP_CUDA(w->d_contacts.ensure(std::max<size_t>(C, 1) * 12 * R));
     RP_CUDA(w->d_ext_lambda.ensure(std::max<size_t>(E, 1) * 4 * 8));
+    {   // phase-major pipeline: body -> scene, collider -> body, per-pair narrowphase hand-off
+        std::vector<int32_t> body_scene(std::max<size_t>(N, 1), 0), col_body(std::max<size_t>(cols.size(), 1), 0);
+        for (int sc = 0; sc < S; ++sc)
+            for (int32_t b = w->scene_body[(size_t)sc]; b < w->scene_body[(size_t)sc + 1]; ++b) body_scene[(size_t)b] = sc;
+        for (size_t slot = 0; slot < N; ++slot)
+            for (int32_t c = col_start[slot]; c < col_start[slot + 1]; ++c) col_body[(size_t)c] = (int32_t)slot;
+        RP_CUDA(upload(w->d_body_scene, body_scene, st));
+        RP_CUDA(upload(w->d_col_body, col_body, st));
+        RP_CUDA(w->d_pose_f.ensure(std::max<size_t>(N, 1) * 32));
+        RP_CUDA(w->d_work_list.ensure(std::max<size_t>(P, 1) * 4));
+        RP_CUDA(w->d_work_state.ensure(std::max<size_t>(P, 1) * 4));
+        RP_CUDA(w->d_gjk_list.ensure(std::max<size_t>(P, 1) * 4));
+        RP_CUDA(w->d_hit_list.ensure(std::max<size_t>(P, 1) * 4));
+        RP_CUDA(w->d_work_simplex.ensure(std::max<size_t>(P, 1) * 16 * R));
+        RP_CUDA(w->d_work_epa.ensure(std::max<size_t>(P, 1) * 4 * 8));
+        std::vector<int32_t> order((size_t)S);
+        for (int sc = 0; sc < S; ++sc) order[(size_t)sc] = sc;
+        // largest estimated sweep cost first: bodies, plus joints weighted for their serial chains
+        auto cost = [&](int32_t x) {
+            return (long long)(w->scene_body[(size_t)x + 1] - w->scene_body[(size_t)x]) +
+                   8LL * (w->scene_ext[(size_t)x + 1] - w->scene_ext[(size_t)x]);
+        };
+        std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+        RP_CUDA(upload(w->d_scene_order, order, st));
+        RP_CUDA(w->d_queue.ensure(16));
+        RP_CUDA(cudaMemsetAsync(w->d_queue.p, 0, 16, st));
+        w->dims.nbodies = (int)N;
+        w->dims.ncolliders = (int)cols.size();
+        w->dims.next = (int)E;
+        w->dims.num_scenes = S;
+        w->dims.grid_mode = w->grid_mode ? 1 : 0;
+        w->layout_gen++;
+    }
     if (!w->d_status.p) {
         RP_CUDA(w->d_barrier.ensure(64));
         RP_CUDA(cudaMemsetAsync(w->d_barrier.p, 0, 64, st));
@@ -449,6 +501,8 @@ WorldView<R> make_view(rp_world* w) {
     V.shapes = w->d_shapes.as<Shape>();
     V.shape_verts = w->d_shape_verts.as<double>();
     V.face_normal = w->d_face_normal.as<double>();
+    V.shape_verts_f = w->d_shape_verts_f.as<float>();
+    V.face_normal_f = w->d_face_normal_f.as<float>();
     V.face_elem_start = w->d_face_elem_start.as<int32_t>();
     V.face_elem = w->d_face_elem.as<int32_t>();
     V.csr_start = w->d_csr_start.as<int32_t>();
@@ -484,6 +538,17 @@ WorldView<R> make_view(rp_world* w) {
     V.barrier = w->d_barrier.as<unsigned int>();
     V.counters = w->d_counters.as<unsigned long long>();
     V.phase_ns = w->d_phase.as<unsigned long long>();
+    V.body_scene = w->d_body_scene.as<int32_t>();
+    V.pose_f = w->d_pose_f.as<float4>();
+    V.col_body = w->d_col_body.as<int32_t>();
+    V.work_list = w->d_work_list.as<int32_t>();
+    V.work_state = w->d_work_state.as<int32_t>();
+    V.gjk_list = w->d_gjk_list.as<int32_t>();
+    V.hit_list = w->d_hit_list.as<int32_t>();
+    V.work_simplex = w->d_work_simplex.as<R>();
+    V.work_epa = w->d_work_epa.as<double>();
+    V.queue = w->d_queue.as<int32_t>();
+    V.scene_order = w->d_scene_order.as<int32_t>();
     return V;
 }
 
@@ -632,7 +697,82 @@ rp_status upload_forces(rp_world* w) {
     return RP_OK;
 }
 
+// The launch mode a frame uses: the persistent kernel (one launch per frame) or the phase-major
+// pipeline (one kernel per phase, replayed from a captured CUDA graph).
+bool use_pipeline(const rp_world* w) {
+    if (w->mode == RP_MODE_PERSISTENT) return false;
+    if (w->mode == RP_MODE_PHASED) return true;
+    const char* env = std::getenv("RP_MODE");
+    if (env && std::strcmp(env, "persistent") == 0) return false;
+    return true;
+}
+
+cudaError_t pipe_frame(rp_world* w, const StepParams& P, PipeMarks* marks) {
+    if (w->precision == RP_PRECISION_FP64) return pipe_frame_f64(make_view<double>(w), P, w->pipe, w->dims, w->stream, marks);
+    return pipe_frame_f32(make_view<float>(w), P, w->pipe, w->dims, w->stream, marks);
+}
+
+cudaError_t launch_pipeline(rp_world* w, const StepParams& P) {
+    cudaError_t e;
+    if (!w->pipe_ready) {
+        e = w->precision == RP_PRECISION_FP64 ? pipe_configure_f64(w->pipe, w->num_sms) : pipe_configure_f32(w->pipe, w->num_sms);
+        if (e != cudaSuccess) return e;
+        w->pipe_ready = true;
+    }
+    w->launches += (uint64_t)(w->precision == RP_PRECISION_FP64 ? pipe_launches_f64(P) : pipe_launches_f32(P));
+    if (!w->timing && w->stream == nullptr) {
+        // the legacy default stream cannot be captured: launch the frame's kernels directly
+        return pipe_frame(w, P, nullptr);
+    }
+    if (w->timing) {
+        // a timed frame runs without the graph, with an event after every phase
+        const int cap = 2 + P.num_substeps * 8;
+        while ((int)w->marks.size() < cap) {
+            cudaEvent_t ev;
+            e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return e;
+            w->marks.push_back(ev);
+        }
+        w->mark_phase.assign((size_t)cap, 0);
+        PipeMarks m;
+        m.ev = w->marks.data();
+        m.phase = w->mark_phase.data();
+        m.cap = cap;
+        e = pipe_frame(w, P, &m);
+        if (e != cudaSuccess) return e;
+        e = cudaEventSynchronize(w->marks[(size_t)m.n - 1]);
+        if (e != cudaSuccess) return e;
+        for (int i = 1; i < m.n; ++i) {
+            float ms = 0.f;
+            e = cudaEventElapsedTime(&ms, w->marks[(size_t)i - 1], w->marks[(size_t)i]);
+            if (e != cudaSuccess) return e;
+            const int ph = m.phase[i];
+            if (ph >= 0 && ph < PHASES) w->phase_ms[ph] += ms;
+        }
+        return cudaSuccess;
+    }
+    const StepParams& G = w->graph_params;
+    if (!w->graph || w->graph_gen != w->layout_gen || G.dt != P.dt || G.num_substeps != P.num_substeps ||
+        G.num_pos_iters != P.num_pos_iters || G.enable_collisions != P.enable_collisions) {
+        if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t le = pipe_frame(w, P, nullptr);
+        e = cudaStreamEndCapture(w->stream, &g);
+        if (le != cudaSuccess) { if (g) cudaGraphDestroy(g); return le; }
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&w->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { w->graph = nullptr; return e; }
+        w->graph_gen = w->layout_gen;
+        w->graph_params = P;
+    }
+    return cudaGraphLaunch(w->graph, w->stream);
+}
+
 cudaError_t launch_step(rp_world* w, const StepParams& P) {
+    if (use_pipeline(w)) return launch_pipeline(w, P);
     cudaError_t e;
     if (w->precision == RP_PRECISION_FP64) e = step_f64(make_view<double>(w), P, w->grid_mode, w->grid_mode ? w->grid_blocks : w->num_scenes, w->stream);
     else e = step_f32(make_view<float>(w), P, w->grid_mode, w->grid_mode ? w->grid_blocks : w->num_scenes, w->stream);
@@ -721,6 +861,8 @@ void rp_world_destroy(rp_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     if (w->ev0) cudaEventDestroy(w->ev0);
     if (w->ev1) cudaEventDestroy(w->ev1);
+    if (w->graph) cudaGraphExecDestroy(w->graph);
+    for (cudaEvent_t ev : w->marks) cudaEventDestroy(ev);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
     delete w;
 }
@@ -883,6 +1025,39 @@ rp_status rp_entity_create(rp_world* w, int32_t scene, const double p[3], const 
     w->bodies.push_back(b);
     w->static_dirty = true;
     *out = (int32_t)w->bodies.size() - 1;
+    return RP_OK;
+}
+
+rp_status rp_entities_create(rp_world* w, uint32_t n, const int32_t* scene, const double* pos, const double* rot,
+                             const double* mass, const int32_t* fixed, const rp_collider_desc* cols, const double* mus,
+                             const double* mud, const double* rest, const double* vel, const double* omega,
+                             int32_t* out_first) {
+    if (check_world(w) || !out_first || (n && (!scene || !pos || !rot || !mass || !fixed || !cols || !mus || !mud || !rest)))
+        return fail(RP_ERR_INVALID, "null argument");
+    *out_first = (int32_t)w->bodies.size();
+    if (w->device_state_valid) {
+        rp_status s = sync_state_to_host(w);
+        if (s != RP_OK) return s;
+        w->device_state_valid = false;
+    }
+    const size_t first = w->bodies.size();
+    w->bodies.reserve(first + n);
+    static const double zero[3] = {0.0, 0.0, 0.0};
+    for (uint32_t i = 0; i < n; ++i) {
+        int32_t e = 0;
+        rp_status s = rp_entity_create(w, scene[i], pos + 3 * (size_t)i, rot + 4 * (size_t)i, mass[i], fixed[i], cols + i, 1,
+                                       mus[i], mud[i], rest[i], &e);
+        if (s == RP_OK && (vel || omega)) {
+            HostBody& b = w->bodies[(size_t)e];
+            const double* v = vel ? vel + 3 * (size_t)i : zero;
+            const double* om = omega ? omega + 3 * (size_t)i : zero;
+            for (int k = 0; k < 3; ++k) { b.v[k] = v[k]; b.w[k] = om[k]; }
+        }
+        if (s != RP_OK) {
+            w->bodies.resize(first);   // all or nothing
+            return s;
+        }
+    }
     return RP_OK;
 }
 
@@ -1277,7 +1452,7 @@ rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]) {
         out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
         out[5] = c[3]; out[6] = c[5]; out[7] = c[6];
         out[8] = c[4]; out[9] = c[7]; out[10] = c[8]; out[11] = c[9]; out[12] = c[10]; out[13] = c[11];
-        out[14] = c[12]; out[15] = c[13]; out[16] = c[14];
+        out[14] = c[12]; out[15] = c[13]; out[16] = c[14]; out[17] = c[15]; out[18] = c[16];
     }
     out[3] = w->steps;
     out[4] = w->substeps;
@@ -1289,11 +1464,12 @@ uint64_t rp_kernel_launches(const rp_world* w) { return w ? w->launches : 0; }
 rp_status rp_phase_times(rp_world* w, double out[9]) {
     if (check_world(w) || !out) return RP_ERR_INVALID;
     for (int k = 0; k < PHASES; ++k) out[k] = 0.0;
+    for (int k = 0; k < PHASES; ++k) out[k] = w->phase_ms[k];
     if (!w->d_phase.p) return RP_OK;
     unsigned long long ns[PHASES];
     RP_CUDA(cudaMemcpyAsync(ns, w->d_phase.p, sizeof(ns), cudaMemcpyDeviceToHost, w->stream));
     RP_CUDA(cudaStreamSynchronize(w->stream));
-    for (int k = 0; k < PHASES; ++k) out[k] = (double)ns[k] * 1e-6;
+    for (int k = 0; k < PHASES; ++k) out[k] += (double)ns[k] * 1e-6;
     return RP_OK;
 }
 
@@ -1307,6 +1483,13 @@ rp_status rp_transfer_bytes(rp_world* w, uint64_t out[2]) {
 rp_status rp_set_timing(rp_world* w, int32_t enabled) {
     if (check_world(w)) return RP_ERR_INVALID;
     w->timing = enabled != 0;
+    return RP_OK;
+}
+
+rp_status rp_world_set_mode(rp_world* w, int32_t mode) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (mode != RP_MODE_AUTO && mode != RP_MODE_PERSISTENT && mode != RP_MODE_PHASED) return fail(RP_ERR_INVALID, "bad mode");
+    w->mode = mode;
     return RP_OK;
 }
 

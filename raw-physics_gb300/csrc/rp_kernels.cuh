@@ -26,32 +26,7 @@ __global__ void __launch_bounds__(32) contacts_kernel(WorldView<R> W, int a, int
         int body = side ? b : a;
         for (int ci = W.col_start[body]; ci < W.col_start[body + 1]; ++ci) {
             const Collider col = W.colliders[ci];
-            if (col.type != COL_HULL) continue;
-            const Shape sh = W.shapes[col.shape];
-            double4_32a p4 = W.pos[body], q4 = W.rot[body];
-            V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
-            V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
-            if (EXACT) {
-                M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
-                for (int i = lane; i < sh.nv; i += 32) {
-                    const double* v = W.shape_verts + 3 * (sh.vert_off + i);
-                    tv[i] = v3cast<R>(m4_point(M, v3<double>(v[0], v[1], v[2])));
-                }
-                for (int i = lane; i < sh.nf; i += 32) {
-                    const double* nrm = W.face_normal + 3 * (sh.face_off + i);
-                    tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
-                }
-            } else {
-                M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
-                for (int i = lane; i < sh.nv; i += 32) {
-                    const double* v = W.shape_verts + 3 * (sh.vert_off + i);
-                    tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
-                }
-                for (int i = lane; i < sh.nf; i += 32) {
-                    const double* nrm = W.face_normal + 3 * (sh.face_off + i);
-                    tn[i] = vnorm(mmulv(Rm, v3<R>((R)nrm[0], (R)nrm[1], (R)nrm[2])));
-                }
-            }
+            if (col.type == COL_HULL) transform_collider<R, EXACT>(W, col, body, lane);
         }
     }
     __syncwarp();

@@ -38,6 +38,22 @@ template <typename T> RP_HD V3<T> vnorm(V3<T> v) {
     return v3<T>(v.x / l, v.y / l, v.z / l);
 }
 template <typename T> RP_HD V3<T> vinv(V3<T> v) { return vsub(v3<T>(0, 0, 0), v); }
+#ifdef __CUDACC__
+// FP64 unit vector without FP64 square root or division (GB300 issues FP64 at 1/64 of the FP32
+// rate): an FP32 reciprocal-square-root seed refined by two Newton-Raphson steps,
+// r <- r (3 - d r^2) / 2, which reach full FP64 precision from the seed's ~23 bits. Lengths outside
+// the FP32 exponent range take the exact path. For the FP32 build's FP64 decisions; the exact build
+// keeps vnorm (the reference's sqrt and divisions).
+__device__ __forceinline__ V3<double> vnorm_fast(V3<double> v) {
+    const double d = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (!(d > 0.0)) return v3<double>(0, 0, 0);
+    if (d < 1e-30 || d > 1e30) return vnorm(v);
+    double r = (double)rsqrtf((float)d);
+    r = r * (1.5 - 0.5 * d * r * r);
+    r = r * (1.5 - 0.5 * d * r * r);
+    return v3<double>(v.x * r, v.y * r, v.z * r);
+}
+#endif
 template <typename T> RP_HD bool veq(V3<T> a, V3<T> b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
 template <typename T> RP_HD Qt<T> qt(T x, T y, T z, T w) { Qt<T> q; q.x = x; q.y = y; q.z = z; q.w = w; return q; }

@@ -53,6 +53,7 @@ struct NarrowSmem {
     V3<R> c_r1[CMAX];   // contacts of the pair (constraint-ready local offsets)
     V3<R> c_r2[CMAX];
     V3<R> c_n[CMAX];
+    R gjk_saved[16];    // GJK state kept for cycle detection (simplex, size, direction)
     int ncontacts;
     int nf, ne, npoly;
     int status;
@@ -112,7 +113,7 @@ struct ColView {
 template <typename R>
 __device__ __forceinline__ V3<double> face_normal64(const WorldView<R>& W, const ColView<R>& c, int f) {
     const double* n = W.face_normal + 3 * (c.shape->face_off + f);
-    return vnorm(mmulv(qmat3(c.q64), v3<double>(n[0], n[1], n[2])));
+    return vnorm_fast(mmulv(qmat3(c.q64), v3<double>(n[0], n[1], n[2])));
 }
 
 template <typename R>
@@ -142,11 +143,33 @@ __device__ V3<R> support_point(const ColView<R>& c, V3<R> d) {
     return vadd(c.center, vscale(c.radius, vnorm(d)));
 }
 
+// support_point_of_minkowski_difference (support.cpp:29-39): both hulls' argmax reductions run
+// interleaved, so each shuffle round waits for one shuffle latency instead of two.
 template <typename R>
 __device__ __forceinline__ V3<R> support_mink(const ColView<R>& a, const ColView<R>& b, V3<R> d) {
-    V3<R> s1 = support_point(a, d);
-    V3<R> s2 = support_point(b, vscale((R)-1.0, d));
-    return vsub(s1, s2);
+    const V3<R> nd = vscale((R)-1.0, d);
+    if (a.type != COL_HULL || b.type != COL_HULL) return vsub(support_point(a, d), support_point(b, nd));
+    const R lowest = sizeof(R) == 4 ? (R)-FLT_MAX : (R)-DBL_MAX;
+    R ba = lowest, bb = lowest;
+    int ia = 0x7fffffff, ib = 0x7fffffff;
+    for (int i = (int)lane_id(); i < a.nv; i += WARP) {
+        R dot = vdot(cv_vertex(a, i), d);
+        if (dot > ba) { ba = dot; ia = i; }
+    }
+    for (int i = (int)lane_id(); i < b.nv; i += WARP) {
+        R dot = vdot(cv_vertex(b, i), nd);
+        if (dot > bb) { bb = dot; ib = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        R ova = __shfl_xor_sync(0xffffffffu, ba, o), ovb = __shfl_xor_sync(0xffffffffu, bb, o);
+        int oia = __shfl_xor_sync(0xffffffffu, ia, o), oib = __shfl_xor_sync(0xffffffffu, ib, o);
+        if (ova > ba || (ova == ba && oia < ia)) { ba = ova; ia = oia; }
+        if (ovb > bb || (ovb == bb && oib < ib)) { bb = ovb; ib = oib; }
+    }
+    if (ia == 0x7fffffff) ia = 0;
+    if (ib == 0x7fffffff) ib = 0;
+    return vsub(cv_vertex(a, ia), cv_vertex(b, ib));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -248,21 +271,61 @@ __device__ bool do_simplex(Simplex<R>& s, V3<R>& dir) {
     return false;
 }
 
+// Component k (0..15) of the GJK iteration state: simplex points a, b, c, d, the simplex size and
+// the search direction. All lanes hold the same state.
 template <typename R>
-__device__ bool gjk_collides(const ColView<R>& c1, const ColView<R>& c2, Simplex<R>& s, int& iters) {
+__device__ __forceinline__ R gjk_state(const Simplex<R>& s, V3<R> dir, int k) {
+    R v[16] = {s.a.x, s.a.y, s.a.z, s.b.x, s.b.y, s.b.z, s.c.x, s.c.y, s.c.z, s.d.x, s.d.y, s.d.z,
+               (R)s.num, dir.x, dir.y, dir.z};
+    R r = v[0];
+#pragma unroll
+    for (int i = 1; i < 16; ++i) r = (k == i) ? v[i] : r;
+    return r;
+}
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+
+// gjk_collides (gjk.cpp:350-379): at most 100 iterations, false when they run out.
+// One iteration is a pure function of the state (simplex, size, direction), so once a state
+// repeats bit for bit the run is periodic: it can neither find the origin nor separate any more
+// and would end false at the iteration cap. Brent's cycle detection (one saved state, saved
+// again at power-of-two distances, kept in `saved`, 16 values in shared memory) stops such runs
+// early with the same result; the iteration count returned is then below 100 and `cycled` is set.
+template <typename R>
+__device__ bool gjk_collides(const ColView<R>& c1, const ColView<R>& c2, Simplex<R>& s, int& iters,
+                             long long& support_cycles, R* saved, bool& cycled) {
+    const int lane = (int)lane_id();
+    long long t0 = clock64();
     s.a = support_mink(c1, c2, v3<R>(0, 0, 1));
     s.b = s.c = s.d = v3<R>(0, 0, 0);
     s.num = 1;
     V3<R> dir = vscale((R)-1.0, s.a);
+    cycled = false;
+    int power = 1, lam = 0;
     for (int i = 0; i < 100; ++i) {
         iters = i + 1;
         V3<R> p = support_mink(c1, c2, dir);
+        support_cycles += clock64() - t0;
         if (vdot(p, dir) < (R)0) return false;
         if (s.num == 1) { s.b = s.a; s.a = p; }
         else if (s.num == 2) { s.c = s.b; s.b = s.a; s.a = p; }
         else { s.d = s.c; s.c = s.b; s.b = s.a; s.a = p; }
         s.num++;
         if (do_simplex(s, dir)) return true;
+        if (i >= 8) {
+            const R mine = gjk_state(s, dir, lane & 15);
+            if (i > 8) {
+                const bool eq = same_bits(saved[lane & 15], mine);
+                if (__all_sync(0xffffffffu, eq)) { cycled = true; return false; }
+            }
+            if (i == 8 || ++lam == power) {
+                __syncwarp();
+                if (lane < 16) saved[lane] = mine;
+                __syncwarp();
+                if (i > 8) { power <<= 1; lam = 0; }
+            }
+        }
+        t0 = clock64();
     }
     return false;
 }
@@ -533,15 +596,34 @@ __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView
         iters = it + 1;
         V3<float> min_n = mi == 0x7fffffff ? v3<float>(0.f, 0.f, 0.f) : sm.fn[mi];
         V3<float> sp = v3cast<float>(support_mink(c1, c2, v3cast<R>(min_n)));
-        double d = (double)min_n.x * sp.x + (double)min_n.y * sp.y + (double)min_n.z * sp.z;
-        if (fabs(d - (double)min_d) < 0.0001) {
-            // the closest face in FP64 (face normal and depth from its three Minkowski points)
+        // Termination test (epa.cpp:153-160) with the FP64 outcome: |<n, s> - d| < 1e-4 for the
+        // closest face. FP32 decides it when the FP32 gap is farther from 1e-4 than its error bound
+        // (the face normal's error grows with the face's conditioning |e1||e2| / |e1 x e2|);
+        // otherwise the face is re-evaluated in FP64. The returned normal and depth are FP64.
+        bool done = false, need64 = true;
+        if (mi != 0x7fffffff) {
+            uchar4 f = sm.f[mi];
+            V3<float> a = sm.poly[f.x], e1 = vsub(sm.poly[f.y], a), e2 = vsub(sm.poly[f.z], a);
+            const float cr = vlen(vcross(e1, e2));
+            const float cond = cr > 0.f ? vlen(e1) * vlen(e2) / cr : FLT_MAX;
+            const float gap = fabsf(vdot(min_n, sp) - min_d);
+            const float err = 1e-6f * (1.f + cond) * (vlen(sp) + vlen(a) + 1e-3f) + 1e-7f;
+            if (cond < 1e6f && gap < 0.0001f - err) { done = true; need64 = false; }
+            else if (cond < 1e6f && gap > 0.0001f + err) { need64 = false; }
+        }
+        V3<double> n64 = v3<double>(0, 0, 0);
+        double d64 = 0.0;
+        if (mi != 0x7fffffff && (need64 || done)) {
             uchar4 f = sm.f[mi];
             V3<double> a = v3cast<double>(sm.poly[f.x]), b = v3cast<double>(sm.poly[f.y]), c = v3cast<double>(sm.poly[f.z]);
-            V3<double> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
-            if (vdot(n, v3cast<double>(min_n)) < 0.0) n = vinv(n);
-            out_n = n;
-            out_pen = vdot(n, a);
+            n64 = vnorm_fast(vcross(vsub(b, a), vsub(c, a)));
+            if (vdot(n64, v3cast<double>(min_n)) < 0.0) n64 = vinv(n64);
+            d64 = vdot(n64, a);
+        }
+        if (need64) done = fabs(vdot(n64, v3cast<double>(sp)) - d64) < 0.0001;
+        if (done) {
+            out_n = n64;
+            out_pen = d64;
             if (st && lane == 0) atomicOr(&smr.status, st);
             return true;
         }
@@ -822,10 +904,11 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         return;
     }
     bool ref1 = d1 > d2;
-    if (!EXACT) {
+    if (!EXACT && fabs((double)d1 - (double)d2) < 1e-5) {
         // The reference face is the better-aligned of the two candidates (clipping.cpp:284). For
         // nearly parallel faces d1 and d2 differ by ~1e-11, below FP32 resolution; decide it from
         // FP64 normals so the FP32 build picks the reference's face (and so its contact order).
+        // Outside 1e-5 (FP32 error of these unit-vector dot products: ~3e-7) FP32 decides the same.
         V3<double> m1 = face_normal64(W, h1, f1), m2 = face_normal64(W, h2, f2);
         ref1 = vdot(m1, normal64) > vdot(m2, vinv(normal64));
     }
@@ -903,11 +986,12 @@ __device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const
     }
 }
 
-// EPA of the FP32 build: false runs the FP64 face-normal / termination EPA on the FP32 polytope
-// (follows the reference's expansion path wherever its decisions are not FP32-rounding ties);
-// true runs the all-FP32 EPA with a final FP64 re-evaluation of the chosen face.
+// EPA of the FP32 build. 1 (default): polytope faces and the closest-face search in FP32, the
+// termination test and the returned normal and depth in FP64 (the closest face re-evaluated from its
+// three Minkowski points every iteration). 0: every face normal and distance in FP64, which on GB300
+// (FP64 at 1/64 of the FP32 rate) made EPA the most expensive part of the batched narrowphase.
 #ifndef RP_EPA_FAST
-#define RP_EPA_FAST 0
+#define RP_EPA_FAST 1
 #endif
 constexpr bool kEpaFast = RP_EPA_FAST != 0;
 
@@ -929,11 +1013,15 @@ __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, cons
     Simplex<R> s;
     int gi = 0, ei = 0;
     const long long t0 = clock64();
-    bool hit = gjk_collides(c1, c2, s, gi);
+    long long tsup = 0;
+    bool cycled = false;
+    bool hit = gjk_collides(c1, c2, s, gi, tsup, sm.gjk_saved, cycled);
     const long long t1 = clock64();
     if (counters && lane_id() == 0) {
         atomicAdd(&counters[0], (unsigned long long)gi);
         atomicAdd(&counters[12], (unsigned long long)(t1 - t0));
+        atomicAdd(&counters[15], (unsigned long long)tsup);
+        if (cycled) atomicAdd(&counters[16], 1ull);
         if (gi >= 100) atomicAdd(&counters[4], 1ull);
     }
     if (!hit) return;

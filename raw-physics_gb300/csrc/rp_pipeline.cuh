@@ -1,0 +1,566 @@
+// Phase-major form of the step: one kernel per phase over every scene of the batch.
+//
+// The persistent step kernels (rp_step.cuh) run a whole frame inside one launch, so every SM
+// interleaves all phases' code — broad phase, schedule, GJK, EPA, clipping, solves — and the
+// instruction working set (~0.8 MB) thrashes the instruction caches. Here each phase is its own
+// small kernel, launched over the whole batch, and a frame is the fixed sequence
+//
+//   setup (per scene: broad phase, islands, schedule, work-list reservation)
+//   per substep: predict, hull transform, GJK, EPA, contact manifold, position sweep(s),
+//                velocity update, velocity sweep
+//
+// replayed from a CUDA graph. Every SM then runs one phase's code at a time, the narrowphase
+// kernels run at the occupancy their register and shared-memory needs allow, and the work is
+// spread over all SMs regardless of how it is split into scenes. Results are identical to the
+// persistent kernels: the same device functions run in the same order per scene.
+//
+// Narrowphase hand-off, per broad-phase pair of the frame's work list (work_state), through two
+// compacted lists rebuilt every substep:
+//   k_cull      thread per pair: liveness and bounds test; GJK candidates -> gjk_list, pairs needing
+//               the general path (compound bodies, sphere colliders) -> hit_list
+//   k_gjk       warp per GJK candidate: GJK on the two staged hulls; a hit stores its simplex and
+//               joins hit_list
+//   k_epa       warp per hit: EPA from the stored simplex; stores the FP64 normal and the penetration
+//   k_manifold  warp per hit_list entry: contact manifold (or the general path); writes contacts
+#pragma once
+#include "rp_step.cuh"
+#include "rp_launch.h"
+
+namespace rp {
+
+constexpr int PIPE_BLOCK = 256;
+constexpr int PIPE_WARPS = PIPE_BLOCK / 32;
+
+// Shared memory of one warp in k_gjk: the two staged hulls and the cycle-detection state.
+template <typename R>
+struct GjkSmem {
+    V3<R> va[STAGE_V];
+    V3<R> vb[STAGE_V];
+    R saved[16];
+};
+
+// Per-warp diagnostic totals, flushed with one atomic each when the warp finishes.
+struct WarpTally {
+    unsigned long long v[8];
+    __device__ WarpTally() {
+        for (int i = 0; i < 8; ++i) v[i] = 0;
+    }
+    __device__ void flush(unsigned long long* counters, const int* slots) {
+        if (lane_id() != 0 || !counters) return;
+        for (int i = 0; i < 8; ++i)
+            if (slots[i] >= 0 && v[i]) atomicAdd(&counters[slots[i]], v[i]);
+    }
+};
+
+// Views of a pair of single-hull bodies in the pair frame of pair_contacts (FP32 build: body a's
+// origin; exact build: world coordinates), staging both hulls' vertices in shared memory.
+template <typename R, bool EXACT>
+__device__ void single_views(const WorldView<R>& W, V3<R>* stage_a, V3<R>* stage_b, int a, int b, ColView<R>& va,
+                             ColView<R>& vb, PairFrame<R, EXACT>& fr) {
+    double4_32a pa = W.pos[a], pb = W.pos[b], qa4 = W.rot[a], qb4 = W.rot[b];
+    fr.raw = false;
+    V3<R> offa = v3<R>(0, 0, 0), offb;
+    if (EXACT) {
+        offb = v3<R>(0, 0, 0);
+        fr.x1 = v3<R>((R)pa.x, (R)pa.y, (R)pa.z);
+        fr.x2 = v3<R>((R)pb.x, (R)pb.y, (R)pb.z);
+    } else {
+        offb = v3<R>((R)(pb.x - pa.x), (R)(pb.y - pa.y), (R)(pb.z - pa.z));
+        fr.x1 = offa;
+        fr.x2 = offb;
+    }
+    fr.q1inv = qinverse(qt<R>((R)qa4.x, (R)qa4.y, (R)qa4.z, (R)qa4.w));
+    fr.q2inv = qinverse(qt<R>((R)qb4.x, (R)qb4.y, (R)qb4.z, (R)qb4.w));
+    va = make_view<R, EXACT>(W, W.col_start[a], EXACT ? fr.x1 : offa, offa, stage_a, qt<double>(qa4.x, qa4.y, qa4.z, qa4.w));
+    vb = make_view<R, EXACT>(W, W.col_start[b], EXACT ? fr.x2 : offb, offb, stage_b, qt<double>(qb4.x, qb4.y, qb4.z, qb4.w));
+}
+
+// True when both bodies have exactly one collider, a hull whose vertices fit the staging area.
+template <typename R>
+__device__ __forceinline__ bool single_hulls(const WorldView<R>& W, int a, int b) {
+    const int ca = W.col_start[a], cb = W.col_start[b];
+    if (W.col_start[a + 1] - ca != 1 || W.col_start[b + 1] - cb != 1) return false;
+    const Collider A = W.colliders[ca], B = W.colliders[cb];
+    if (A.type != COL_HULL || B.type != COL_HULL) return false;
+    return W.shapes[A.shape].nv <= STAGE_V && W.shapes[B.shape].nv <= STAGE_V;
+}
+
+// Copies the warp's contacts of global pair slot gp into the scene's contact buffer.
+template <typename R>
+__device__ void emit_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int s, int gp, unsigned long long& tally) {
+    const int lane = (int)lane_id();
+    const int cbase = W.scene_contact_cap[s];
+    const int ccap = W.scene_contact_cap[s + 1] - cbase;
+    int nc = sm.ncontacts, start = 0;
+    if (lane == 0) {
+        start = nc ? atomicAdd(&W.contact_count[s], nc) : 0;
+        if (start + nc > ccap) {
+            atomicOr(&W.status[s], (uint32_t)ST_CONTACT_OVERFLOW);
+            nc = 0;
+        }
+        if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+        tally += (unsigned long long)nc;
+        W.pair_cstart[gp] = start;
+        W.pair_ccount[gp] = nc;
+    }
+    start = __shfl_sync(0xffffffffu, start, 0);
+    nc = __shfl_sync(0xffffffffu, nc, 0);
+    for (int k = lane; k < nc; k += 32) {
+        R* c = W.contacts + 12 * (size_t)(cbase + start + k);
+        V3<R> r1 = sm.c_r1[k], r2 = sm.c_r2[k], n = sm.c_n[k];
+        c[0] = r1.x; c[1] = r1.y; c[2] = r1.z; c[3] = 0;
+        c[4] = r2.x; c[5] = r2.y; c[6] = r2.z; c[7] = 0;
+        c[8] = n.x; c[9] = n.y; c[10] = n.z; c[11] = 0;
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Frame setup: broad phase, islands, schedule, then the frame's narrowphase work list.
+template <typename R, class G>
+__device__ void setup_scene(const WorldView<R>& W, const G& g, int s, double dt, int* smem, int* base_smem) {
+    broad_phase(W, g, s, smem);
+    islands(W, g, s, dt);
+    schedule(W, g, s, smem);
+    const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+    if (threadIdx.x == 0 && g.block() == 0) *base_smem = np ? atomicAdd(&W.queue[0], np) : 0;
+    if (g.nblocks() == 1) {
+        __syncthreads();
+        const int base = *base_smem;
+        for (int p = g.rank(); p < np; p += g.size()) W.work_list[base + p] = W.scene_pair_cap[s] + p;
+    } else {
+        // one reservation per scene; block 0 publishes it through the scan scratch
+        if (threadIdx.x == 0 && g.block() == 0) W.scan_tmp[0] = *base_smem;
+        g.sync();
+        const int base = W.scan_tmp[0];
+        for (int p = g.rank(); p < np; p += g.size()) W.work_list[base + p] = W.scene_pair_cap[s] + p;
+        g.sync();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_setup_cta(WorldView<R> W, double dt) {
+    __shared__ int scan_smem[32];
+    __shared__ int base_smem;
+    CtaGroup g;
+    for (int s = blockIdx.x; s < W.num_scenes; s += gridDim.x) {
+        setup_scene(W, g, s, dt, scan_smem, &base_smem);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_setup_grid(WorldView<R> W, double dt) {
+    __shared__ int scan_smem[32];
+    __shared__ int base_smem;
+    GridGroup g;
+    g.bar = W.barrier;
+    g.status = W.status;
+    setup_scene(W, g, 0, dt, scan_smem, &base_smem);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Per-substep body phases
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbodies, int next, double h) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+    for (int b = t; b < nbodies; b += n) {
+        predict_body<R, EXACT>(W, b, h);
+        const double4_32a p = W.pos[b], q = W.rot[b];
+        W.pose_f[2 * b] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+        W.pose_f[2 * b + 1] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+    }
+    for (int e = t; e < next; e += n)
+        for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
+    for (int s = t; s < W.num_scenes; s += n) W.contact_count[s] = 0;
+    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; }
+}
+
+// Eight threads per collider: the typical hull has 8-64 vertices, so a whole warp per collider
+// would leave most lanes idle.
+constexpr int TRANSFORM_GROUP = 8;
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int ncolliders, int include_fixed) {
+    const int sub = threadIdx.x % TRANSFORM_GROUP;
+    const int gi = (blockIdx.x * blockDim.x + threadIdx.x) / TRANSFORM_GROUP;
+    const int ng = (gridDim.x * blockDim.x) / TRANSFORM_GROUP;
+    for (int ci = gi; ci < ncolliders; ci += ng) {
+        const Collider col = W.colliders[ci];
+        if (col.type != COL_HULL) continue;
+        const int b = W.col_body[ci];
+        if (W.fixed[b] && !include_fixed) continue;
+        transform_collider<R, EXACT>(W, col, b, sub, TRANSFORM_GROUP);
+    }
+}
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK) k_velocity(WorldView<R> W, int nbodies, double h) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+    for (int b = t; b < nbodies; b += n) velocity_body<R, EXACT>(W, b, h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Narrowphase kernels
+// Appends `item` (valid where `take`) to list[*count ...] with one atomic per CTA: a block-wide
+// scan of the flags, then thread 0 reserves the block's range. Every thread of the block calls it.
+__device__ __forceinline__ void block_append(int32_t* list, int32_t* count, bool take, int item, int* smem, int* base_smem) {
+    int total;
+    const int incl = block_incl_scan(take ? 1 : 0, smem, total);
+    if (threadIdx.x == 0) *base_smem = total ? atomicAdd(count, total) : 0;
+    __syncthreads();
+    if (take) list[*base_smem + incl - 1] = item;
+    __syncthreads();
+}
+
+// Thread per work item: liveness (pbd.cpp:583-590 skips pairs of two fixed or sleeping bodies), the
+// bounds test, and the split into the GJK list (pairs of two single hulls that may touch) and the
+// general path (compound bodies, sphere colliders), which goes straight to the contact list.
+template <typename R>
+__global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled) {
+    __shared__ int scan_smem[32];
+    __shared__ int base_smem;
+    const int n = W.queue[0];
+    unsigned long long apart = 0;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int k = base + (int)threadIdx.x;
+        int state = WS_NONE;
+        bool gjk = false;
+        if (k < n) {
+            const int gp = W.work_list[k];
+            const int2 pr = W.pairs[gp];
+            const int a = pr.x, b = pr.y;
+            const bool live = !((W.fixed[a] || !W.active[a]) && (W.fixed[b] || !W.active[b]));
+            if (live && enabled) {
+                if (!single_hulls(W, a, b)) state = WS_GENERAL;
+                else if (bounds_apart_f(W, a, b)) ++apart;
+                else gjk = true;
+            }
+            W.work_state[k] = state;
+            if (state == WS_NONE && !gjk) { W.pair_ccount[gp] = 0; W.pair_cstart[gp] = 0; }
+        }
+        block_append(W.gjk_list, &W.queue[2], gjk, k, scan_smem, &base_smem);
+        block_append(W.hit_list, &W.queue[3], state == WS_GENERAL, k, scan_smem, &base_smem);
+    }
+    for (int o = 16; o > 0; o >>= 1) apart += __shfl_xor_sync(0xffffffffu, apart, o);
+    if ((threadIdx.x & 31) == 0 && apart && W.counters) atomicAdd(&W.counters[11], apart);
+}
+
+// Warp per GJK candidate: GJK on the two staged hulls. A hit keeps its simplex and joins the
+// contact list; the list entries are gathered per warp and appended 32 at a time.
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK, 3) k_gjk(WorldView<R> W) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    GjkSmem<R>& sm = reinterpret_cast<GjkSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = W.queue[2];
+    WarpTally t;   // GJK iterations, cap hits, cycles, support cycles, cycle exits, -, GJK runs
+    int pending = 0, mine = 0;
+    for (int j = gw; j < n; j += nw) {
+        const int k = W.gjk_list[j];
+        const int gp = W.work_list[k];
+        const int2 pr = W.pairs[gp];
+        const int a = pr.x, b = pr.y;
+        ColView<R> va, vb;
+        PairFrame<R, EXACT> fr;
+        single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+        Simplex<R> sx;
+        int gi = 0;
+        long long tsup = 0;
+        bool cycled = false;
+        const long long t0 = clock64();
+        const bool hit = gjk_collides(va, vb, sx, gi, tsup, sm.saved, cycled);
+        t.v[0] += gi;
+        t.v[1] += gi >= 100;
+        t.v[2] += clock64() - t0;
+        t.v[3] += tsup;
+        t.v[4] += cycled;
+        t.v[6] += 1;
+        if (hit) {
+            R* out = W.work_simplex + 16 * (size_t)k;
+            const R comp[12] = {sx.a.x, sx.a.y, sx.a.z, sx.b.x, sx.b.y, sx.b.z,
+                                sx.c.x, sx.c.y, sx.c.z, sx.d.x, sx.d.y, sx.d.z};
+#pragma unroll
+            for (int i = 0; i < 12; ++i)
+                if (lane == i) out[i] = comp[i];
+            if (lane == pending) mine = k;
+            if (++pending == 32) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&W.queue[3], 32);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                W.hit_list[base + lane] = mine;
+                pending = 0;
+            }
+        }
+        if (lane == 0) {
+            W.work_state[k] = hit ? WS_HIT : WS_NONE;
+            if (!hit) { W.pair_ccount[gp] = 0; W.pair_cstart[gp] = 0; }
+        }
+        __syncwarp();
+    }
+    if (pending) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&W.queue[3], pending);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < pending) W.hit_list[base + lane] = mine;
+    }
+    const int slots[8] = {0, 4, 12, 15, 16, -1, 10, -1};
+    t.flush(W.counters, slots);
+}
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = W.queue[3];
+    WarpTally t;   // EPA iterations, EPA calls, EPA cycles, EPA cap hits
+    for (int j = gw; j < n; j += nw) {
+        const int k = W.hit_list[j];
+        if (W.work_state[k] != WS_HIT) continue;
+        {
+            const int gp = W.work_list[k];
+            const int2 pr = W.pairs[gp];
+            const int a = pr.x, b = pr.y;
+            if (lane == 0) { sm.status = 0; }
+            ColView<R> va, vb;
+            PairFrame<R, EXACT> fr;
+            single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+            const R* in = W.work_simplex + 16 * (size_t)k;
+            Simplex<R> sx;
+            sx.a = v3<R>(in[0], in[1], in[2]);
+            sx.b = v3<R>(in[3], in[4], in[5]);
+            sx.c = v3<R>(in[6], in[7], in[8]);
+            sx.d = v3<R>(in[9], in[10], in[11]);
+            sx.num = 4;
+            V3<double> nrm;
+            double pen = 0.0;
+            int ei = 0;
+            const long long t0 = clock64();
+            const bool ok = (EXACT || !kEpaFast) ? epa(sm, va, vb, sx, nrm, pen, ei) : epa_fast(sm, va, vb, sx, nrm, pen, ei);
+            t.v[0] += ei;
+            t.v[1] += 1;
+            t.v[2] += clock64() - t0;
+            t.v[3] += ei >= 100;
+            const int s = W.body_scene[a];
+            if (lane == 0) {
+                if (!ok) atomicOr(&W.status[s], (uint32_t)ST_EPA_NOT_CONVERGED);
+                if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+                if (ok) {
+                    double* o = W.work_epa + 4 * (size_t)k;
+                    o[0] = nrm.x; o[1] = nrm.y; o[2] = nrm.z; o[3] = pen;
+                    W.work_state[k] = WS_EPA_OK;
+                } else {
+                    W.work_state[k] = WS_NONE;
+                    W.pair_ccount[gp] = 0;
+                    W.pair_cstart[gp] = 0;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    const int slots[8] = {1, 2, 13, 7, -1, -1, -1, -1};
+    t.flush(W.counters, slots);
+}
+
+template <typename R, bool EXACT>
+__global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = W.queue[3];
+    WarpTally t;   // contacts, manifold cycles
+    for (int j = gw; j < n; j += nw) {
+        const int k = W.hit_list[j];
+        const int st = W.work_state[k];
+        if (st != WS_EPA_OK && st != WS_GENERAL) continue;
+        {
+            const int gp = W.work_list[k];
+            const int2 pr = W.pairs[gp];
+            const int a = pr.x, b = pr.y;
+            const int s = W.body_scene[a];
+            const long long t0 = clock64();
+            if (st == WS_GENERAL) {
+                pair_contacts<R, EXACT>(W, sm, a, b, false);
+            } else {
+                if (lane == 0) { sm.ncontacts = 0; sm.status = 0; }
+                __syncwarp();
+                ColView<R> va, vb;
+                PairFrame<R, EXACT> fr;
+                single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+                const double* e = W.work_epa + 4 * (size_t)k;
+                const V3<double> n64 = v3<double>(e[0], e[1], e[2]);
+                contact_manifold<R, EXACT>(sm, W, va, vb, v3cast<R>(n64), n64, (R)e[3], fr);
+            }
+            t.v[1] += clock64() - t0;
+            emit_contacts(W, sm, s, gp, t.v[0]);
+        }
+    }
+    const int slots[8] = {3, 14, -1, -1, -1, -1, -1, -1};
+    t.flush(W.counters, slots);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Gauss–Seidel sweeps: one CTA per scene, or the whole cooperative grid on one large scene.
+template <typename R, bool EXACT, bool VELOCITY>
+__global__ void __launch_bounds__(BLOCK) k_sweep_cta(WorldView<R> W, double h) {
+    CtaGroup g;
+    for (int s = blockIdx.x; s < W.num_scenes; s += gridDim.x) {
+        const int L = W.scene_levels[s];
+        const int* lstart = W.level_count + s * (W.max_levels + 1);
+        sweep_levels<R, EXACT, VELOCITY>(W, g, s, L, lstart, W.scene_node_cap[s], (R)h);
+        __syncthreads();
+    }
+}
+
+// One warp per scene: a scene's levels are mostly a few nodes wide, so a warp (barrier: __syncwarp)
+// sweeps them as fast as a CTA would while many more scenes are in flight per SM. Warps take scenes
+// from a counter (queue[1], zeroed before the launch) in decreasing-size order.
+constexpr int SWEEP_WARP_BLOCK = 128;
+
+template <typename R, bool EXACT, bool VELOCITY>
+__global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h) {
+    WarpGroup g;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&W.queue[1], 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= W.num_scenes) break;
+        const int s = W.scene_order[i];
+        const int L = W.scene_levels[s];
+        const int* lstart = W.level_count + s * (W.max_levels + 1);
+        sweep_levels<R, EXACT, VELOCITY>(W, g, s, L, lstart, W.scene_node_cap[s], (R)h);
+        __syncwarp();
+    }
+}
+
+template <typename R, bool EXACT, bool VELOCITY>
+__global__ void __launch_bounds__(BLOCK) k_sweep_grid(WorldView<R> W, double h) {
+    GridGroup g;
+    g.bar = W.barrier;
+    g.status = W.status;
+    const int L = W.scene_levels[0];
+    sweep_levels<R, EXACT, VELOCITY>(W, g, 0, L, W.level_count, W.scene_node_cap[0], (R)h);
+}
+
+}  // namespace rp
+
+namespace rp {
+
+// Host-side launch sequence of one frame of the phase-major form.
+template <typename R, bool EXACT>
+struct PipeLauncher {
+    static size_t gjk_smem() { return sizeof(GjkSmem<R>) * PIPE_WARPS; }
+    static size_t narrow_smem() { return sizeof(NarrowSmem<R>) * PIPE_WARPS; }
+
+    static cudaError_t configure(PipeConfig& c, int sms) {
+        cudaError_t e = cudaFuncSetAttribute(k_gjk<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gjk_smem());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_epa<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_manifold<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
+        if (e != cudaSuccess) return e;
+        int nb = 0;
+        auto occ = [&](const void* f, int block, size_t smem) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, block, smem) != cudaSuccess) b = 1;
+            return b < 1 ? 1 : b;
+        };
+        nb = occ((const void*)k_gjk<R, EXACT>, PIPE_BLOCK, gjk_smem());
+        c.gjk_blocks = nb * sms;
+        nb = occ((const void*)k_epa<R, EXACT>, PIPE_BLOCK, narrow_smem());
+        c.epa_blocks = nb * sms;
+        nb = occ((const void*)k_manifold<R, EXACT>, PIPE_BLOCK, narrow_smem());
+        c.manifold_blocks = nb * sms;
+        c.sweep_warp_blocks = occ((const void*)k_sweep_warp<R, EXACT, false>, SWEEP_WARP_BLOCK, 0) * sms;
+        c.cull_blocks = occ((const void*)k_cull<R>, PIPE_BLOCK, 0) * sms;
+        // cooperative kernels: one CTA per SM keeps the grid barrier's arrival count low
+        (void)occ((const void*)k_setup_grid<R>, BLOCK, 0);
+        c.setup_grid_blocks = sms;
+        c.sweep_grid_blocks = sms;
+        c.vsweep_grid_blocks = sms;
+        c.sms = sms;
+        return cudaSuccess;
+    }
+
+    template <typename... Args>
+    static cudaError_t coop(void (*kernel)(Args...), int blocks, int block, cudaStream_t st, Args... args) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(block);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, kernel, args...);
+    }
+
+    template <bool VELOCITY>
+    static cudaError_t sweep_warp(const WorldView<R>& W, const PipeConfig& c, cudaStream_t st, double h) {
+        cudaError_t e = cudaMemsetAsync(W.queue + 1, 0, sizeof(int32_t), st);
+        if (e != cudaSuccess) return e;
+        k_sweep_warp<R, EXACT, VELOCITY><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t frame(const WorldView<R>& W, const StepParams& P, const PipeConfig& c, const PipeDims& d,
+                             cudaStream_t st, PipeMarks* marks) {
+        cudaError_t e = cudaMemsetAsync(W.queue, 0, sizeof(int32_t), st);
+        if (e != cudaSuccess) return e;
+        auto mark = [&](int phase) -> cudaError_t {
+            if (!marks || marks->n >= marks->cap) return cudaSuccess;
+            marks->phase[marks->n] = phase;
+            return cudaEventRecord(marks->ev[marks->n++], st);
+        };
+        const double h = P.dt / P.num_substeps;
+        const int body_blocks = (d.nbodies + d.next + PIPE_BLOCK - 1) / PIPE_BLOCK + 1;
+        const int col_blocks = (d.ncolliders * TRANSFORM_GROUP + PIPE_BLOCK - 1) / PIPE_BLOCK + 1;
+        if ((e = mark(-1)) != cudaSuccess) return e;
+        if (d.grid_mode) e = coop(k_setup_grid<R>, c.setup_grid_blocks, BLOCK, st, W, P.dt);
+        else k_setup_cta<R><<<d.num_scenes, BLOCK, 0, st>>>(W, P.dt), e = cudaGetLastError();
+        if (e != cudaSuccess || (e = mark(PH_BROAD)) != cudaSuccess) return e;
+        for (int sub = 0; sub < P.num_substeps; ++sub) {
+            k_predict<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, d.next, h);
+            if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_PREDICT)) != cudaSuccess) return e;
+            if (P.enable_collisions) {
+                k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0);
+                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
+            }
+            k_cull<R><<<c.cull_blocks, PIPE_BLOCK, 0, st>>>(W, P.enable_collisions);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if (P.enable_collisions) {
+                k_gjk<R, EXACT><<<c.gjk_blocks, PIPE_BLOCK, gjk_smem(), st>>>(W);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                k_epa<R, EXACT><<<c.epa_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                k_manifold<R, EXACT><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            }
+            if ((e = mark(PH_NARROW)) != cudaSuccess) return e;
+            for (int it = 0; it < P.num_pos_iters; ++it) {
+                if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, false>, c.sweep_grid_blocks, BLOCK, st, W, h);
+                else e = sweep_warp<false>(W, c, st, h);
+                if (e != cudaSuccess) return e;
+            }
+            if ((e = mark(PH_SOLVE)) != cudaSuccess) return e;
+            k_velocity<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, h);
+            if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_VELOCITY)) != cudaSuccess) return e;
+            if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, true>, c.vsweep_grid_blocks, BLOCK, st, W, h);
+            else e = sweep_warp<true>(W, c, st, h);
+            if (e != cudaSuccess || (e = mark(PH_VSOLVE)) != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+
+    static int launches_per_frame(const StepParams& P) {
+        const int per_sub = 2 + (P.enable_collisions ? 5 : 1) + P.num_pos_iters + 1;
+        return 1 + P.num_substeps * per_sub;
+    }
+};
+
+}  // namespace rp

@@ -238,6 +238,24 @@ __device__ bool limit_angle(V3<R> n, V3<R> n1, V3<R> n2, R alpha, R beta, V3<R>&
     return false;
 }
 
+// True when limit_angle could apply a correction. With limits at or beyond +-pi the wrapped angle
+// can never leave them (any build). Otherwise, in the FP32 build, an FP32 estimate of the angle from
+// FP32 axes decides when it lies more than 0.01 rad inside both limits: its error stays below 1e-3 rad
+// even where asin is ill-conditioned (|s| -> 1). Near a limit, near the +-pi wrap, or where the
+// branch on <n1, n2> is within 1e-3 of flipping, the FP64 evaluation runs.
+__device__ __forceinline__ bool limit_may_act(V3<float> n, V3<float> n1, V3<float> n2, double lo, double hi) {
+    if (lo <= -PI_REF && hi >= PI_REF) return false;
+    if (lo < -PI_REF + 0.02 || hi > PI_REF - 0.02) return true;
+    const float c = vdot(n1, n2);
+    if (fabsf(c) < 1e-3f) return true;
+    const float pi = (float)PI_REF;
+    float phi = asinf(fminf(fmaxf(vdot(vcross(n1, n2), n), -1.f), 1.f));
+    if (c < 0.f) phi = pi - phi;
+    if (phi > pi) phi -= 2.f * pi;
+    if (phi < -pi) phi += 2.f * pi;
+    return !(phi >= (float)lo + 0.01f && phi <= (float)hi - 0.01f);
+}
+
 template <typename R, bool EXACT>
 __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double* lam, R h) {
     Body<R> a = load_body(W, C.e1), b = load_body(W, C.e2);
@@ -270,7 +288,12 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
         dl = pos_dlambda(a, b, p, h, (R)0, (R)lam[0], dx);
         pos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
-        if (C.limited) {
+        bool act = C.limited != 0;
+        if (act && !EXACT) {
+            const Qt<float> qa = qcast<float>(a.q), qb = qcast<float>(b.q);
+            act = limit_may_act(qaxis(qa, C.a1), qaxis(qa, C.l1), qaxis(qb, C.l2), C.lo, C.hi);
+        }
+        if (act) {
             V3<double> n1 = qaxis(a.q, C.l1), n2 = qaxis(b.q, C.l2), n = qaxis(a.q, C.a1), dq64;
             if (limit_angle<double>(n, n1, n2, C.lo, C.hi, dq64)) {
                 dq = v3cast<R>(dq64);
@@ -287,11 +310,18 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
         R dl = pos_dlambda(a, b, p, h, (R)0, (R)lam[0], dx);
         pos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
-        // swing and twist limits: axes and angles in FP64 (see limit_angle)
+        // swing and twist limits: axes and angles in FP64 (see limit_angle), after an FP32 screen
         const double EPS64 = 1e-50;
+        bool swing = true, twist = true;
+        if (!EXACT) {
+            const Qt<float> qa = qcast<float>(a.q), qb = qcast<float>(b.q);
+            V3<float> f1 = qaxis(qa, C.a1), f2 = qaxis(qb, C.a2), fn = vcross(f1, f2);
+            const float fl = vlen(fn);
+            swing = fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi);
+        }
         V3<double> n1 = qaxis(a.q, C.a1), n2 = qaxis(b.q, C.a2);
         V3<double> n = vcross(n1, n2);
-        double nl = vlen(n);
+        double nl = swing ? vlen(n) : 0.0;
         if (nl > EPS64) {
             n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
             V3<double> dq64;
@@ -303,10 +333,26 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
                 lam[1] += (double)d2;
             }
         }
+        if (!EXACT) {   // screened on the orientations after the swing correction
+            const Qt<float> qa = qcast<float>(a.q), qb = qcast<float>(b.q);
+            V3<float> f1 = qaxis(qa, C.a1), f2 = qaxis(qb, C.a2);
+            V3<float> g1 = qaxis(qa, C.l1), g2 = qaxis(qb, C.l2), gn = vadd(f1, f2);
+            const float gl = vlen(gn);
+            const bool never = C.lo2 <= -PI_REF && C.hi2 >= PI_REF;
+            if (gl < 1e-3f) {
+                twist = !never;
+            } else {
+                gn = vscale(1.f / gl, gn);
+                V3<float> h1 = vsub(g1, vscale(vdot(gn, g1), gn)), h2 = vsub(g2, vscale(vdot(gn, g2), gn));
+                const float l1 = vlen(h1), l2 = vlen(h2);
+                twist = (l1 < 1e-3f || l2 < 1e-3f) ? !never
+                                                   : limit_may_act(gn, vscale(1.f / l1, h1), vscale(1.f / l2, h2), C.lo2, C.hi2);
+            }
+        }
         V3<double> a1 = qaxis(a.q, C.a1), b1 = qaxis(a.q, C.l1);
         V3<double> a2 = qaxis(b.q, C.a2), b2 = qaxis(b.q, C.l2);
         n = vadd(a1, a2);
-        nl = vlen(n);
+        nl = twist ? vlen(n) : 0.0;
         if (nl > EPS64) {
             n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
             n1 = vsub(b1, vscale(vdot(n, b1), n));

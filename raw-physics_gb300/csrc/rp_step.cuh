@@ -70,6 +70,14 @@ struct CtaGroup {
     __device__ void sync() const { __syncthreads(); }
 };
 
+struct WarpGroup {   // one warp per scene (small scenes of a batch; barrier = __syncwarp)
+    __device__ int rank() const { return (int)(threadIdx.x & 31); }
+    __device__ int size() const { return 32; }
+    __device__ int nblocks() const { return 1; }
+    __device__ int block() const { return 0; }
+    __device__ void sync() const { __syncwarp(); }
+};
+
 struct GridGroup {
     unsigned* bar;
     uint32_t* status;
@@ -393,46 +401,50 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Hull transform (colliders_update, collider.cpp:409-446) for every collider of the scene
+// Hull transform (colliders_update, collider.cpp:409-446): one collider of body b by `nsub` threads
+// (index `lane` among them)
+template <typename R, bool EXACT>
+__device__ void transform_collider(const WorldView<R>& W, const Collider& col, int b, int lane, int nsub = 32) {
+    const Shape sh = W.shapes[col.shape];
+    double4_32a p4 = W.pos[b], q4 = W.rot[b];
+    V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
+    V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
+    if (EXACT) {
+        M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
+        for (int i = lane; i < sh.nv; i += nsub) {
+            const double* v = W.shape_verts + 3 * (sh.vert_off + i);
+            tv[i] = v3cast<R>(m4_point(M, v3<double>(v[0], v[1], v[2])));
+        }
+        for (int i = lane; i < sh.nf; i += nsub) {
+            const double* nrm = W.face_normal + 3 * (sh.face_off + i);
+            tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
+        }
+    } else {
+        M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
+        for (int i = lane; i < sh.nv; i += nsub) {
+            const float* v = W.shape_verts_f + 3 * (sh.vert_off + i);
+            tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
+        }
+        for (int i = lane; i < sh.nf; i += nsub) {
+            const float* nrm = W.face_normal_f + 3 * (sh.face_off + i);
+            tn[i] = vnorm(mmulv(Rm, v3<R>((R)nrm[0], (R)nrm[1], (R)nrm[2])));
+        }
+    }
+}
+
+// every collider of scene s
 template <typename R, bool EXACT, class G>
 __device__ void transform_hulls(const WorldView<R>& W, const G& g, int s, bool include_fixed) {
     const int b0 = W.scene_body[s], b1 = W.scene_body[s + 1];
     const int c0 = W.col_start[b0], c1 = W.col_start[b1];
     const int lane = threadIdx.x & 31;
     const int gw = g.rank() >> 5, nw = g.size() >> 5;
-    // bodies are found by a short search: colliders are stored body by body
     for (int ci = c0 + gw; ci < c1; ci += nw) {
         const Collider col = W.colliders[ci];
         if (col.type != COL_HULL) continue;
-        int lo = b0, hi = b1 - 1;
-        while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (W.col_start[mid] <= ci) lo = mid; else hi = mid - 1; }
-        int b = lo;
+        const int b = W.col_body[ci];
         if (W.fixed[b] && !include_fixed) continue;
-        const Shape sh = W.shapes[col.shape];
-        double4_32a p4 = W.pos[b], q4 = W.rot[b];
-        V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
-        V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
-        if (EXACT) {
-            M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
-            for (int i = lane; i < sh.nv; i += 32) {
-                const double* v = W.shape_verts + 3 * (sh.vert_off + i);
-                tv[i] = v3cast<R>(m4_point(M, v3<double>(v[0], v[1], v[2])));
-            }
-            for (int i = lane; i < sh.nf; i += 32) {
-                const double* nrm = W.face_normal + 3 * (sh.face_off + i);
-                tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
-            }
-        } else {
-            M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
-            for (int i = lane; i < sh.nv; i += 32) {
-                const double* v = W.shape_verts + 3 * (sh.vert_off + i);
-                tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
-            }
-            for (int i = lane; i < sh.nf; i += 32) {
-                const double* nrm = W.face_normal + 3 * (sh.face_off + i);
-                tn[i] = vnorm(mmulv(Rm, v3<R>((R)nrm[0], (R)nrm[1], (R)nrm[2])));
-            }
-        }
+        transform_collider<R, EXACT>(W, col, b, lane);
     }
 }
 
@@ -505,11 +517,11 @@ __device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, i
 }
 
 // Gap between the box bound of one body and the sphere bound of another (metres, FP32; exact up to
-// ~1e-6 relative), and the scale its rounding error is relative to.
-__device__ __forceinline__ float box_sphere_gap(float4 c, float4 hx, double4_32a pbox, double4_32a qbox, double4_32a psph,
-                                                float rs, float& scale) {
-    const float dx = (float)(psph.x - pbox.x), dy = (float)(psph.y - pbox.y), dz = (float)(psph.z - pbox.z);
-    const float ux = -(float)qbox.x, uy = -(float)qbox.y, uz = -(float)qbox.z, qw = (float)qbox.w;
+// ~1e-6 relative), and the scale its rounding error is relative to. d: sphere centre minus the box
+// body's origin; q: the box body's orientation.
+__device__ __forceinline__ float box_sphere_gap_f(float4 c, float4 hx, float dx, float dy, float dz, float4 q, float rs,
+                                                  float& scale) {
+    const float ux = -q.x, uy = -q.y, uz = -q.z, qw = q.w;
     // rotate d by the inverse of the box body's rotation: v = d + w t + u x t, t = 2 u x d
     const float tx = 2.f * (uy * dz - uz * dy), ty = 2.f * (uz * dx - ux * dz), tz = 2.f * (ux * dy - uy * dx);
     const float vx = dx + qw * tx + (uy * tz - uz * ty);
@@ -519,6 +531,12 @@ __device__ __forceinline__ float box_sphere_gap(float4 c, float4 hx, double4_32a
                 ez = fmaxf(fabsf(vz - c.z) - hx.z, 0.f);
     scale = fabsf(dx) + fabsf(dy) + fabsf(dz) + fabsf(c.x) + fabsf(c.y) + fabsf(c.z) + hx.x + hx.y + hx.z + rs;
     return sqrtf(ex * ex + ey * ey + ez * ez) - rs;
+}
+
+__device__ __forceinline__ float box_sphere_gap(float4 c, float4 hx, double4_32a pbox, double4_32a qbox, double4_32a psph,
+                                                float rs, float& scale) {
+    return box_sphere_gap_f(c, hx, (float)(psph.x - pbox.x), (float)(psph.y - pbox.y), (float)(psph.z - pbox.z),
+                            make_float4((float)qbox.x, (float)qbox.y, (float)qbox.z, (float)qbox.w), rs, scale);
 }
 
 // True only when the hulls of bodies a and b are certainly apart by much more than rounding: the
@@ -540,6 +558,29 @@ __device__ __forceinline__ bool bounds_apart(const WorldView<R>& W, int a, int b
     if (hb.w != 0.f) {
         float gap = box_sphere_gap(cb, hb, pb, qb, pa, ca.w, scale);
         if (gap > 1e-5f * scale + 1e-6f) return true;
+    }
+    return false;
+}
+
+// bounds_apart on the FP32 pose copies: the position rounding (<= 6e-8 |p| per component) is
+// covered by widening the margin with the bodies' distance from the origin.
+template <typename R>
+__device__ __forceinline__ bool bounds_apart_f(const WorldView<R>& W, int a, int b) {
+    const float4 pa = W.pose_f[2 * a], qa = W.pose_f[2 * a + 1], pb = W.pose_f[2 * b], qb = W.pose_f[2 * b + 1];
+    const float4 ca = W.bound[2 * a], ha = W.bound[2 * a + 1], cb = W.bound[2 * b], hb = W.bound[2 * b + 1];
+    const float na = qa.x * qa.x + qa.y * qa.y + qa.z * qa.z + qa.w * qa.w;
+    const float nb = qb.x * qb.x + qb.y * qb.y + qb.z * qb.z + qb.w * qb.w;
+    if (fabsf(na - 1.f) > 1e-5f || fabsf(nb - 1.f) > 1e-5f) return false;
+    const float far = 4e-7f * (fabsf(pa.x) + fabsf(pa.y) + fabsf(pa.z) + fabsf(pb.x) + fabsf(pb.y) + fabsf(pb.z));
+    const float dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
+    float scale;
+    if (ha.w != 0.f) {
+        float gap = box_sphere_gap_f(ca, ha, dx, dy, dz, qa, cb.w, scale);
+        if (gap > 1e-5f * scale + far + 1e-6f) return true;
+    }
+    if (hb.w != 0.f) {
+        float gap = box_sphere_gap_f(cb, hb, -dx, -dy, -dz, qb, ca.w, scale);
+        if (gap > 1e-5f * scale + far + 1e-6f) return true;
     }
     return false;
 }

@@ -54,6 +54,9 @@ struct Shape {               // one convex hull's topology (collider_convex_hull
     int32_t max_face_neighbours;
 };
 
+// Per-pair state between the narrowphase kernels of the phase-major pipeline
+enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3 };
+
 // Phases of the step kernel timed by group rank 0 (rp_phase_times)
 enum { PH_BROAD = 0, PH_ISLANDS, PH_SCHEDULE, PH_PREDICT, PH_TRANSFORM, PH_NARROW, PH_SOLVE, PH_VELOCITY, PH_VSOLVE, PHASES };
 
@@ -111,6 +114,8 @@ struct WorldView {
     const Shape* shapes;
     const double* shape_verts;   // [3 * total verts] local vertices
     const double* face_normal;   // [3 * total faces] local face normals
+    const float* shape_verts_f;  // FP32 copies of shape_verts / face_normal (the FP32 build's
+    const float* face_normal_f;  // transform reads them without FP64 conversions)
     const int32_t* face_elem_start;  // [total faces + num shapes] CSR starts (per shape: nf+1 entries)
     const int32_t* face_elem;        // vertex indices of faces
     const int32_t* csr_start;        // shared CSR start table for v2f / v2n / f2n
@@ -144,6 +149,21 @@ struct WorldView {
     R* contacts;             // [12 * contacts] r1_lc, lambda_n, r2_lc, lambda_t, normal, (unused)
     double* ext_lambda;      // [4 * ext] per-substep lambdas of external constraints
     int32_t max_levels;
+    // ---- phase-major pipeline (one kernel per phase over every scene of the batch) ----------
+    const int32_t* body_scene;   // [N] scene of each body
+    float4* pose_f;              // [2N] FP32 copy of the predicted pose (xyz, 0), (quaternion), written
+                                 // by the predict kernel for the narrowphase's bounds test
+    const int32_t* col_body;     // [colliders] body of each collider
+    int32_t* work_list;          // [pair capacity] global pair slots narrowphased this frame
+    int32_t* work_state;         // [pair capacity] per work item: WS_* below
+    int32_t* gjk_list;           // [pair capacity] work items needing GJK this substep (queue[2] of them)
+    int32_t* hit_list;           // [pair capacity] work items needing a manifold this substep (queue[3])
+    R* work_simplex;             // [16 * pair capacity] GJK simplex of a hit (a, b, c, d)
+    double* work_epa;            // [4 * pair capacity] EPA normal (FP64) and penetration of a hit
+    int32_t* queue;              // [4] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
+                                 //     [2] gjk_list length, [3] hit_list length
+    const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
+    int32_t max_colliders_per_body;
     // ---- control ----------------------------------------------------------------------------
     uint32_t* status;        // [S] status bits per scene
     unsigned int* barrier;   // [2] grid barrier counter / generation

@@ -48,6 +48,8 @@ SIGNATURES = {
     "rp_hull_face": (_i, [_W, _i, _i, _P(_d), _P(_i), _i, _P(_i)]),
     "rp_entity_create": (_i, [_W, _i, _P(_d), _P(_d), _d, _i, _P(ColliderDesc), _u, _d, _d, _d, _P(_i)]),
     "rp_entity_set_velocity": (_i, [_W, _i, _P(_d), _P(_d)]),
+    "rp_entities_create": (_i, [_W, _u, _P(_i), _P(_d), _P(_d), _P(_d), _P(_i), _P(ColliderDesc), _P(_d), _P(_d),
+                                _P(_d), _P(_d), _P(_d), _P(_i)]),
     "rp_entity_add_force": (_i, [_W, _i, _P(_d), _P(_d), _i]),
     "rp_entity_clear_forces": (_i, [_W, _i]),
     "rp_world_set_gravity": (_i, [_W, _d]),
@@ -66,6 +68,7 @@ SIGNATURES = {
     "rp_broad_pairs": (_i, [_W, _i, _P(_u), _u, _P(_u)]),
     "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_counters": (_i, [_W, _P(_u64)]),
+    "rp_world_set_mode": (_i, [_W, _i]),
     "rp_kernel_launches": (_u64, [_W]),
     "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
     "rp_phase_times": (_i, [_W, _P(_d)]),
@@ -245,6 +248,43 @@ class World:
         self.scene = scene
         return first
 
+    def load_batch(self, batch) -> int:
+        """Create every scene of a rawphys.scenes.SceneBatch (scene s of the batch becomes world scene
+        first_scene + s; the world's scene 0 is used first when it is still empty). Returns the index
+        of the first entity."""
+        base = 0 if self.num_entities() == 0 else self.new_scene()
+        for _ in range(batch.num_scenes - 1):
+            self.new_scene()
+        keys = {}
+        hull_of = np.zeros(batch.num_bodies, dtype=np.int32)
+        for i in range(batch.num_bodies):
+            key = (int(batch.mesh[i]), tuple(batch.scale[i]))
+            h = keys.get(key)
+            if h is None:
+                m = batch.meshes[key[0]]
+                h = self.hull(m.positions.astype(np.float64) * np.asarray(key[1], dtype=np.float64), m.indices)
+                keys[key] = h
+            hull_of[i] = h
+        cols = (ColliderDesc * batch.num_bodies)()
+        for i in range(batch.num_bodies):
+            cols[i].type = COLLIDER_HULL
+            cols[i].hull = int(hull_of[i])
+            cols[i].radius = 0.0
+        scene = np.ascontiguousarray(batch.scene + base, dtype=np.int32)
+        c64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        pos, rot, mass, vel, om = c64(batch.pos), c64(batch.rot), c64(batch.mass), c64(batch.vel), c64(batch.omega)
+        mus, mud, rest = c64(batch.mus), c64(batch.mud), c64(batch.rest)
+        fixed = np.ascontiguousarray(batch.fixed, dtype=np.int32)
+        first = _i()
+        self._check(self.lib.rp_entities_create(self.h, batch.num_bodies, scene.ctypes.data_as(_P(_i)), _dp(pos), _dp(rot),
+                                                _dp(mass), fixed.ctypes.data_as(_P(_i)), cols, _dp(mus), _dp(mud),
+                                                _dp(rest), _dp(vel), _dp(om), C.byref(first)))
+        for c in batch.constraints:
+            self.constraint(c, base=first.value)
+        self.set_gravity(batch.gravity)
+        self.scene = batch
+        return first.value
+
     # -- stepping and state ----------------------------------------------------------------
     def simulate(self, dt, substeps, pos_iters=1, collisions=True, steps=1):
         self._check(self.lib.rp_simulate(self.h, float(dt), int(substeps), int(pos_iters), int(bool(collisions)), int(steps)))
@@ -304,6 +344,13 @@ class World:
         self._check(self.lib.rp_last_contacts(self.h, scene, pairs.ctypes.data_as(_P(_i)), _dp(out), cap, C.byref(n)))
         k = min(n.value, cap)
         return pairs[: 2 * k].reshape(-1, 2), out[: 11 * k].reshape(-1, 11)
+
+    MODES = {"auto": 0, "persistent": 1, "phased": 2}
+
+    def set_mode(self, mode: str):
+        """Launch mode of a frame: "phased" (one kernel per phase, CUDA graph), "persistent" (one
+        kernel per frame) or "auto"."""
+        self._check(self.lib.rp_world_set_mode(self.h, self.MODES[mode]))
 
     def counters(self):
         out = (C.c_uint64 * 20)()

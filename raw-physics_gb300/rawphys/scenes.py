@@ -338,3 +338,175 @@ def sphere_scene(n: int = 6, seed: int = 0) -> Scene:
     b.body([Collider("hull", cm, (0.3, 0.3, 0.3)), Collider("hull", cm, (0.6, 0.1, 0.1))], (0.3, 0.5 + 1.1 * n, 0.2),
            mass=2.0)
     return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=120)
+
+
+# ---------------------------------------------------------------------------------------------
+# Batches of many independent scenes
+@dataclass
+class SceneBatch:
+    """Many independent scenes as flat per-body arrays (bodies of scene s are contiguous, scenes in
+    order). Every body has one hull collider: mesh index into `meshes` and a scale vector."""
+    name: str
+    meshes: List[M.Mesh]
+    scene: np.ndarray            # (N,) int32
+    mesh: np.ndarray             # (N,) int32
+    scale: np.ndarray            # (N, 3)
+    pos: np.ndarray              # (N, 3)
+    rot: np.ndarray              # (N, 4)
+    mass: np.ndarray             # (N,)
+    fixed: np.ndarray            # (N,) bool
+    mus: np.ndarray
+    mud: np.ndarray
+    rest: np.ndarray
+    vel: np.ndarray              # (N, 3)
+    omega: np.ndarray            # (N, 3)
+    constraints: List[Constraint] = field(default_factory=list)   # e1 / e2: global body indices
+    num_scenes: int = 1
+    dt: float = 1.0 / 60.0
+    substeps: int = 20
+    pos_iters: int = 1
+    collisions: bool = True
+    gravity: float = 10.0
+    steps: int = 300
+
+    @property
+    def num_bodies(self) -> int:
+        return int(self.pos.shape[0])
+
+    @property
+    def num_dynamic(self) -> int:
+        return int(np.count_nonzero(~self.fixed))
+
+    def scene_sizes(self) -> np.ndarray:
+        """Dynamic bodies per scene."""
+        return np.bincount(self.scene[~self.fixed], minlength=self.num_scenes)
+
+
+def batched_scenes(num_scenes: int = 16384, seed: int = 0, min_bodies: int = 2, max_bodies: int = 512,
+                   chain_fraction: float = 0.25, chain_links=(8, 64)) -> SceneBatch:
+    """Independent scenes of uneven size for the batched form of the step.
+
+    Per scene: N dynamic bodies, N log-uniform in [min_bodies, max_bodies], drawn uniformly from the
+    large scene's shapes (cube, icosahedron, 32-segment cylinder, 42-vertex icosphere) with uniform
+    scale U(0.5, 1.5) (quantised to 1/256 so that bodies of equal shape and scale share one hull),
+    density 1, uniform random orientation, v ~ N(0, 1) m/s. Bodies sit one per cell of a jittered
+    2.86 m grid (the large scene's 23.4 m^3 per body) inside a fixed floor-and-walls box sized to N
+    (box dimensions quantised to 0.5 m). A `chain_fraction` of the scenes also hang a chain of
+    8-64 cube links (0.2 x 0.2 x 0.6 m) from a fixed anchor, joined by spherical joints or by hinges
+    whose axis is a seeded random unit vector, compliance 0, down the box's central column."""
+    rng = np.random.default_rng(seed)
+    meshes = [M.MESHES[n]() for n in SHAPES]
+    CUBE = 0
+    cell = 23.4 ** (1.0 / 3.0)
+    rows = {k: [] for k in ("scene", "mesh", "scale", "pos", "rot", "mass", "fixed", "mus", "mud", "rest", "vel", "omega")}
+    cons: List[Constraint] = []
+    vol_cache = {}
+    n_per = np.exp(rng.uniform(math.log(min_bodies), math.log(max_bodies + 1), size=num_scenes)).astype(int)
+    n_per = np.clip(n_per, min_bodies, max_bodies)
+    has_chain = rng.random(num_scenes) < chain_fraction
+    count = 0
+
+    def add(scene, mesh, scale, pos, rot=(0.0, 0.0, 0.0, 1.0), mass=1.0, fixed=False, v=(0.0, 0.0, 0.0), w=(0.0, 0.0, 0.0)):
+        nonlocal count
+        rows["scene"].append(scene)
+        rows["mesh"].append(mesh)
+        rows["scale"].append(scale)
+        rows["pos"].append(pos)
+        rows["rot"].append(rot)
+        rows["mass"].append(mass)
+        rows["fixed"].append(fixed)
+        rows["mus"].append(0.5)
+        rows["mud"].append(0.3)
+        rows["rest"].append(0.0)
+        rows["vel"].append(v)
+        rows["omega"].append(w)
+        count += 1
+        return count - 1
+
+    for s in range(num_scenes):
+        n = int(n_per[s])
+        links = int(rng.integers(chain_links[0], chain_links[1] + 1)) if has_chain[s] else 0
+        # box: the large scene's 40 x 40 x 60 m for 4096 bodies, scaled to n, at least 3 cells wide
+        f = (n / 4096.0) ** (1.0 / 3.0)
+        half = max(1.5 * cell, math.ceil(20.0 * f * 2.0) / 2.0)
+        nx = max(1, int(2 * half / cell))
+        free_cells = nx * nx - (1 if links else 0)
+        ny = max(1, math.ceil(n / max(free_cells, 1)))
+        height = max(ny * cell, (0.6 * links + 3.0) if links else 0.0)
+        height = math.ceil(height * 2.0) / 2.0
+        t = 0.5
+        add(s, CUBE, (half, t, half), (0.0, -t, 0.0), fixed=True)
+        hy = height / 2.0
+        add(s, CUBE, (t, hy, half), (half + t, hy, 0.0), fixed=True)
+        add(s, CUBE, (t, hy, half), (-half - t, hy, 0.0), fixed=True)
+        add(s, CUBE, (half, hy, t), (0.0, hy, half + t), fixed=True)
+        add(s, CUBE, (half, hy, t), (0.0, hy, -half - t), fixed=True)
+        # grid cells, the central column kept free for a chain
+        cx = (np.arange(nx) + 0.5) * (2 * half / nx) - half
+        cy = (np.arange(max(ny, int(height / cell))) + 0.5) * cell
+        grid = np.stack(np.meshgrid(cx, cy, cx, indexing="ij"), axis=-1).reshape(-1, 3)
+        if links:
+            grid = grid[(np.abs(grid[:, 0]) > 0.7) | (np.abs(grid[:, 2]) > 0.7)]
+        pick = rng.choice(len(grid), size=min(n, len(grid)), replace=False)
+        shapes = rng.integers(0, len(SHAPES), size=len(pick))
+        scales = 0.5 + np.round(rng.uniform(0.0, 1.0, size=len(pick)) * 256.0) / 256.0
+        rots = random_quaternions(rng, len(pick))
+        vels = rng.normal(0.0, 1.0, size=(len(pick), 3))
+        jit = rng.uniform(-0.1, 0.1, size=(len(pick), 3))
+        for i, g in enumerate(pick):
+            sc = _BASE_SCALE * float(scales[i])
+            key = (int(shapes[i]), sc)
+            if key not in vol_cache:
+                vol_cache[key] = M.hull_volume(meshes[key[0]], (sc, sc, sc))
+            add(s, int(shapes[i]), (sc, sc, sc), tuple(grid[g] + jit[i]), rot=tuple(rots[i]), mass=vol_cache[key],
+                v=tuple(vels[i]))
+        if links:
+            joint = "hinge" if rng.random() < 0.5 else "spherical"
+            axis = rng.normal(size=3)
+            rot = _axis_rotation(axis) if joint == "hinge" else (0.0, 0.0, 0.0, 1.0)
+            R = _rot_matrix(rot)
+            down = R @ np.array([0.0, -1.0, 0.0])
+            top = np.array([0.0, height - 0.5, 0.0])
+            anchor = add(s, CUBE, (0.1, 0.1, 0.1), tuple(top), rot=rot, fixed=True)
+            prev, prev_c = anchor, top
+            for i in range(links):
+                centre = prev_c + R @ np.array([0.0, -0.1, 0.0]) + down * 0.3 if i == 0 else prev_c + down * 0.6
+                e = add(s, CUBE, (0.1, 0.3, 0.1), tuple(centre), rot=rot, mass=8.0 * 0.1 * 0.3 * 0.1,
+                        v=tuple(rng.normal(0.0, 0.5, size=3)))
+                r1 = (0.0, -0.1, 0.0) if i == 0 else (0.0, -0.3, 0.0)
+                if joint == "hinge":
+                    cons.append(Constraint("hinge", prev, e, r1, (0.0, 0.3, 0.0), 0.0, axis1=POS_X, axis2=POS_X,
+                                           limited=True, limit_axis1=POS_Y, limit_axis2=POS_Y,
+                                           lower=-0.5 * math.pi, upper=0.5 * math.pi))
+                else:
+                    cons.append(Constraint("spherical", prev, e, r1, (0.0, 0.3, 0.0), swing_axis1=POS_Y,
+                                           swing_axis2=POS_Y, twist_axis1=POS_X, twist_axis2=POS_X,
+                                           swing_lower=-math.pi, swing_upper=math.pi, twist_lower=-math.pi,
+                                           twist_upper=math.pi))
+                prev, prev_c = e, centre
+    f64 = lambda k, d: np.asarray(rows[k], dtype=np.float64).reshape(-1, d)
+    return SceneBatch("batch%d" % num_scenes, meshes, np.asarray(rows["scene"], dtype=np.int32),
+                      np.asarray(rows["mesh"], dtype=np.int32), f64("scale", 3), f64("pos", 3), f64("rot", 4),
+                      np.asarray(rows["mass"], dtype=np.float64), np.asarray(rows["fixed"], dtype=bool),
+                      np.asarray(rows["mus"]), np.asarray(rows["mud"]), np.asarray(rows["rest"]), f64("vel", 3),
+                      f64("omega", 3), cons, num_scenes=num_scenes)
+
+
+def batch_scene(batch: SceneBatch, s: int) -> Scene:
+    """Scene s of a batch as a stand-alone Scene (entity indices local to it), for checks."""
+    idx = np.nonzero(batch.scene == s)[0]
+    b0 = int(idx[0])
+    b = _Builder("%s_scene%d" % (batch.name, s))
+    names = {id(m): n for n, m in zip(SHAPES, batch.meshes)}
+    for i in idx:
+        b.hull_body(names[id(batch.meshes[batch.mesh[i]])], tuple(batch.scale[i]), tuple(batch.pos[i]),
+                    rot=tuple(batch.rot[i]), mass=float(batch.mass[i]), fixed=bool(batch.fixed[i]),
+                    mus=float(batch.mus[i]), mud=float(batch.mud[i]), rest=float(batch.rest[i]),
+                    v=tuple(batch.vel[i]), w=tuple(batch.omega[i]))
+    for c in batch.constraints:
+        if b0 <= c.e1 <= idx[-1]:
+            d = Constraint(**{k: getattr(c, k) for k in c.__dataclass_fields__})
+            d.e1, d.e2 = c.e1 - b0, c.e2 - b0
+            b.scene.constraints.append(d)
+    return b.finish(dt=batch.dt, substeps=batch.substeps, pos_iters=batch.pos_iters, collisions=batch.collisions,
+                    steps=batch.steps)

@@ -116,6 +116,30 @@ def test_scratch_overflow_regrows_and_redoes(ext_built, oracle_built, monkeypatc
     w.close()
 
 
+def test_gjk_cycle_exit_keeps_reference_results(ext_built, oracle_built):
+    """A settled pile of curved hulls (32-segment cylinders, icospheres) resting on the floor and
+    walls: GJK runs that repeat a state stop early instead of running to the 100-iteration cap.
+    Every pair's contacts stay bit-identical to the reference's in the FP64 build, and the early
+    exit is exercised."""
+    from rawphys import scenes as S
+    sc = S.large_scene(1024, seed=0)
+    w = ext_built.World(0, "fp64")
+    w.load(sc)
+    w.step(60)
+    st = w.get_state()
+    o = oracle_built("port").load(sc)
+    o.set_state(st)
+    pairs = o.broad_pairs()
+    w.set_state(st)
+    assert np.array_equal(w.broad_pairs(), pairs)
+    c0 = w.counters()
+    for a, b in pairs:
+        assert np.array_equal(w.contacts(int(a), int(b)), o.contacts(int(a), int(b))), (a, b)
+    c1 = w.counters()
+    assert c1[18] > c0[18], "no GJK run ended on a repeated state"
+    w.close()
+
+
 def test_deep_overlap_and_status(ext_built):
     """Bodies spawned inside each other (EPA from deep penetration) run without fault; the device
     reports informational status only."""

@@ -64,6 +64,37 @@ def test_port_contacts_known_answers(oracle_built, name):
         k += cnt
 
 
+@pytest.mark.parametrize("name", ["stack10", "chain8_hinge", "pile16"])
+def test_port_manifold_for_given_normal(oracle_built, name):
+    """clipping_get_contact_manifold with EPA's own normal reproduces colliders_get_contacts (single
+    hull bodies), and with a tilted normal the port's manifold equals the reference's (live)."""
+    from oracle.oracle import reference_available
+    g = golden(name)
+    scene = SCENES[name][0]()
+    kinds = ["port"] + (["reference"] if reference_available() else [])
+    outs = {}
+    for kind in kinds:
+        o = oracle_built(kind).load(scene)
+        o.set_state(g["kat_state"])
+        res = []
+        k = 0
+        for (a, b), cnt in zip(g["kat_pairs"], g["kat_counts"]):
+            expect = g["kat_contacts"][k:k + cnt]
+            k += cnt
+            hit, e = o.gjk_epa(int(a), int(b))
+            if hit != 1 or len(scene.colliders[a]) != 1 or len(scene.colliders[b]) != 1:
+                continue
+            assert np.array_equal(o.manifold(int(a), int(b), e[0:3], e[3]), expect), (kind, a, b)
+            tilted = e[0:3] + np.array([1e-3, -2e-3, 1.5e-3])
+            tilted /= np.linalg.norm(tilted)
+            res.append(o.manifold(int(a), int(b), tilted, e[3]))
+        outs[kind] = res
+    if "reference" in outs:
+        assert len(outs["port"]) == len(outs["reference"])
+        for x, y in zip(outs["port"], outs["reference"]):
+            assert np.array_equal(x, y)
+
+
 def test_port_large_one_frame(oracle_built):
     g = golden("large1024")
     scene = SCENES["large1024"][0]()
