@@ -13,14 +13,19 @@ Printed JSON line (rank 0):
             (CUDA events on the world's stream; L2 flushed with a 256 MiB write before every frame)
   e2e       the same metric through the C ABI with host buffers: every frame uploads the full body
             state (rp_state_set), steps, and downloads it (rp_state_get), copies inside the timer
-  roofline  the step kernel's algorithmic bytes per launch / its average duration, against the
-            measured HBM copy bandwidth
+  roofline  the dominant kernel (the position sweep, one launch per substep): its algorithmic
+            bytes per launch / its average duration from CUDA events around each phase, against
+            the measured HBM copy bandwidth
   cpu_baseline  the oracle port (plain-C restatement of the reference, bit-exact to it) on one host
             core, on a bounded sample of the same workload
+  batched   the batched form beside it: 16384 independent scenes of 2-512 bodies (a quarter with
+            hinge / spherical chains) in one world, one CUDA-graph replay per frame
+--workload batched measures the batched form alone (its value becomes the line's value).
 --impl reference times that CPU implementation on every host core instead (one replica of the
 workload per core; the reference is single-threaded and keeps process-global state).
 Multi-GPU (torchrun): the single scene does not shard, so every rank steps its own replica
-("replicas only"); value is the sum over ranks of body-substeps over the slowest rank's time.
+("replicas only"); value is the sum over ranks of body-substeps over the slowest rank's time. The
+batched form shards by scene: every rank steps its own batch.
 """
 from __future__ import annotations
 
@@ -42,6 +47,10 @@ UNIT = "body-substeps/s"
 # Algorithmic bytes of the plain form (per substep): body state read + written, the pair list, and
 # every contact record written once and read by the position and velocity solves.
 STATE_READ_B, STATE_WRITE_B, PAIR_B, CONTACT_B = 160, 84, 16, 156
+# Algorithmic bytes of one position sweep (the dominant kernel): every contact record read (48 B)
+# and its two lambdas written back (8 B); per solved pair node, both bodies' pose read and written
+# (2 x 64 B) and their inverse mass and inertia read (2 x 28 B).
+SWEEP_CONTACT_B, SWEEP_NODE_B = 56, 2 * (64 + 64 + 28)
 
 
 def make_scene(name):
@@ -104,8 +113,8 @@ def measured_peak_hbm():
 
 
 def profile_traffic():
-    """DRAM bytes per step-kernel launch from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "step_kernel_large4096.md")
+    """DRAM bytes per position-sweep launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "pipeline_large4096.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -196,6 +205,9 @@ def run_ours(args):
         torch.cuda.set_device(local)
     dev = local
     torch.cuda.set_device(dev)
+    if args.workload == "batched":
+        run_batched_only(args, dev, rank, world_size)
+        return
     stream = torch.cuda.Stream(dev)          # a capturable stream: frames replay from a CUDA graph
     scene = make_scene(args.workload)
     w = rawphys.World(dev, "fp32")
@@ -247,12 +259,14 @@ def run_ours(args):
     value = nd * scene.substeps * args.steps * world_size / (total_ms / 1e3)
     status = w.status()
 
-    # roofline of the step kernel: algorithmic bytes per launch over its measured duration
+    # roofline of the dominant kernel, the position sweep (one launch per substep): algorithmic bytes
+    # per launch over its duration, both from the phase pass (CUDA events around each phase)
     pairs_per_step = (c1[6] - c0[6]) / args.steps
     contacts_per_step = (c1[5] - c0[5]) / args.steps
-    alg_bytes = scene.substeps * (STATE_READ_B + STATE_WRITE_B) * nd + scene.substeps * PAIR_B * pairs_per_step + \
-        CONTACT_B * contacts_per_step
-    launch_ms = total_ms / max(launches, 1) if world_size == 1 else total_ms / args.steps
+    manifolds_per_step = (c1[2] - c0[2]) / args.steps
+    sweeps = scene.substeps * scene.pos_iters
+    alg_bytes = (contacts_per_step * SWEEP_CONTACT_B + manifolds_per_step * SWEEP_NODE_B) / scene.substeps
+    launch_ms = phase_ms["solve"] / sweeps
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     traffic = profile_traffic()
@@ -271,6 +285,9 @@ def run_ours(args):
     b1 = w.transfer_bytes()
     e2e = {"value": nd * scene.substeps * e2e_steps * world_size / e2e_wall, "unit": UNIT,
            "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_steps, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_steps}
+
+    w.close()
+    batched = measure_batched(args, dev, rank, world_size, value) if args.batched_scenes > 0 else None
 
     if rank == 0:
         cpu_v, cpu_t = cpu_baseline_sample(scene, start_state, frames=args.cpu_frames)
@@ -300,13 +317,96 @@ def run_ours(args):
                            "phase_ms_per_step": phase_ms},
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "peak_kind": peak_kind, "traffic": traffic,
+                             "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_sweep_grid (position sweep)",
                              "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
+                "batched": batched,
                 "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                                  "sample": "%d frames of the same scene from the state the timed GPU frames start "
                                            "from, oracle port (bit-exact restatement of the reference), %.1f s"
                                            % (args.cpu_frames, cpu_t)},
                 "e2e": e2e, "clocks": clk.summary(), "device_status": status}
+        print(json.dumps(line), flush=True)
+    if world_size > 1:
+        torch.distributed.destroy_process_group()
+
+
+def measure_batched(args, dev, rank, world_size, plain_value):
+    """The batched form: many independent scenes of uneven size in one world (rawphys.scenes.
+    batched_scenes), every frame one replay of the captured phase-major graph. Weak scaling: every
+    rank steps its own batch (seed = rank)."""
+    import torch
+    import rawphys
+    from rawphys import scenes as S
+    batch = S.batched_scenes(args.batched_scenes, seed=rank)
+    stream = torch.cuda.Stream(dev)
+    w = rawphys.World(dev, "fp32")
+    w.set_stream(stream.cuda_stream)
+    w.load_batch(batch)
+    w.step(args.batched_settle)
+    w.step(3)
+    w.sync()
+    nd = batch.num_dynamic
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    c0 = w.counters()
+    l0 = w.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.batched_steps)]
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.batched_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            w.step(1)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    total_ms = float(sum(a.elapsed_time(b) for a, b in ev))
+    c1 = w.counters()
+    launches = w.kernel_launches() - l0
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    p0 = w.phase_times()
+    w.set_timing(True)
+    w.step(2)
+    w.sync()
+    w.set_timing(False)
+    p1 = w.phase_times()
+    value = nd * batch.substeps * args.batched_steps * world_size / (total_ms / 1e3)
+    sizes = batch.scene_sizes()
+    out = {"value": value, "unit": UNIT, "ms_per_step": total_ms / args.batched_steps, "steps": args.batched_steps,
+           "vs_plain_gpu": value / plain_value if plain_value else None,
+           "workload": "%d independent scenes, dynamic bodies per scene log-uniform in [2, 512] (mean %.1f, max %d; "
+                       "%d dynamic bodies in all), large-scene shape mix, %d scenes with 8-64-link hinge or spherical "
+                       "chains (%d joints), dt=1/60, %d substeps, FP32 with FP64 poses; frames %d-%d after a %d-frame "
+                       "settle" % (batch.num_scenes, sizes.mean(), sizes.max(), nd,
+                                   len({int(batch.scene[c.e1]) for c in batch.constraints}), len(batch.constraints),
+                                   batch.substeps, args.batched_settle + 3, args.batched_settle + 3 + args.batched_steps,
+                                   args.batched_settle),
+           "l2": "flushed (256 MiB write) before every timed frame",
+           "pairs_per_step": (c1[6] - c0[6]) / args.batched_steps,
+           "contacts_per_step": (c1[5] - c0[5]) / args.batched_steps,
+           "phase_ms_per_step": {k: round((p1[k] - p0[k]) / 2, 3) for k in p0},
+           "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches}
+    w.close()
+    return out
+
+
+def run_batched_only(args, dev, rank, world_size):
+    """--workload batched: the batched form alone, as the line's own value."""
+    import torch
+    b = measure_batched(args, dev, rank, world_size, None)
+    if rank == 0:
+        line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": world_size, "steps": b["steps"],
+                "warmup": 3, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+                "config": {"workload": b["workload"], "l2": b["l2"],
+                           "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
+                           "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
+                           "phase_ms_per_step": b["phase_ms_per_step"]},
+                "gpu_launches": b["gpu_launches"], "clocks": b["clocks"], "device_status": b["device_status"]}
         print(json.dumps(line), flush=True)
     if world_size > 1:
         torch.distributed.destroy_process_group()
@@ -319,8 +419,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--settle", type=int, default=120)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="large4096", choices=["large4096", "stack10"])
+    ap.add_argument("--workload", default="large4096", choices=["large4096", "stack10", "batched"])
     ap.add_argument("--cpu-frames", type=int, default=2)
+    ap.add_argument("--batched-scenes", type=int, default=16384, help="0 skips the batched measurement")
+    ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--batched-settle", type=int, default=20)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -503,6 +503,162 @@ static __device__ void fcollision_solve(const WorldView<float>& W, FBody& a, FBo
 }
 
 // --------------------------------------------------------------------------------------------
+// External constraints of the FP32 build on FP64-base / FP32-delta bodies (pbd.cpp:81-379): the
+// same order of corrections as ext_solve, each applied to the FP32 deltas; joint-limit angles are
+// screened in FP32 and evaluated in FP64 (from the FP64 orientation q0 + dq) where they may act.
+__device__ __forceinline__ float fdlambda(float c, float w1, float w2, float h, float compliance, float lambda) {
+    const float til = compliance / (h * h);
+    return (-c - til * lambda) / (w1 + w2 + til);
+}
+
+__device__ __forceinline__ float fpos_dlambda_c(const FBody& a, const FBody& b, const Pcpd<float>& p, float h,
+                                                float compliance, float lambda, V3<float> dx) {
+    const float c = vlen(dx);
+    if (c <= 0.f) return 0.f;
+    const V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
+    const float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
+    const float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    return fdlambda(c, w1, w2, h, compliance, lambda);
+}
+
+__device__ __forceinline__ Acpd<float> facpd(const FBody& a, const FBody& b) {
+    Acpd<float> r;
+    r.I1 = world_tensor(a.q(), a.Iinv);
+    r.I2 = world_tensor(b.q(), b.Iinv);
+    return r;
+}
+
+__device__ __forceinline__ void fang_apply(FBody& a, FBody& b, const Acpd<float>& A, float dl, V3<float> dq) {
+    const float th = vlen(dq);
+    if (th <= 0.f) return;
+    const V3<float> n = v3<float>(dq.x / th, dq.y / th, dq.z / th);
+    const V3<float> imp = vscale(-dl, n);
+    const V3<float> a1 = mmulv(A.I1, imp), a2 = mmulv(A.I2, imp);
+    const Qt<float> q1 = qmul(qt<float>(a1.x, a1.y, a1.z, 0.f), a.q());
+    const Qt<float> q2 = qmul(qt<float>(a2.x, a2.y, a2.z, 0.f), b.q());
+    if (!a.fixed) frot_update(a, qt<float>(0.5f * q1.x, 0.5f * q1.y, 0.5f * q1.z, 0.5f * q1.w));
+    if (!b.fixed) frot_update(b, qt<float>(-0.5f * q2.x, -0.5f * q2.y, -0.5f * q2.z, -0.5f * q2.w));
+}
+
+// the FP64 orientation of a body in delta form
+__device__ __forceinline__ Qt<double> fq64(const FBody& B) {
+    return qt<double>(B.q0.x + (double)B.dq.x, B.q0.y + (double)B.dq.y, B.q0.z + (double)B.dq.z, B.q0.w + (double)B.dq.w);
+}
+
+// angular correction of one joint limit (limit_angle's dq, FP64) on the deltas
+__device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64, float h, double* lam) {
+    const V3<float> dq = v3cast<float>(dq64);
+    const Acpd<float> B = facpd(a, b);
+    const float th = vlen(dq);
+    if (th <= 0.f) return;
+    const V3<float> n = v3<float>(dq.x / th, dq.y / th, dq.z / th);
+    const float dl = fdlambda(th, vdot(n, mmulv(B.I1, n)), vdot(n, mmulv(B.I2, n)), h, 0.f, (float)*lam);
+    fang_apply(a, b, B, dl, dq);
+    *lam += (double)dl;
+}
+
+static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint& C, double* lam, float h) {
+    FBody a = load_fbody(W, C.e1), b = load_fbody(W, C.e2);
+    const V3<float> r1 = v3<float>((float)C.r1[0], (float)C.r1[1], (float)C.r1[2]);
+    const V3<float> r2 = v3<float>((float)C.r2[0], (float)C.r2[1], (float)C.r2[2]);
+    const V3<float> base_ab = v3cast<float>(vsub(a.x0, b.x0));
+    auto anchor = [&](const Pcpd<float>& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
+    switch (C.type) {
+    case CON_POSITIONAL: {  // pbd.cpp:81-97
+        const V3<float> base = v3cast<float>(vsub(vsub(a.x0, b.x0), v3<double>(C.distance[0], C.distance[1], C.distance[2])));
+        const V3<float> dx = vadd(base, vsub(a.dx, b.dx));
+        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const float dl = fpos_dlambda_c(a, b, p, h, (float)C.compliance, (float)lam[0], dx);
+        fpos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+    } break;
+    case CON_MUTUAL_ORIENTATION: {  // pbd.cpp:156-173
+        const Acpd<float> A = facpd(a, b);
+        const Qt<float> aux = qmul(a.q(), qinverse(b.q()));
+        const V3<float> dq = v3<float>(2.f * aux.x, 2.f * aux.y, 2.f * aux.z);
+        const float dl = ang_dlambda(A, h, (float)C.compliance, (float)lam[0], dq);
+        fang_apply(a, b, A, dl, dq);
+        lam[0] += (double)dl;
+    } break;
+    case CON_HINGE: {  // pbd.cpp:245-299
+        const Acpd<float> A = facpd(a, b);
+        const V3<float> dq = vcross(qaxis(a.q(), C.a1), qaxis(b.q(), C.a2));
+        float dl = ang_dlambda(A, h, (float)C.compliance, (float)lam[1], dq);
+        fang_apply(a, b, A, dl, dq);
+        lam[1] += (double)dl;
+        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const V3<float> dx = anchor(p);
+        dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
+        fpos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+        if (C.limited && limit_may_act(qaxis(a.q(), C.a1), qaxis(a.q(), C.l1), qaxis(b.q(), C.l2), C.lo, C.hi)) {
+            const Qt<double> qa = fq64(a), qb = fq64(b);
+            V3<double> dq64;
+            if (limit_angle<double>(qaxis(qa, C.a1), qaxis(qa, C.l1), qaxis(qb, C.l2), C.lo, C.hi, dq64))
+                flimit_apply(a, b, dq64, h, &lam[2]);
+        }
+    } break;
+    case CON_SPHERICAL: {  // pbd.cpp:301-379
+        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const V3<float> dx = anchor(p);
+        const float dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
+        fpos_apply(a, b, p, dl, dx);
+        lam[0] += (double)dl;
+        const double EPS64 = 1e-50;
+        {   // swing
+            const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2), fn = vcross(f1, f2);
+            const float fl = vlen(fn);
+            if (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi)) {
+                const Qt<double> qa = fq64(a), qb = fq64(b);
+                const V3<double> n1 = qaxis(qa, C.a1), n2 = qaxis(qb, C.a2);
+                V3<double> n = vcross(n1, n2);
+                const double nl = vlen(n);
+                V3<double> dq64;
+                if (nl > EPS64 && limit_angle<double>(v3<double>(n.x / nl, n.y / nl, n.z / nl), n1, n2, C.lo, C.hi, dq64))
+                    flimit_apply(a, b, dq64, h, &lam[1]);
+            }
+        }
+        {   // twist, on the orientations after the swing correction
+            const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2);
+            const V3<float> g1 = qaxis(a.q(), C.l1), g2 = qaxis(b.q(), C.l2);
+            V3<float> gn = vadd(f1, f2);
+            const float gl = vlen(gn);
+            const bool never = C.lo2 <= -PI_REF && C.hi2 >= PI_REF;
+            bool act;
+            if (gl < 1e-3f) {
+                act = !never;
+            } else {
+                gn = vscale(1.f / gl, gn);
+                const V3<float> h1 = vsub(g1, vscale(vdot(gn, g1), gn)), h2 = vsub(g2, vscale(vdot(gn, g2), gn));
+                const float l1 = vlen(h1), l2 = vlen(h2);
+                act = (l1 < 1e-3f || l2 < 1e-3f) ? !never
+                                                 : limit_may_act(gn, vscale(1.f / l1, h1), vscale(1.f / l2, h2), C.lo2, C.hi2);
+            }
+            if (act) {
+                const Qt<double> qa = fq64(a), qb = fq64(b);
+                const V3<double> a1 = qaxis(qa, C.a1), b1 = qaxis(qa, C.l1), a2 = qaxis(qb, C.a2), b2 = qaxis(qb, C.l2);
+                V3<double> n = vadd(a1, a2);
+                const double nl = vlen(n);
+                if (nl > EPS64) {
+                    n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
+                    V3<double> n1 = vsub(b1, vscale(vdot(n, b1), n)), n2 = vsub(b2, vscale(vdot(n, b2), n));
+                    const double l1 = vlen(n1), l2 = vlen(n2);
+                    V3<double> dq64;
+                    if (l1 > EPS64 && l2 > EPS64 &&
+                        limit_angle<double>(n, v3<double>(n1.x / l1, n1.y / l1, n1.z / l1),
+                                            v3<double>(n2.x / l2, n2.y / l2, n2.z / l2), C.lo2, C.hi2, dq64))
+                        flimit_apply(a, b, dq64, h, &lam[2]);
+                }
+            }
+        }
+    } break;
+    default: break;
+    }
+    store_fbody(W, a);
+    store_fbody(W, b);
+}
+
+// --------------------------------------------------------------------------------------------
 // Predict (pbd.cpp:537-577) for one body
 template <typename R, bool EXACT>
 __device__ void predict_body(const WorldView<R>& W, int b, double h) {

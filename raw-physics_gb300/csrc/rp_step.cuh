@@ -657,7 +657,8 @@ template <typename R, bool EXACT>
 __device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
     const int e0 = W.scene_ext[s], ne = W.scene_ext[s + 1] - e0;
     if (k < ne) {
-        ext_solve<R, EXACT>(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
+        if constexpr (EXACT) ext_solve<R, EXACT>(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
+        else fext_solve(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
         return;
     }
     const int p = W.scene_pair_cap[s] + (k - ne);

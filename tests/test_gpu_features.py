@@ -301,3 +301,49 @@ def test_pbd_simulate_dropin(ext_built, oracle_built, monkeypatch):
     for i in range(8):
         assert np.allclose([tv[i].x, tv[i].y, tv[i].z], R @ np.array([v[i].x, v[i].y, v[i].z]) + p, atol=1e-12)
     lib.rp_compat_reset()
+
+
+def test_batched_form_matches_oracle_per_scene(ext_built, oracle_built):
+    """The batched form (many scenes of uneven size, a quarter with hinge or spherical chains) in one
+    world: every scene's trajectory equals the oracle's run of that scene alone, bit for bit in the
+    FP64 build, in both launch modes."""
+    from rawphys import scenes as S
+    batch = S.batched_scenes(12, seed=5, min_bodies=2, max_bodies=40, chain_fraction=0.5, chain_links=(8, 12))
+    frames = 8
+    got = {}
+    for mode in ("phased", "persistent"):
+        w = ext_built.World(0, "fp64")
+        w.set_mode(mode)
+        first = w.load_batch(batch)
+        w.simulate(batch.dt, batch.substeps, batch.pos_iters, batch.collisions, frames)
+        got[mode] = w.get_state()[first:]
+        assert (w.status() & ~(1 << 8)) == 0
+        w.close()
+    assert np.array_equal(got["phased"], got["persistent"])
+    for s in range(batch.num_scenes):
+        idx = np.nonzero(batch.scene == s)[0]
+        o = oracle_built("port").load(S.batch_scene(batch, s))
+        o.step(frames)
+        assert np.array_equal(got["phased"][idx], o.get_state()), "scene %d" % s
+
+
+def test_batched_form_fp32_per_step_error(ext_built, oracle_built):
+    """FP32 batched form: per-step position error from identical states against the oracle, per
+    scene of a mixed batch (contacts and joints)."""
+    from rawphys import scenes as S
+    batch = S.batched_scenes(8, seed=6, min_bodies=4, max_bodies=30, chain_fraction=0.25, chain_links=(8, 10))
+    w = ext_built.World(0, "fp32")
+    first = w.load_batch(batch)
+    w.simulate(batch.dt, batch.substeps, 1, True, 30)
+    st = w.get_state()[first:]
+    w.simulate(batch.dt, batch.substeps, 1, True, 1)
+    nxt = w.get_state()[first:]
+    errs = []
+    for s in range(batch.num_scenes):
+        idx = np.nonzero(batch.scene == s)[0]
+        o = oracle_built("port").load(S.batch_scene(batch, s))
+        o.set_state(st[idx])
+        o.step(1)
+        errs.append(float(np.max(np.abs(o.get_state()[:, 0:3] - nxt[idx, 0:3]))))
+    assert np.median(errs) <= 1e-4, errs
+    w.close()
