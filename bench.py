@@ -20,6 +20,9 @@ Printed JSON line (rank 0):
             core, on a bounded sample of the same workload
   batched   the batched form beside it: 16384 independent scenes of 2-512 bodies (a quarter with
             hinge / spherical chains) in one world, one CUDA-graph replay per frame
+  precision the precision-stress report: 128 towers of 64 cubes (masses 1:100, 50 substeps) run
+            in the FP32 and the all-FP64 builds side by side for 300 frames (per-step error from
+            identical states, trajectory divergence, tower drift, energy drift)
 --workload batched measures the batched form alone (its value becomes the line's value).
 --impl reference times that CPU implementation on every host core instead (one replica of the
 workload per core; the reference is single-threaded and keeps process-global state).
@@ -288,6 +291,16 @@ def run_ours(args):
 
     w.close()
     batched = measure_batched(args, dev, rank, world_size, value) if args.batched_scenes > 0 else None
+    precision = None
+    if args.precision_towers > 0 and rank == 0:
+        from rawphys import scenes as S
+        from rawphys.precision import precision_report
+        precision = precision_report(rawphys, S.tower_batch(args.precision_towers, n=64, seed=0),
+                                     frames=args.precision_frames, sample_every=max(1, args.precision_frames // 6),
+                                     device=dev)
+        precision["workload"] = ("%d towers of 64 unit cubes, masses alternating 1:100, 50 substeps, dt=1/60; FP32 build "
+                                 "against the all-FP64 build (bit-identical to the FP64 CPU oracle, tests/test_gpu_precision.py)"
+                                 % args.precision_towers)
 
     if rank == 0:
         cpu_v, cpu_t = cpu_baseline_sample(scene, start_state, frames=args.cpu_frames)
@@ -320,6 +333,7 @@ def run_ours(args):
                              "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_sweep_grid (position sweep)",
                              "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
                 "batched": batched,
+                "precision": precision,
                 "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                                  "sample": "%d frames of the same scene from the state the timed GPU frames start "
                                            "from, oracle port (bit-exact restatement of the reference), %.1f s"
@@ -424,6 +438,8 @@ def main():
     ap.add_argument("--batched-scenes", type=int, default=16384, help="0 skips the batched measurement")
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--batched-settle", type=int, default=20)
+    ap.add_argument("--precision-towers", type=int, default=128, help="0 skips the precision-stress report")
+    ap.add_argument("--precision-frames", type=int, default=300)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -510,3 +510,55 @@ def batch_scene(batch: SceneBatch, s: int) -> Scene:
             b.scene.constraints.append(d)
     return b.finish(dt=batch.dt, substeps=batch.substeps, pos_iters=batch.pos_iters, collisions=batch.collisions,
                     steps=batch.steps)
+
+
+def shard_batch(batch: SceneBatch, rank: int, world: int) -> SceneBatch:
+    """Scenes of a batch for one of `world` ranks: contiguous scene ranges balanced by body count
+    (scenes are independent, so ranks exchange nothing while stepping)."""
+    sizes = np.bincount(batch.scene, minlength=batch.num_scenes).astype(np.float64)
+    cum = np.concatenate([[0.0], np.cumsum(sizes)])
+    bounds = [int(np.searchsorted(cum, cum[-1] * r / world, side="left")) for r in range(world + 1)]
+    bounds[0], bounds[-1] = 0, batch.num_scenes
+    s0, s1 = bounds[rank], max(bounds[rank], bounds[rank + 1])
+    keep = (batch.scene >= s0) & (batch.scene < s1)
+    idx = np.nonzero(keep)[0]
+    remap = -np.ones(batch.num_bodies, dtype=np.int64)
+    remap[idx] = np.arange(len(idx))
+    cons = []
+    for c in batch.constraints:
+        if keep[c.e1]:
+            d = Constraint(**{k: getattr(c, k) for k in c.__dataclass_fields__})
+            d.e1, d.e2 = int(remap[c.e1]), int(remap[c.e2])
+            cons.append(d)
+    return SceneBatch("%s_rank%d" % (batch.name, rank), batch.meshes, (batch.scene[idx] - s0).astype(np.int32),
+                      batch.mesh[idx], batch.scale[idx], batch.pos[idx], batch.rot[idx], batch.mass[idx],
+                      batch.fixed[idx], batch.mus[idx], batch.mud[idx], batch.rest[idx], batch.vel[idx],
+                      batch.omega[idx], cons, num_scenes=s1 - s0, dt=batch.dt, substeps=batch.substeps,
+                      pos_iters=batch.pos_iters, collisions=batch.collisions, gravity=batch.gravity,
+                      steps=batch.steps)
+
+
+def tower_batch(num_towers: int = 2048, n: int = 64, ratio: float = 100.0, seed: int = 0, substeps: int = 50) -> SceneBatch:
+    """Precision-stress batch: `num_towers` independent scenes, each a tower of n unit cubes on its
+    own fixed floor, masses alternating 1 : ratio, xz jitter U(-0.005, 0.005) m, 50 substeps."""
+    rng = np.random.default_rng(seed)
+    meshes = [M.MESHES[name]() for name in SHAPES]
+    N = num_towers * (n + 1)
+    scene = np.repeat(np.arange(num_towers, dtype=np.int32), n + 1)
+    mesh = np.zeros(N, dtype=np.int32)
+    scale = np.tile(np.array([[20.0, 0.5, 20.0]] + [[0.5, 0.5, 0.5]] * n), (num_towers, 1))
+    pos = np.zeros((N, 3))
+    jit = rng.uniform(-0.005, 0.005, size=(num_towers, n, 2))
+    for t in range(num_towers):
+        base = t * (n + 1)
+        pos[base] = (0.0, -0.5, 0.0)
+        pos[base + 1:base + n + 1, 0] = jit[t, :, 0]
+        pos[base + 1:base + n + 1, 1] = 0.5 + np.arange(n) * 1.0005
+        pos[base + 1:base + n + 1, 2] = jit[t, :, 1]
+    rot = np.tile(np.array([0.0, 0.0, 0.0, 1.0]), (N, 1))
+    mass = np.tile(np.array([1.0] + [1.0 if i % 2 == 0 else ratio for i in range(n)]), num_towers)
+    fixed = np.tile(np.array([True] + [False] * n), num_towers)
+    z = np.zeros((N, 3))
+    return SceneBatch("towers%d_%d" % (num_towers, n), meshes, scene, mesh, scale, pos, rot, mass, fixed,
+                      np.full(N, 0.5), np.full(N, 0.3), np.zeros(N), z, z.copy(), [], num_scenes=num_towers,
+                      substeps=substeps, steps=10000)
