@@ -217,9 +217,10 @@ def run_ours(args):
     w.set_stream(stream.cuda_stream)
     w.load(scene)
     nd = scene.num_dynamic
-    # untimed: settle into the colliding regime, then warm up
+    # untimed: settle into the colliding regime, pick the launch configuration, then warm up
     if args.settle:
         w.step(args.settle)
+    tuned = w.autotune(frames=3) if args.autotune else None
     w.step(args.warmup)
     w.sync()
     start_state = w.get_state()
@@ -327,7 +328,7 @@ def run_ours(args):
                            "pairs_narrowphased_per_step": (c1[12] - c0[12]) / args.steps,
                            "pairs_bounds_apart_per_step": (c1[13] - c0[13]) / args.steps,
                            "gjk_epa_manifold_support_cycles_per_step": [(c1[k] - c0[k]) / args.steps for k in (14, 15, 16, 17)],
-                           "phase_ms_per_step": phase_ms},
+                           "phase_ms_per_step": phase_ms, "autotuned": tuned},
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                              "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_sweep_grid (position sweep)",
@@ -357,6 +358,7 @@ def measure_batched(args, dev, rank, world_size, plain_value):
     w.set_stream(stream.cuda_stream)
     w.load_batch(batch)
     w.step(args.batched_settle)
+    tuned = w.autotune(frames=2) if args.autotune else None
     w.step(3)
     w.sync()
     nd = batch.num_dynamic
@@ -403,7 +405,7 @@ def measure_batched(args, dev, rank, world_size, plain_value):
            "pairs_per_step": (c1[6] - c0[6]) / args.batched_steps,
            "contacts_per_step": (c1[5] - c0[5]) / args.batched_steps,
            "phase_ms_per_step": {k: round((p1[k] - p0[k]) / 2, 3) for k in p0},
-           "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches}
+           "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches, "autotuned": tuned}
     w.close()
     return out
 
@@ -439,6 +441,7 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--batched-settle", type=int, default=20)
     ap.add_argument("--precision-towers", type=int, default=128, help="0 skips the precision-stress report")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default launch configuration")
     ap.add_argument("--precision-frames", type=int, default=300)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -89,6 +89,14 @@ void      rp_world_destroy(rp_world* w);
 rp_status rp_world_set_stream(rp_world* w, void* cuda_stream);
 /* Selects the launch mode (RP_MODE_*); no counterpart in the reference. */
 rp_status rp_world_set_mode(rp_world* w, int32_t mode);
+/* Autotuner (no counterpart in the reference): times `frames` frames of the world's current scenes
+ * from their current state under each candidate launch configuration — launch mode, threads per
+ * collider in the hull transform (4/8/16/32), and the sweep layout (levels swept by one CTA below
+ * 128..2048 nodes for one large scene; one warp or one CTA per scene for a batch) — keeps the
+ * fastest, and restores the state. Every configuration gives identical results. Call it with no
+ * forces pending. choice receives {mode, transform threads, CTA-per-scene sweeps, solo level size}. */
+rp_status rp_autotune(rp_world* w, double dt, uint32_t num_substeps, uint32_t num_pos_iters, int32_t enable_collisions,
+                      uint32_t frames, int32_t choice[4]);
 const char* rp_last_error(void);
 /* Adds a new empty scene; scene 0 exists from creation. */
 rp_status rp_scene_create(rp_world* w, int32_t* out_scene);

@@ -121,6 +121,7 @@ struct rp_world {
     // phase-major pipeline
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
+    int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     bool pipe_ready = false;
     PipeConfig pipe;
     PipeDims dims;
@@ -549,6 +550,7 @@ WorldView<R> make_view(rp_world* w) {
     V.work_epa = w->d_work_epa.as<double>();
     V.queue = w->d_queue.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
+    V.solo_nodes = w->solo_nodes;
     return V;
 }
 
@@ -1484,6 +1486,84 @@ rp_status rp_set_timing(rp_world* w, int32_t enabled) {
     if (check_world(w)) return RP_ERR_INVALID;
     w->timing = enabled != 0;
     return RP_OK;
+}
+
+rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters, int32_t collisions, uint32_t frames,
+                      int32_t choice[4]) {
+    if (check_world(w) || !choice) return RP_ERR_INVALID;
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
+    if (!(dt > 0.0) || substeps == 0 || frames == 0) return fail(RP_ERR_INVALID, "bad step arguments");
+    for (const HostBody& b : w->bodies)
+        if (!b.forces.empty()) return fail(RP_ERR_STATE, "autotune runs before forces are added for the next frame");
+    if (w->bodies.empty()) return RP_OK;
+    // trials run from the same state, which is restored at the end; results do not depend on the choice
+    const size_t n = w->bodies.size();
+    std::vector<double> saved(n * RP_STATE_DOUBLES);
+    rp_status s = rp_state_get(w, saved.data());
+    if (s != RP_OK) return s;
+    const uint64_t steps0 = w->steps, substeps0 = w->substeps;
+    const uint32_t status0 = w->status_accum;
+    cudaEvent_t e0, e1;
+    RP_CUDA(cudaEventCreate(&e0));
+    RP_CUDA(cudaEventCreate(&e1));
+    auto trial = [&](float& ms) -> rp_status {
+        rp_status r = rp_state_set(w, saved.data());
+        if (r == RP_OK) r = rp_simulate(w, dt, substeps, iters, collisions, 1);   // warm-up, graph capture
+        if (r != RP_OK) return r;
+        if (cudaEventRecord(e0, w->stream) != cudaSuccess) return fail(RP_ERR_CUDA, "event");
+        r = rp_simulate(w, dt, substeps, iters, collisions, frames);
+        if (r != RP_OK) return r;
+        if (cudaEventRecord(e1, w->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+            return fail(RP_ERR_CUDA, "event timing");
+        return RP_OK;
+    };
+    auto set_tune = [&](int mode, int group, int cta, int solo) {
+        w->mode = mode;
+        w->pipe.transform_group = group;
+        w->pipe.sweep_cta = cta;
+        w->solo_nodes = solo;
+        w->layout_gen++;   // recapture the frame graph with the new launch shapes
+    };
+    int best[4] = {RP_MODE_PHASED, 8, 0, 512};
+    float best_ms = 0.f;
+    auto consider = [&](int mode, int group, int cta, int solo) -> rp_status {
+        set_tune(mode, group, cta, solo);
+        float ms = 0.f;
+        rp_status r = trial(ms);
+        if (r != RP_OK) return r;
+        if (best_ms == 0.f || ms < best_ms) {
+            best_ms = ms;
+            best[0] = mode; best[1] = group; best[2] = cta; best[3] = solo;
+        }
+        return RP_OK;
+    };
+    // coordinate search: launch mode, then the hull-transform group, then the sweep layout
+    s = consider(RP_MODE_PHASED, 8, 0, 512);
+    if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, 0, 512);
+    if (s == RP_OK && best[0] == RP_MODE_PHASED) {
+        for (int g : {4, 16, 32})
+            if (s == RP_OK) s = consider(RP_MODE_PHASED, g, 0, 512);
+        const int g = best[1];
+        if (w->grid_mode) {
+            for (int solo : {128, 256, 1024, 2048})
+                if (s == RP_OK) s = consider(RP_MODE_PHASED, g, 0, solo);
+        } else if (s == RP_OK) {
+            s = consider(RP_MODE_PHASED, g, 1, 512);
+        }
+    } else if (s == RP_OK && w->grid_mode) {
+        for (int solo : {128, 256, 1024, 2048})
+            if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, 0, solo);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_tune(best[0], best[1], best[2], best[3]);
+    rp_status r = rp_state_set(w, saved.data());
+    w->steps = steps0;
+    w->substeps = substeps0;
+    w->status_accum = status0;
+    for (int k = 0; k < 4; ++k) choice[k] = best[k];
+    return s != RP_OK ? s : r;
 }
 
 rp_status rp_world_set_mode(rp_world* w, int32_t mode) {

@@ -176,21 +176,19 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
     if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; }
 }
 
-// Eight threads per collider: the typical hull has 8-64 vertices, so a whole warp per collider
-// would leave most lanes idle.
-constexpr int TRANSFORM_GROUP = 8;
-
+// `group` threads per collider (a power of two up to 32; 8 by default: the typical hull has 8-64
+// vertices, so a whole warp per collider would leave most lanes idle).
 template <typename R, bool EXACT>
-__global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int ncolliders, int include_fixed) {
-    const int sub = threadIdx.x % TRANSFORM_GROUP;
-    const int gi = (blockIdx.x * blockDim.x + threadIdx.x) / TRANSFORM_GROUP;
-    const int ng = (gridDim.x * blockDim.x) / TRANSFORM_GROUP;
+__global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int ncolliders, int include_fixed, int group) {
+    const int sub = threadIdx.x % group;
+    const int gi = (blockIdx.x * blockDim.x + threadIdx.x) / group;
+    const int ng = (gridDim.x * blockDim.x) / group;
     for (int ci = gi; ci < ncolliders; ci += ng) {
         const Collider col = W.colliders[ci];
         if (col.type != COL_HULL) continue;
         const int b = W.col_body[ci];
         if (W.fixed[b] && !include_fixed) continue;
-        transform_collider<R, EXACT>(W, col, b, sub, TRANSFORM_GROUP);
+        transform_collider<R, EXACT>(W, col, b, sub, group);
     }
 }
 
@@ -519,7 +517,7 @@ struct PipeLauncher {
         };
         const double h = P.dt / P.num_substeps;
         const int body_blocks = (d.nbodies + d.next + PIPE_BLOCK - 1) / PIPE_BLOCK + 1;
-        const int col_blocks = (d.ncolliders * TRANSFORM_GROUP + PIPE_BLOCK - 1) / PIPE_BLOCK + 1;
+        const int col_blocks = (d.ncolliders * c.transform_group + PIPE_BLOCK - 1) / PIPE_BLOCK + 1;
         if ((e = mark(-1)) != cudaSuccess) return e;
         if (d.grid_mode) e = coop(k_setup_grid<R>, c.setup_grid_blocks, BLOCK, st, W, P.dt);
         else k_setup_cta<R><<<d.num_scenes, BLOCK, 0, st>>>(W, P.dt), e = cudaGetLastError();
@@ -528,7 +526,7 @@ struct PipeLauncher {
             k_predict<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, d.next, h);
             if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_PREDICT)) != cudaSuccess) return e;
             if (P.enable_collisions) {
-                k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0);
+                k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0, c.transform_group);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
             }
             k_cull<R><<<c.cull_blocks, PIPE_BLOCK, 0, st>>>(W, P.enable_collisions);
@@ -544,6 +542,7 @@ struct PipeLauncher {
             if ((e = mark(PH_NARROW)) != cudaSuccess) return e;
             for (int it = 0; it < P.num_pos_iters; ++it) {
                 if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, false>, c.sweep_grid_blocks, BLOCK, st, W, h);
+                else if (c.sweep_cta) k_sweep_cta<R, EXACT, false><<<d.num_scenes, BLOCK, 0, st>>>(W, h), e = cudaGetLastError();
                 else e = sweep_warp<false>(W, c, st, h);
                 if (e != cudaSuccess) return e;
             }
@@ -551,6 +550,7 @@ struct PipeLauncher {
             k_velocity<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, h);
             if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_VELOCITY)) != cudaSuccess) return e;
             if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, true>, c.vsweep_grid_blocks, BLOCK, st, W, h);
+            else if (c.sweep_cta) k_sweep_cta<R, EXACT, true><<<d.num_scenes, BLOCK, 0, st>>>(W, h), e = cudaGetLastError();
             else e = sweep_warp<true>(W, c, st, h);
             if (e != cudaSuccess || (e = mark(PH_VSOLVE)) != cudaSuccess) return e;
         }

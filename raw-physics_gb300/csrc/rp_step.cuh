@@ -751,14 +751,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // levels that each hold at most SOLO_NODES nodes is swept by CTA 0 alone, separated by
 // __syncthreads, while the other CTAs wait at one grid barrier: the dependent chain of small levels
 // then costs a block barrier per level instead of a grid barrier. Larger levels use the whole grid.
-constexpr int SOLO_NODES = 2 * BLOCK;
+constexpr int SOLO_NODES = 2 * BLOCK;   // default of WorldView::solo_nodes
 
 template <typename R, bool EXACT, bool VELOCITY, class G>
 __device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, int L, const int* lstart, int nbase, R hR) {
+    const int solo = W.solo_nodes > 0 ? W.solo_nodes : SOLO_NODES;
     int l = 0;
     while (l < L) {
         int cnt = lstart[l + 1] - lstart[l];
-        if (g.nblocks() == 1 || cnt > SOLO_NODES) {
+        if (g.nblocks() == 1 || cnt > solo) {
             for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size()) {
                 if (VELOCITY) vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
                 else solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
@@ -768,7 +769,7 @@ __device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, int L, co
             continue;
         }
         int l2 = l;
-        while (l2 < L && lstart[l2 + 1] - lstart[l2] <= SOLO_NODES) ++l2;
+        while (l2 < L && lstart[l2 + 1] - lstart[l2] <= solo) ++l2;
         if (g.block() == 0) {
             for (int k = l; k < l2; ++k) {
                 for (int i = lstart[k] + (int)threadIdx.x; i < lstart[k + 1]; i += blockDim.x) {

@@ -164,6 +164,7 @@ struct WorldView {
                                  //     [2] gjk_list length, [3] hit_list length
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
     int32_t max_colliders_per_body;
+    int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
     // ---- control ----------------------------------------------------------------------------
     uint32_t* status;        // [S] status bits per scene
     unsigned int* barrier;   // [2] grid barrier counter / generation

@@ -69,6 +69,7 @@ SIGNATURES = {
     "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_counters": (_i, [_W, _P(_u64)]),
     "rp_world_set_mode": (_i, [_W, _i]),
+    "rp_autotune": (_i, [_W, _d, _u, _u, _i, _u, _P(_i)]),
     "rp_kernel_launches": (_u64, [_W]),
     "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
     "rp_phase_times": (_i, [_W, _P(_d)]),
@@ -351,6 +352,17 @@ class World:
         """Launch mode of a frame: "phased" (one kernel per phase, CUDA graph), "persistent" (one
         kernel per frame) or "auto"."""
         self._check(self.lib.rp_world_set_mode(self.h, self.MODES[mode]))
+
+    def autotune(self, frames: int = 3) -> dict:
+        """Pick the fastest launch configuration for the loaded scenes (results are identical under
+        every configuration); returns the choice."""
+        s = self.scene
+        out = (_i * 4)()
+        self._check(self.lib.rp_autotune(self.h, float(s.dt), int(s.substeps), int(s.pos_iters), int(bool(s.collisions)),
+                                         int(frames), out))
+        modes = {v: k for k, v in self.MODES.items()}
+        return {"mode": modes.get(out[0], out[0]), "transform_threads": out[1], "cta_per_scene_sweeps": bool(out[2]),
+                "solo_level_nodes": out[3]}
 
     def counters(self):
         out = (C.c_uint64 * 20)()

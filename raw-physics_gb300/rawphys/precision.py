@@ -45,15 +45,30 @@ def precision_report(rawphys, batch, frames: int = 300, sample_every: int = 50, 
     s0 = w64.get_state()
     e0 = {p: energies(batch, s0, inertia, g) for p in worlds}
     top = np.array([np.max(np.nonzero(batch.scene == s)[0]) for s in range(batch.num_scenes)])
-    step_pos, step_rot, at, done = [], [], [], 0
+    rng = np.random.default_rng(0)
+    step_pos, step_rot, spread, at, done = [], [], [], [], 0
     while done < frames:
         if done % sample_every == 0:
             at.append(done)
-            # one FP32 frame from the FP64 trajectory's state, against the FP64 frame
-            w32.set_state(w64.get_state())
-            w32.step(1)
+            st = w64.get_state()
+            # the FP64 build's own response to FP32-scale noise (1e-7 m, 1e-7 relative) on this
+            # frame's input: the floor below which no FP32 implementation can agree
+            sp = 0.0
             w64.step(1)
-            pe, re = pose_error(w32.get_state(), w64.get_state())
+            ref = w64.get_state()
+            for _ in range(2):
+                p = st.copy()
+                p[:, 0:3] += 1e-7 * rng.standard_normal(p[:, 0:3].shape)
+                p[:, 3:7] *= 1.0 + 1e-7 * rng.standard_normal(p[:, 3:7].shape)
+                w64.set_state(p)
+                w64.step(1)
+                sp = max(sp, max(pose_error(w64.get_state(), ref)))
+            spread.append(sp)
+            # one FP32 frame from the FP64 trajectory's state, against the FP64 frame
+            w32.set_state(st)
+            w32.step(1)
+            w64.set_state(ref)
+            pe, re = pose_error(w32.get_state(), ref)
             step_pos.append(pe)
             step_rot.append(re)
             done += 1
@@ -77,7 +92,8 @@ def precision_report(rawphys, batch, frames: int = 300, sample_every: int = 50, 
     return {"frames": frames, "scenes": batch.num_scenes, "bodies": int(dyn.sum()), "substeps": batch.substeps,
             "step_pos_err_fp32_vs_fp64": {"median": float(np.median(step_pos)), "max": float(np.max(step_pos))},
             "step_rot_err_fp32_vs_fp64": {"median": float(np.median(step_rot)), "max": float(np.max(step_rot))},
-            "step_err_by_frame": [[f, p, r] for f, p, r in zip(at, step_pos, step_rot)],
+            "step_err_by_frame": [[f, p, r, n] for f, p, r, n in zip(at, step_pos, step_rot, spread)],
+            "step_err_by_frame_columns": ["frame", "pos err m", "rot err", "FP64 spread under 1e-7 input noise"],
             "trajectory_divergence_m": {"median": float(np.median(div)), "max": float(np.max(div))},
             "top_body_horizontal_drift_m": tower_drift,
             "relative_energy_drift": drift,

@@ -347,3 +347,23 @@ def test_batched_form_fp32_per_step_error(ext_built, oracle_built):
         errs.append(float(np.max(np.abs(o.get_state()[:, 0:3] - nxt[idx, 0:3]))))
     assert np.median(errs) <= 1e-4, errs
     w.close()
+
+
+def test_autotune_keeps_results_and_state(ext_built, oracle_built):
+    """rp_autotune times every launch configuration from the current state, restores it, and the
+    chosen configuration gives the oracle's results bit for bit (FP64 build)."""
+    from rawphys import scenes as S
+    for sc in (S.random_pile_scene(10, seed=12), S.large_scene(1024, seed=1)):
+        w = ext_built.World(0, "fp64")
+        w.load(sc)
+        w.step(2)
+        st = w.get_state()
+        choice = w.autotune(frames=2)
+        assert choice["mode"] in ("phased", "persistent")
+        assert np.array_equal(w.get_state(), st)
+        w.step(3)
+        o = oracle_built("port").load(sc)
+        o.set_state(st)
+        o.step(3)
+        assert np.array_equal(w.get_state(), o.get_state()), (sc.name, choice)
+        w.close()
