@@ -204,6 +204,18 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out_pairs, uint32
 /* colliders_update + colliders_get_contacts for one entity pair on the current state, computed by
  * the device narrowphase. out: RP_CONTACT_DOUBLES per contact. */
 rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
+/* rp_contacts without any allocation: no cudaMalloc / cudaFree and no host heap allocation in the
+ * call. For callers that must not allocate mid-frame: a render or debug thread drawing contact
+ * points while the simulation thread holds the device (a device allocation synchronises the whole
+ * device and stalls it), or a caller with a fixed memory budget. The contacts are computed into a
+ * static device scratch of at most 64 contacts and copied into out; cap > 64 is rejected with
+ * RP_ERR_CAPACITY, a pair with more contacts reports its full count with the first cap written. The
+ * world must already be built on the device (it has been stepped), else RP_ERR_STATE. The first call
+ * on a device looks up the scratch's address (set-up) and should come before any stream capture.
+ * Calls on the same device must not overlap: they share the scratch. No counterpart in the
+ * reference. */
+#define RP_NOALLOC_MAX_CONTACTS 64
+rp_status rp_contacts_noalloc(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
 /* The collision constraints of the last substep of the last rp_simulate call, in the reference's
  * constraint order (pairs in broad-phase order, contacts in manifold order): entity pairs (2 per
  * contact) and 11 doubles per contact: r1_lc[3], r2_lc[3], normal[3], lambda_n, lambda_t

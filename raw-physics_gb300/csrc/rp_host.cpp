@@ -1400,6 +1400,37 @@ rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t
     return RP_OK;
 }
 
+rp_status rp_contacts_noalloc(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count) {
+    if (check_world(w) || e1 < 0 || e2 < 0 || e1 >= (int32_t)w->bodies.size() || e2 >= (int32_t)w->bodies.size() || e1 == e2)
+        return fail(RP_ERR_INVALID, "bad entity");
+    if (!out || !count) return fail(RP_ERR_INVALID, "null argument");
+    if (cap > (uint32_t)NOALLOC_MAX_CONTACTS)
+        return fail(RP_ERR_CAPACITY, "rp_contacts_noalloc: cap exceeds the static scratch (64 contacts per call)");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
+    if (w->static_dirty || !w->device_state_valid || !w->d_pos.p)
+        return fail(RP_ERR_STATE, "rp_contacts_noalloc: the device world is not built; step the world (rp_simulate) first");
+    RP_CUDA(cudaSetDevice(w->device));
+    double* scratch = nullptr;
+    int* d_count = nullptr;
+    RP_CUDA(noalloc_scratch(w->device, &scratch, &d_count));
+    const int a = w->bodies[(size_t)e1].slot, b = w->bodies[(size_t)e2].slot;
+    if (w->precision == RP_PRECISION_FP64)
+        RP_CUDA(contacts_f64(make_view<double>(w), a, b, scratch, NOALLOC_MAX_CONTACTS, d_count, w->stream));
+    else
+        RP_CUDA(contacts_f32(make_view<float>(w), a, b, scratch, NOALLOC_MAX_CONTACTS, d_count, w->stream));
+    w->launches++;
+    int n = 0;
+    RP_CUDA(cudaMemcpyAsync(&n, d_count, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    const int m = std::min(std::min(n, NOALLOC_MAX_CONTACTS), (int)cap);
+    if (m > 0) {
+        RP_CUDA(cudaMemcpyAsync(out, scratch, (size_t)m * 9 * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaStreamSynchronize(w->stream));
+    }
+    *count = (uint32_t)n;
+    return RP_OK;
+}
+
 rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, double* out, uint32_t cap, uint32_t* count) {
     if (check_world(w) || scene < 0 || scene >= w->num_scenes) return fail(RP_ERR_INVALID, "bad argument");
     if (w->device < 0 || !w->d_pair_count.p || w->static_dirty) return fail(RP_ERR_STATE, "no step has run");

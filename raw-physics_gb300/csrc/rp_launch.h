@@ -38,6 +38,10 @@ struct PipeMarks {
                                  cudaStream_t st, PipeMarks* marks);                                          \
     int pipe_launches_##SUF(const StepParams& P);
 
+// No-allocation contact query: contacts per call held by its static device scratch (rp_noalloc.cu).
+constexpr int NOALLOC_MAX_CONTACTS = 64;
+cudaError_t noalloc_scratch(int device, double** contacts, int** count);
+
 RP_DECLARE_LAUNCHERS(f32, float)
 RP_DECLARE_LAUNCHERS(f64, double)
 #undef RP_DECLARE_LAUNCHERS

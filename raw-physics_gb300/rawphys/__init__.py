@@ -74,6 +74,7 @@ SIGNATURES = {
     "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
     "rp_phase_times": (_i, [_W, _P(_d)]),
     "rp_last_contacts": (_i, [_W, _i, _P(_i), _P(_d), _u, _P(_u)]),
+    "rp_contacts_noalloc": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_set_timing": (_i, [_W, _i]),
     "rp_last_step_ms": (_i, [_W, _P(_d)]),
 }
@@ -335,6 +336,13 @@ class World:
         n = _u()
         self._check(self.lib.rp_contacts(self.h, e1, e2, _dp(out), cap, C.byref(n)))
         return out[: min(n.value, cap) * CONTACT_DOUBLES].reshape(-1, CONTACT_DOUBLES)
+
+    def contacts_noalloc(self, e1: int, e2: int, cap: int = 64) -> np.ndarray:
+        """rp_contacts through the no-allocation entry point (static device scratch)."""
+        out = np.zeros(max(cap, 1) * 9)
+        n = _u()
+        self._check(self.lib.rp_contacts_noalloc(self.h, e1, e2, _dp(out), cap, C.byref(n)))
+        return out[: min(n.value, cap) * 9].reshape(-1, 9)
 
     def last_contacts(self, scene: int = 0):
         """(pairs (k,2), constraints (k,11)) of the last substep of the last simulate call."""

@@ -1,0 +1,45 @@
+"""rp_contacts_noalloc (static device scratch, no allocation in the call) against rp_contacts on every
+broad-phase pair of a settled pile pressed 3 mm into its supports, two calls in a row each: identical contacts in both builds. Kept
+in its own file, collected last, so it runs after every other GPU test as well as alone."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_noalloc_contacts_match_rp_contacts(ext_built, precision):
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(14, seed=21)
+    w = ext_built.World(0, precision)
+    w.load(sc)
+    w.step(40)
+    st = w.get_state()
+    st[~sc.fixed, 1] -= 0.003          # resting bodies pushed 3 mm into their supports: contacts exist
+    w.set_state(st)
+    pairs = w.broad_pairs()
+    assert len(pairs) > 0
+    seen = 0
+    for a, b in pairs:
+        ref = w.contacts(int(a), int(b))
+        for _ in range(2):
+            got = w.contacts_noalloc(int(a), int(b))
+            assert np.array_equal(got, ref), (precision, a, b)
+        seen += len(ref) > 0
+    assert seen > 0, "no pair in contact"
+    w.close()
+
+
+def test_noalloc_rejects_cap_beyond_scratch_and_unbuilt_world(ext_built):
+    from rawphys import scenes as S
+    sc = S.random_pile_scene(4, seed=2)
+    w = ext_built.World(0, "fp32")
+    w.load(sc)
+    with pytest.raises(ext_built.RPError, match="not built"):
+        w.contacts_noalloc(0, 1)
+    w.step(1)
+    with pytest.raises(ext_built.RPError, match="static scratch"):
+        w.contacts_noalloc(0, 1, cap=65)
+    w.close()
