@@ -229,8 +229,10 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
  * [13] pairs skipped because their bounding box and sphere are certainly apart, [14] GJK cycles,
  * [15] EPA cycles, [16] contact-manifold cycles (summed over calls), [17] GJK cycles spent in
  * support mapping, [18] GJK runs ended early on a repeated state (they would have reached the
- * iteration cap and returned no collision), [19] reserved (0). */
-#define RP_NUM_COUNTERS 20
+ * iteration cap and returned no collision), [19] EPA set-up cycles (hull staging, simplex load),
+ * [20] EPA support-mapping cycles, [21] manifold set-up cycles, [22] contact write-out cycles,
+ * [23] reserved (0). Cycle counters of the phase-major kernels are summed per warp. */
+#define RP_NUM_COUNTERS 24
 rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */
 uint64_t  rp_kernel_launches(const rp_world* w);

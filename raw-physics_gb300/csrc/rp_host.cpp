@@ -1486,6 +1486,7 @@ rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]) {
         out[5] = c[3]; out[6] = c[5]; out[7] = c[6];
         out[8] = c[4]; out[9] = c[7]; out[10] = c[8]; out[11] = c[9]; out[12] = c[10]; out[13] = c[11];
         out[14] = c[12]; out[15] = c[13]; out[16] = c[14]; out[17] = c[15]; out[18] = c[16];
+        out[19] = c[17]; out[20] = c[18]; out[21] = c[19]; out[22] = c[20];
     }
     out[3] = w->steps;
     out[4] = w->substeps;

@@ -565,7 +565,7 @@ __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, u
 
 template <typename R>
 __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView<R>& c2, const Simplex<R>& s,
-                         V3<double>& out_n, double& out_pen, int& iters) {
+                         V3<double>& out_n, double& out_pen, int& iters, long long* support_cycles = nullptr) {
     static_assert(sizeof(EpaFastSmem<R>) <= sizeof(typename NarrowSmem<R>::U), "EPA scratch must fit the union");
     EpaFastSmem<R>& sm = *reinterpret_cast<EpaFastSmem<R>*>(&smr.u);
     const unsigned lane = lane_id();
@@ -595,7 +595,9 @@ __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView
     for (int it = 0; it < 100; ++it) {
         iters = it + 1;
         V3<float> min_n = mi == 0x7fffffff ? v3<float>(0.f, 0.f, 0.f) : sm.fn[mi];
+        const long long ts = clock64();
         V3<float> sp = v3cast<float>(support_mink(c1, c2, v3cast<R>(min_n)));
+        if (support_cycles) *support_cycles += clock64() - ts;
         // Termination test (epa.cpp:153-160) with the FP64 outcome: |<n, s> - d| < 1e-4 for the
         // closest face. FP32 decides it when the FP32 gap is farther from 1e-4 than its error bound
         // (the face normal's error grows with the face's conditioning |e1||e2| / |e1 x e2|);
@@ -757,10 +759,15 @@ __device__ __forceinline__ bool plane_edge(V3<R> pn, V3<R> pp, V3<R> start, V3<R
     return false;
 }
 
-// One Sutherland–Hodgman pass against one plane, one lane per polygon edge. Returns the output count.
+// One Sutherland–Hodgman pass against one plane, one lane per polygon edge. Returns the output count,
+// or -1 when every vertex lies inside the plane: the pass would then emit its input unchanged and in
+// order (each edge emits its end point), so the caller keeps the input buffer.
 template <typename R>
 __device__ int sh_pass(const V3<R>* in, int n, V3<R>* out, V3<R> pn, V3<R> pp, bool remove_only, int& status) {
     const unsigned lane = lane_id();
+    bool all_in = true;
+    for (int j = (int)lane; j < n; j += WARP) all_in = all_in && in_plane(pn, pp, in[j]);
+    if (__all_sync(0xffffffffu, all_in)) return -1;
     int carry = 0;
     for (int base = 0; base < n; base += WARP) {
         int j = base + (int)lane;
@@ -935,14 +942,14 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
     int n = ninc, cur = 0;
     for (int p = 0; p < npl; ++p) {
         if (n == 0) break;
-        n = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], sm.u.clip.pn[p], sm.u.clip.pp[p], false, st);
-        cur ^= 1;
+        const int m = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], sm.u.clip.pn[p], sm.u.clip.pp[p], false, st);
+        if (m >= 0) { n = m; cur ^= 1; }
     }
     V3<R> ref_n = vinv(rh.norms[rf]);
     V3<R> ref_p = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + rf]]);
     if (n > 0) {
-        n = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], ref_n, ref_p, true, st);
-        cur ^= 1;
+        const int m = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], ref_n, ref_p, true, st);
+        if (m >= 0) { n = m; cur ^= 1; }
     }
     if (st && lane == 0) atomicOr(&sm.status, (int)st);
     // contacts from the kept points (clipping.cpp:302-327)

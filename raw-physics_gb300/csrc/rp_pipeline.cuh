@@ -323,6 +323,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             const int2 pr = W.pairs[gp];
             const int a = pr.x, b = pr.y;
             if (lane == 0) { sm.status = 0; }
+            const long long tv = clock64();
             ColView<R> va, vb;
             PairFrame<R, EXACT> fr;
             single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
@@ -337,11 +338,15 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             double pen = 0.0;
             int ei = 0;
             const long long t0 = clock64();
-            const bool ok = (EXACT || !kEpaFast) ? epa(sm, va, vb, sx, nrm, pen, ei) : epa_fast(sm, va, vb, sx, nrm, pen, ei);
+            long long tsup = 0;
+            const bool ok = (EXACT || !kEpaFast) ? epa(sm, va, vb, sx, nrm, pen, ei)
+                                                 : epa_fast(sm, va, vb, sx, nrm, pen, ei, &tsup);
             t.v[0] += ei;
             t.v[1] += 1;
             t.v[2] += clock64() - t0;
             t.v[3] += ei >= 100;
+            t.v[4] += t0 - tv;
+            t.v[5] += tsup;
             const int s = W.body_scene[a];
             if (lane == 0) {
                 if (!ok) atomicOr(&W.status[s], (uint32_t)ST_EPA_NOT_CONVERGED);
@@ -359,7 +364,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             __syncwarp();
         }
     }
-    const int slots[8] = {1, 2, 13, 7, -1, -1, -1, -1};
+    const int slots[8] = {1, 2, 13, 7, 17, 18, -1, -1};
     t.flush(W.counters, slots);
 }
 
@@ -381,6 +386,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
             const int a = pr.x, b = pr.y;
             const int s = W.body_scene[a];
             const long long t0 = clock64();
+            long long t1 = t0;
             if (st == WS_GENERAL) {
                 pair_contacts<R, EXACT>(W, sm, a, b, false);
             } else {
@@ -391,13 +397,17 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
                 single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
                 const double* e = W.work_epa + 4 * (size_t)k;
                 const V3<double> n64 = v3<double>(e[0], e[1], e[2]);
+                t1 = clock64();
                 contact_manifold<R, EXACT>(sm, W, va, vb, v3cast<R>(n64), n64, (R)e[3], fr);
             }
-            t.v[1] += clock64() - t0;
+            const long long t2 = clock64();
+            t.v[1] += t2 - t0;
+            t.v[2] += t1 - t0;
             emit_contacts(W, sm, s, gp, t.v[0]);
+            t.v[3] += clock64() - t2;
         }
     }
-    const int slots[8] = {3, 14, -1, -1, -1, -1, -1, -1};
+    const int slots[8] = {3, 14, 19, 20, -1, -1, -1, -1};
     t.flush(W.counters, slots);
 }
 

@@ -373,7 +373,7 @@ class World:
                 "solo_level_nodes": out[3]}
 
     def counters(self):
-        out = (C.c_uint64 * 20)()
+        out = (C.c_uint64 * 24)()
         self._check(self.lib.rp_counters(self.h, out))
         return list(out)
 
