@@ -87,7 +87,27 @@ rp_status rp_world_create(rp_world** out, int32_t device, int32_t precision);
 void      rp_world_destroy(rp_world* w);
 /* Use an existing cudaStream_t (passed as void*) for every launch and copy of this world. */
 rp_status rp_world_set_stream(rp_world* w, void* cuda_stream);
-/* Selects the launch mode (RP_MODE_*); no counterpart in the reference. */
+/* Adjoint of the step (no counterpart in the reference): for every scene, the loss
+ * |x_e(T) - target|^2 of one entity e = loss_entity[scene] after `frames` frames (dt, substeps,
+ * iterations and enable_collisions as rp_simulate, gravity as set, no other forces) and its gradient
+ * with respect to every entity's initial linear and angular velocity (grad_v, grad_w: 3 doubles per
+ * entity), mass (grad_mass) and static / dynamic friction (grad_friction, 2 per entity, may be NULL).
+ * Everything the step does is differentiated: free motion, the external joints (positional, mutual
+ * orientation, hinge, spherical, limits included) and, with collisions, hull-hull contacts (the EPA
+ * normal and clipped contact points as functions of the poses, the normal and static-friction
+ * solves, the velocity solver with dynamic friction and restitution). Discrete events are held
+ * fixed: the broad-phase pairs and awake bodies of every frame, every branch (a limit or a contact
+ * acting, static friction holding), the support features GJK, EPA and the clipping select; the
+ * clipping's float roundings are differentiated as identity. Static friction only enters through a
+ * comparison, so its gradient is zero. Scenes whose contact pairs involve sphere colliders report
+ * RP_ERR_INVALID with collisions on. The forward pass is the all-FP64 step: its loss equals the FP64
+ * build's. Reverse mode over a tape, one scene per GPU thread, with the trajectory checkpointed
+ * every `checkpoint_every` frames and recomputed segment by segment. Starts from the world's current
+ * state, which it does not change. target: 3 doubles per scene. */
+rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t num_substeps, uint32_t num_pos_iters,
+                                int32_t enable_collisions, uint32_t frames, uint32_t checkpoint_every,
+                                const int32_t* loss_entity, const double* target, double* loss_out, double* grad_v,
+                                double* grad_w, double* grad_mass, double* grad_friction);
 rp_status rp_world_set_mode(rp_world* w, int32_t mode);
 /* Autotuner (no counterpart in the reference): times `frames` frames of the world's current scenes
  * from their current state under each candidate launch configuration — launch mode, threads per

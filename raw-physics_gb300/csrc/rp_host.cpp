@@ -119,6 +119,8 @@ struct rp_world {
         d_counters, d_phase, d_kat_out, d_kat_count;
 
     // phase-major pipeline
+    DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
+    double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
@@ -1596,6 +1598,313 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
     w->status_accum = status0;
     for (int k = 0; k < 4; ++k) choice[k] = best[k];
     return s != RP_OK ? s : r;
+}
+
+rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t substeps, uint32_t iters, int32_t collisions,
+                                uint32_t frames, uint32_t checkpoint_every, const int32_t* loss_entity, const double* target,
+                                double* loss_out, double* grad_v, double* grad_w, double* grad_mass, double* grad_friction) {
+    if (check_world(w) || !loss_entity || !target || !loss_out || !grad_v || !grad_w || !grad_mass)
+        return fail(RP_ERR_INVALID, "null argument");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
+    if (!(dt > 0.0) || substeps == 0 || iters == 0 || frames == 0 || checkpoint_every == 0)
+        return fail(RP_ERR_INVALID, "bad step arguments");
+    for (const HostBody& b : w->bodies)
+        if (!b.forces.empty()) return fail(RP_ERR_STATE, "the adjoint covers gravity only: clear the pending forces");
+    RP_CUDA(cudaSetDevice(w->device));
+    rp_status st = ensure_device(w);   // slots, the scene layout and the geometry
+    if (st != RP_OK) return st;
+    if (w->device_state_valid) {
+        st = sync_state_to_host(w);
+        if (st != RP_OK) return st;
+    }
+    const int S = w->num_scenes;
+    for (int s = 0; s < S; ++s) {
+        const int e = loss_entity[s];
+        if (e < 0 || e >= (int)w->bodies.size() || w->bodies[(size_t)e].scene != s)
+            return fail(RP_ERR_INVALID, "loss entity must belong to its scene");
+    }
+    // host copies by slot: start states, mass properties, materials, sleeping state
+    const size_t N = w->bodies.size();
+    std::vector<double> start(13 * N), invm(N), I6(6 * N), Ii6(6 * N), mat(3 * N), pvel(6 * N), deact(N);
+    std::vector<uint8_t> fixedv(N), activev(N);
+    std::vector<int> tv_of(N + 1, 0), tn_of(N + 1, 0);   // transformed vertices / normals before each slot
+    const int sym[6] = {0, 4, 8, 1, 2, 5};
+    for (size_t slot = 0; slot < N; ++slot) {
+        const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
+        double* o = &start[13 * slot];
+        for (int k = 0; k < 3; ++k) { o[k] = b.pos[k]; o[7 + k] = b.v[k]; o[10 + k] = b.w[k]; }
+        for (int k = 0; k < 4; ++k) o[3 + k] = b.rot[k];
+        invm[slot] = b.invm;
+        for (int k = 0; k < 6; ++k) { I6[6 * slot + (size_t)k] = b.I[sym[k]]; Ii6[6 * slot + (size_t)k] = b.Iinv[sym[k]]; }
+        mat[3 * slot] = b.mus;
+        mat[3 * slot + 1] = b.mud;
+        mat[3 * slot + 2] = b.rest;
+        for (int k = 0; k < 3; ++k) { pvel[6 * slot + (size_t)k] = b.pv[k]; pvel[6 * slot + 3 + (size_t)k] = b.pw[k]; }
+        deact[slot] = b.deact;
+        activev[slot] = b.active != 0.0 ? 1 : 0;
+        fixedv[slot] = (uint8_t)b.fixed;
+        int nv = 0, nf = 0;
+        for (const rp_collider_desc& d : b.cols) {
+            if (d.type != RP_COLLIDER_HULL) continue;
+            nv += w->hulls[(size_t)d.hull]->nv();
+            nf += w->hulls[(size_t)d.hull]->nf();
+        }
+        tv_of[slot + 1] = tv_of[slot] + nv;
+        tn_of[slot + 1] = tn_of[slot] + nf;
+    }
+    std::vector<ExtConstraint> ext;
+    std::vector<int> ext_start((size_t)S + 1, 0);
+    for (int s = 0; s < S; ++s) {
+        ext_start[(size_t)s] = (int)ext.size();
+        for (const HostExt& x : w->exts) {
+            if (x.scene != s) continue;
+            ExtConstraint c = x.c;
+            c.e1 = w->bodies[(size_t)c.e1].slot;
+            c.e2 = w->bodies[(size_t)c.e2].slot;
+            ext.push_back(c);
+        }
+    }
+    ext_start[(size_t)S] = (int)ext.size();
+    const size_t K = checkpoint_every;
+    const size_t body_d = adjoint_body_bytes(false), body_a = adjoint_body_bytes(true), var = adjoint_var_bytes();
+    const size_t con_d = adjoint_contact_bytes(false), con_a = adjoint_contact_bytes(true);
+    const size_t clip_d = adjoint_clip_bytes(false), clip_a = adjoint_clip_bytes(true), epa = adjoint_epa_bytes();
+    struct Off {
+        size_t ckpt, seg, work, deact, active, aseg, pairs, npairs, uf, awake, stamp, tvd, tnd, tva, tna, tvv, tnv, cond, cona,
+            clipd, clipa, epa, grad, ginv, gmu, loss, status, prof, bd, ba, lamd, lama, tab, td, tadj;
+        int cap, pcap, ccap;
+    };
+    std::vector<Off> off((size_t)S);
+    // the tape of one substep: bodies, joints, and with collisions the hull transforms, narrowphase
+    // and contact solves; an overflow doubles it and runs again
+    size_t tape_scale = 1;
+    rp_status result = RP_OK;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        size_t total = 0;
+        auto take = [&](size_t bytes) { size_t o = total; total += (bytes + 255) & ~(size_t)255; return o; };
+        for (int s = 0; s < S; ++s) {
+            const int b0 = w->scene_body[(size_t)s];
+            const size_t nb = (size_t)(w->scene_body[(size_t)s + 1] - b0);
+            const size_t ne = (size_t)(ext_start[(size_t)s + 1] - ext_start[(size_t)s]);
+            const size_t ntv = (size_t)(tv_of[(size_t)b0 + nb] - tv_of[(size_t)b0]);
+            const size_t ntn = (size_t)(tn_of[(size_t)b0 + nb] - tn_of[(size_t)b0]);
+            const size_t stride = 13 * nb * 8;
+            Off& o = off[(size_t)s];
+            o.pcap = (int)std::min<size_t>(nb * (nb - 1) / 2 + 1, 16 * nb + 64);
+            o.ccap = collisions ? (int)(32 * nb + 256) : 1;
+            const size_t cap = (600 * nb + 2500 * ne * iters + (collisions ? 8000 * nb * iters : 0) + 4096) * tape_scale;
+            o.cap = (int)std::min<size_t>((size_t)1 << 30, cap);
+            o.ckpt = take(((frames + K - 1) / K + 1) * 15 * nb * 8);
+            o.seg = take((K * substeps + 1) * stride);
+            o.work = take(stride);
+            o.deact = take(nb * 8);
+            o.active = take(nb);
+            o.aseg = take(K * nb);
+            o.pairs = take(K * (size_t)o.pcap * 8);
+            o.npairs = take(K * 4);
+            o.uf = take(nb * 4);
+            o.awake = take(nb);
+            o.stamp = take(nb * 4);
+            o.tvd = take(ntv * 24 + 8);
+            o.tnd = take(ntn * 24 + 8);
+            o.tva = take(ntv * 3 * var + var);
+            o.tna = take(ntn * 3 * var + var);
+            o.tvv = take(ntv * 24 + 8);
+            o.tnv = take(ntn * 24 + 8);
+            o.cond = take((size_t)o.ccap * con_d);
+            o.cona = take((size_t)o.ccap * con_a);
+            o.clipd = take(collisions ? clip_d : 8);
+            o.clipa = take(collisions ? clip_a : 8);
+            o.epa = take(collisions ? epa : 8);
+            o.grad = take(stride);
+            o.ginv = take(nb * 8);
+            o.gmu = take(2 * nb * 8);
+            o.loss = take(8);
+            o.status = take(8);
+            o.prof = take(6 * 8);
+            o.bd = take(nb * body_d);
+            o.ba = take(nb * body_a);
+            o.lamd = take(4 * ne * 8 + 8);
+            o.lama = take(4 * ne * var + var);
+            o.tab = take((size_t)o.cap * 8);
+            o.td = take((size_t)o.cap * 16);
+            o.tadj = take((size_t)o.cap * 8);
+        }
+        const size_t inputs = (13 + 1 + 12 + 3 + 6 + 1) * N * 8 + 2 * N + 256;
+        RP_CUDA(w->d_adj_data.ensure(total + inputs + 1024));
+        RP_CUDA(w->d_adj_ext.ensure(std::max<size_t>(ext.size(), 1) * sizeof(ExtConstraint)));
+        RP_CUDA(w->d_adj_scenes.ensure((size_t)S * sizeof(AdjointScene)));
+        char* base = (char*)w->d_adj_data.p;
+        char* in = base + total;
+        double* d_start = (double*)in;
+        double* d_invm = d_start + 13 * N;
+        double* d_I = d_invm + N;
+        double* d_Ii = d_I + 6 * N;
+        double* d_mat = d_Ii + 6 * N;
+        double* d_pvel = d_mat + 3 * N;
+        double* d_deact = d_pvel + 6 * N;
+        uint8_t* d_fixed = (uint8_t*)(d_deact + N);
+        uint8_t* d_active = d_fixed + N;
+        RP_CUDA(cudaMemcpyAsync(d_start, start.data(), start.size() * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_invm, invm.data(), N * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_I, I6.data(), I6.size() * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_Ii, Ii6.data(), Ii6.size() * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_mat, mat.data(), mat.size() * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_pvel, pvel.data(), pvel.size() * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_deact, deact.data(), N * 8, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_fixed, fixedv.data(), N, cudaMemcpyHostToDevice, w->stream));
+        RP_CUDA(cudaMemcpyAsync(d_active, activev.data(), N, cudaMemcpyHostToDevice, w->stream));
+        if (!ext.empty())
+            RP_CUDA(cudaMemcpyAsync(w->d_adj_ext.p, ext.data(), ext.size() * sizeof(ExtConstraint), cudaMemcpyHostToDevice,
+                                    w->stream));
+        std::vector<AdjointScene> scenes((size_t)S);
+        for (int s = 0; s < S; ++s) {
+            AdjointScene& a = scenes[(size_t)s];
+            const Off& o = off[(size_t)s];
+            const int b0 = w->scene_body[(size_t)s];
+            a.nb = w->scene_body[(size_t)s + 1] - b0;
+            a.ne = ext_start[(size_t)s + 1] - ext_start[(size_t)s];
+            a.body0 = b0;
+            a.ext = w->d_adj_ext.as<ExtConstraint>() + ext_start[(size_t)s];
+            a.start = d_start + 13 * (size_t)b0;
+            a.invm = d_invm + b0;
+            a.inertia = d_I + 6 * (size_t)b0;
+            a.inv_inertia = d_Ii + 6 * (size_t)b0;
+            a.material = d_mat + 3 * (size_t)b0;
+            a.prev_vel = d_pvel + 6 * (size_t)b0;
+            a.deact0 = d_deact + b0;
+            a.active0 = d_active + b0;
+            a.fixed = d_fixed + b0;
+            a.loss_body = w->bodies[(size_t)loss_entity[s]].slot - b0;
+            for (int k = 0; k < 3; ++k) a.target[k] = target[3 * s + k];
+            a.tv0 = tv_of[(size_t)b0];
+            a.tn0 = tn_of[(size_t)b0];
+            a.ntv = tv_of[(size_t)b0 + (size_t)a.nb] - a.tv0;
+            a.ntn = tn_of[(size_t)b0 + (size_t)a.nb] - a.tn0;
+            a.pair_cap = o.pcap;
+            a.contact_cap = o.ccap;
+            a.checkpoints = (double*)(base + o.ckpt);
+            a.segment = (double*)(base + o.seg);
+            a.work = (double*)(base + o.work);
+            a.deact = (double*)(base + o.deact);
+            a.active = (uint8_t*)(base + o.active);
+            a.active_seg = (uint8_t*)(base + o.aseg);
+            a.pairs = (int2*)(base + o.pairs);
+            a.npairs = (int*)(base + o.npairs);
+            a.uf = (int*)(base + o.uf);
+            a.awake = (uint8_t*)(base + o.awake);
+            a.stamp = (int*)(base + o.stamp);
+            a.tv_d = base + o.tvd;
+            a.tn_d = base + o.tnd;
+            a.tv_a = base + o.tva;
+            a.tn_a = base + o.tna;
+            a.tv_val = (double*)(base + o.tvv);
+            a.tn_val = (double*)(base + o.tnv);
+            a.con_d = base + o.cond;
+            a.con_a = base + o.cona;
+            a.clip_d = base + o.clipd;
+            a.clip_a = base + o.clipa;
+            a.epa = base + o.epa;
+            a.grad_state = (double*)(base + o.grad);
+            a.grad_invm = (double*)(base + o.ginv);
+            a.grad_mu = (double*)(base + o.gmu);
+            a.loss = (double*)(base + o.loss);
+            a.status = (int*)(base + o.status);
+            a.prof = (long long*)(base + o.prof);
+            a.bodies_d = base + o.bd;
+            a.bodies_a = base + o.ba;
+            a.lam_d = (double*)(base + o.lamd);
+            a.lam_a = base + o.lama;
+            a.tape_ab = (int2*)(base + o.tab);
+            a.tape_d = (double2*)(base + o.td);
+            a.tape_adj = (double*)(base + o.tadj);
+            a.tape_cap = o.cap;
+        }
+        RP_CUDA(cudaMemcpyAsync(w->d_adj_scenes.p, scenes.data(), scenes.size() * sizeof(AdjointScene),
+                                cudaMemcpyHostToDevice, w->stream));
+        AdjointParams P;
+        P.dt = dt;
+        P.gravity = w->gravity;
+        P.substeps = (int)substeps;
+        P.pos_iters = (int)iters;
+        P.frames = (int)frames;
+        P.checkpoint_every = (int)checkpoint_every;
+        P.collisions = collisions ? 1 : 0;
+        P.geom.colliders = w->d_colliders.as<Collider>();
+        P.geom.shapes = w->d_shapes.as<Shape>();
+        P.geom.shape_verts = w->d_shape_verts.as<double>();
+        P.geom.face_normal = w->d_face_normal.as<double>();
+        P.geom.face_elem_start = w->d_face_elem_start.as<int32_t>();
+        P.geom.face_elem = w->d_face_elem.as<int32_t>();
+        P.geom.csr_start = w->d_csr_start.as<int32_t>();
+        P.geom.csr_data = w->d_csr_data.as<int32_t>();
+        P.geom.col_start = w->d_col_start.as<int32_t>();
+        P.geom.radius = w->d_radius.as<double>();
+        RP_CUDA(adjoint_launch(w->d_adj_scenes.as<AdjointScene>(), S, P, w->stream));
+        w->launches++;
+        // results
+        std::vector<double> g(13 * N), gi(N), gmu(2 * N);
+        std::vector<int> status((size_t)S, 0);
+        std::vector<long long> prof(6 * (size_t)S, 0);
+        for (int s = 0; s < S; ++s) {
+            const Off& o = off[(size_t)s];
+            const int b0 = w->scene_body[(size_t)s], nb = w->scene_body[(size_t)s + 1] - b0;
+            RP_CUDA(cudaMemcpyAsync(&g[13 * (size_t)b0], base + o.grad, 13 * (size_t)nb * 8, cudaMemcpyDeviceToHost, w->stream));
+            RP_CUDA(cudaMemcpyAsync(&gi[(size_t)b0], base + o.ginv, (size_t)nb * 8, cudaMemcpyDeviceToHost, w->stream));
+            RP_CUDA(cudaMemcpyAsync(&gmu[2 * (size_t)b0], base + o.gmu, 2 * (size_t)nb * 8, cudaMemcpyDeviceToHost, w->stream));
+            RP_CUDA(cudaMemcpyAsync(&loss_out[s], base + o.loss, 8, cudaMemcpyDeviceToHost, w->stream));
+            RP_CUDA(cudaMemcpyAsync(&status[(size_t)s], base + o.status, 4, cudaMemcpyDeviceToHost, w->stream));
+            RP_CUDA(cudaMemcpyAsync(&prof[6 * (size_t)s], base + o.prof, 48, cudaMemcpyDeviceToHost, w->stream));
+        }
+        RP_CUDA(cudaStreamSynchronize(w->stream));
+        {
+            // the slowest scene's phase split, in ms at the SM clock
+            int clock_khz = 1;
+            cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, w->device);
+            size_t worst = 0;
+            long long worst_c = -1;
+            for (size_t s = 0; s < (size_t)S; ++s) {
+                const long long c = prof[6 * s] + prof[6 * s + 1] + prof[6 * s + 2] + prof[6 * s + 3];
+                if (c > worst_c) { worst_c = c; worst = s; }
+            }
+            for (int k = 0; k < 4; ++k) w->adj_prof[k] = (double)prof[6 * worst + (size_t)k] / (double)std::max(clock_khz, 1);
+            w->adj_prof[4] = (double)prof[6 * worst + 4];
+            w->adj_prof[5] = (double)prof[6 * worst + 5];
+        }
+        int bad = 0;
+        for (int v : status) bad |= v;
+        if (bad & ADJ_ST_TAPE) {
+            if (attempt < 2) { tape_scale *= 4; continue; }
+            return fail(RP_ERR_CAPACITY, "adjoint tape overflow");
+        }
+        if (bad & ADJ_ST_BAD_TAPE) return fail(RP_ERR_STATE, "adjoint tape inconsistent (an entry refers to a later one)");
+        if (bad & ADJ_ST_UNSUPPORTED) return fail(RP_ERR_INVALID, "the adjoint's contacts cover hull colliders only");
+        if (bad & (ADJ_ST_PAIRS | ADJ_ST_CONTACTS)) return fail(RP_ERR_CAPACITY, "adjoint pair or contact scratch overflow");
+        if (bad & ADJ_ST_NARROW) return fail(RP_ERR_DEGENERATE, "degenerate or oversized narrowphase in the adjoint");
+        for (size_t e = 0; e < N; ++e) {
+            const HostBody& b = w->bodies[e];
+            const size_t slot = (size_t)b.slot;
+            for (int k = 0; k < 3; ++k) {
+                grad_v[3 * e + k] = g[13 * slot + 7 + (size_t)k];
+                grad_w[3 * e + k] = g[13 * slot + 10 + (size_t)k];
+            }
+            // d loss / d m = d loss / d invm * d invm / d m = -invm^2 d loss / d invm
+            grad_mass[e] = b.fixed ? 0.0 : -b.invm * b.invm * gi[slot];
+            if (grad_friction) {
+                grad_friction[2 * e] = gmu[2 * slot];
+                grad_friction[2 * e + 1] = gmu[2 * slot + 1];
+            }
+        }
+        result = RP_OK;
+        break;
+    }
+    return result;
+}
+
+rp_status rp_adjoint_profile(rp_world* w, double out[6]) {
+    if (check_world(w) || !out) return RP_ERR_INVALID;
+    for (int k = 0; k < 6; ++k) out[k] = w->adj_prof[k];
+    return RP_OK;
 }
 
 rp_status rp_world_set_mode(rp_world* w, int32_t mode) {

@@ -38,6 +38,85 @@ struct PipeMarks {
                                  cudaStream_t st, PipeMarks* marks);                                          \
     int pipe_launches_##SUF(const StepParams& P);
 
+// Adjoint of the substep (rp_adjoint.cu): one scene per thread.
+struct AdjGeom {                           // the world's collider geometry (FP64), shared by all scenes
+    const Collider* colliders;
+    const Shape* shapes;
+    const double* shape_verts;
+    const double* face_normal;
+    const int32_t* face_elem_start;
+    const int32_t* face_elem;
+    const int32_t* csr_start;
+    const int32_t* csr_data;
+    const int32_t* col_start;              // [N+1] collider ranges by body slot
+    const double* radius;                  // [N] bounding_sphere_radius by body slot
+};
+struct AdjointParams {
+    double dt, gravity;
+    int substeps, pos_iters, frames, checkpoint_every;
+    int collisions;                        // enable_collisions of the differentiated step
+    AdjGeom geom;
+};
+// Status bits of one scene's adjoint
+enum : int { ADJ_ST_TAPE = 1, ADJ_ST_BAD_TAPE = 2, ADJ_ST_UNSUPPORTED = 4, ADJ_ST_PAIRS = 8, ADJ_ST_CONTACTS = 16,
+             ADJ_ST_NARROW = 32 };
+struct AdjointScene {
+    int nb, ne, body0;                     // the scene's bodies are world slots body0 .. body0 + nb
+    const ExtConstraint* ext;              // its external constraints (global slots)
+    const double* start;                   // [13 nb] x, q, v, w at the trajectory start
+    const double* invm;                    // [nb]
+    const double* inertia;                 // [6 nb] local inertia (symmetric storage: xx yy zz xy xz yz)
+    const double* inv_inertia;             // [6 nb] local inverse inertia
+    const double* material;                // [3 nb] static friction, dynamic friction, restitution
+    const double* prev_vel;                // [6 nb] previous linear and angular velocity (fixed bodies keep theirs)
+    const double* deact0;                  // [nb] deactivation time at the start
+    const uint8_t* active0;                // [nb] awake flag at the start
+    const uint8_t* fixed;                  // [nb]
+    int loss_body;                         // scene-local body of the loss |x - target|^2
+    double target[3];
+    int tv0, tn0, ntv, ntn;                // the scene's transformed vertices / normals (global offset, count)
+    int pair_cap, contact_cap;
+    double* checkpoints;                   // [(frames / K + 1) * 15 nb]: state, deactivation time, awake flag
+    double* segment;                       // [(K * substeps + 1) * 13 nb]
+    double* work;                          // [13 nb]
+    double* deact;                         // [nb]
+    uint8_t* active;                       // [nb]
+    uint8_t* active_seg;                   // [K nb] awake flags of each frame of the segment
+    int2* pairs;                           // [K pair_cap] broad-phase pairs of each frame of the segment
+    int* npairs;                           // [K]
+    int* uf;                               // [nb] union-find parents
+    uint8_t* awake;                        // [nb]
+    int* stamp;                            // [nb] substep of the body's last hull transform
+    void* tv_d; void* tn_d;                // transformed vertices / normals, scalar pass
+    void* tv_a; void* tn_a;                // taped pass
+    double* tv_val; double* tn_val;        // their values (every decision is taken on these)
+    void* con_d; void* con_a;              // [contact_cap] contact constraints of the substep
+    void* clip_d; void* clip_a;            // clipping buffers
+    void* epa;                             // EPA polytope
+    double* grad_state;                    // [13 nb] adjoint of the state (ends as d loss / d start)
+    double* grad_invm;                     // [nb]
+    double* grad_mu;                       // [2 nb] static, dynamic friction
+    double* loss;                          // [1]
+    int* status;                           // [1] ADJ_ST_* bits
+    long long* prof;                       // [6] SM cycles: forward, segment recompute, taped substeps, reverse
+                                           //     sweeps; largest and total tape entries of a substep
+    void* bodies_d;                        // nb bodies of the scalar pass
+    void* bodies_a;                        // nb bodies of the taped pass
+    double* lam_d;                         // [4 ne]
+    void* lam_a;                           // [4 ne] taped lambdas
+    int2* tape_ab;
+    double2* tape_d;
+    double* tape_adj;
+    int tape_cap;
+};
+cudaError_t adjoint_launch(AdjointScene* d_scenes, int nscenes, const AdjointParams& P, cudaStream_t st);
+size_t adjoint_body_bytes(bool tape);
+size_t adjoint_var_bytes();
+// scratch sizes of the contact pipeline: contact record, clipping buffers (per pass), EPA polytope
+size_t adjoint_contact_bytes(bool tape);
+size_t adjoint_clip_bytes(bool tape);
+size_t adjoint_epa_bytes();
+
 // No-allocation contact query: contacts per call held by its static device scratch (rp_noalloc.cu).
 constexpr int NOALLOC_MAX_CONTACTS = 64;
 cudaError_t noalloc_scratch(int device, double** contacts, int** count);

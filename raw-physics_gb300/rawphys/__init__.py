@@ -69,6 +69,8 @@ SIGNATURES = {
     "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_counters": (_i, [_W, _P(_u64)]),
     "rp_world_set_mode": (_i, [_W, _i]),
+    "rp_adjoint_profile": (_i, [_W, _P(_d)]),
+    "rp_adjoint_trajectory": (_i, [_W, _d, _u, _u, _i, _u, _u, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d)]),
     "rp_autotune": (_i, [_W, _d, _u, _u, _i, _u, _P(_i)]),
     "rp_kernel_launches": (_u64, [_W]),
     "rp_transfer_bytes": (_i, [_W, _P(_u64)]),
@@ -202,6 +204,11 @@ class World:
         r = _d()
         self._check(self.lib.rp_entity_get_mass_properties(self.h, e, C.byref(invm), I, Ii, C.byref(r)))
         return invm.value, np.array(I[:]).reshape(3, 3), np.array(Ii[:]).reshape(3, 3), r.value
+
+    def set_mass_properties(self, e, inverse_mass, inertia, inverse_inertia, radius):
+        I = np.ascontiguousarray(inertia, dtype=np.float64).reshape(9)
+        Ii = np.ascontiguousarray(inverse_inertia, dtype=np.float64).reshape(9)
+        self._check(self.lib.rp_entity_set_mass_properties(self.h, e, float(inverse_mass), _dp(I), _dp(Ii), float(radius)))
 
     def constraint(self, c, base: int = 0):
         o = _i()
@@ -353,6 +360,33 @@ class World:
         self._check(self.lib.rp_last_contacts(self.h, scene, pairs.ctypes.data_as(_P(_i)), _dp(out), cap, C.byref(n)))
         k = min(n.value, cap)
         return pairs[: 2 * k].reshape(-1, 2), out[: 11 * k].reshape(-1, 11)
+
+    def adjoint(self, frames: int, loss_entity, target, checkpoint_every: int = 10, dt=None, substeps=None, pos_iters=None,
+                collisions=None):
+        """Loss |x_e(T) - target|^2 per scene after `frames` frames and its gradient with respect to
+        initial velocities, masses and static / dynamic friction (rp_adjoint_trajectory). Step
+        arguments default to the loaded scene's."""
+        s = self.scene
+        dt = s.dt if dt is None else dt
+        substeps = s.substeps if substeps is None else substeps
+        pos_iters = s.pos_iters if pos_iters is None else pos_iters
+        collisions = bool(s.collisions) if collisions is None else bool(collisions)
+        le = np.ascontiguousarray(np.atleast_1d(loss_entity), dtype=np.int32)
+        tg = np.ascontiguousarray(np.reshape(target, (-1, 3)), dtype=np.float64)
+        n = self.num_entities()
+        loss = np.zeros(len(le))
+        gv, gw, gm, gf = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n), np.zeros((n, 2))
+        self._check(self.lib.rp_adjoint_trajectory(self.h, float(dt), int(substeps), int(pos_iters), int(collisions), int(frames),
+                                                   int(checkpoint_every), le.ctypes.data_as(_P(_i)), _dp(tg), _dp(loss),
+                                                   _dp(gv), _dp(gw), _dp(gm), _dp(gf)))
+        return {"loss": loss, "grad_v": gv, "grad_w": gw, "grad_mass": gm, "grad_friction": gf}
+
+    def adjoint_profile(self) -> dict:
+        """Time split of the last adjoint's slowest scene (rp_adjoint_profile)."""
+        out = np.zeros(6)
+        self._check(self.lib.rp_adjoint_profile(self.h, _dp(out)))
+        return {"forward_ms": out[0], "recompute_ms": out[1], "taped_ms": out[2], "reverse_ms": out[3],
+                "max_tape_entries": int(out[4]), "tape_entries": int(out[5])}
 
     MODES = {"auto": 0, "persistent": 1, "phased": 2}
 

@@ -16,6 +16,7 @@ Workloads (all seeded; none is a published dataset):
   tower_scene        a tower of unit cubes with alternating mass ratio
   chain_scene        cube links joined by hinge or spherical joints
   domino_scene       a row of 0.2x1x2 m dominoes and a thrown cube
+  domino_batch       1024 domino rows of 16-64 with a thrown cube each (the differentiation workload)
   random_pile_scene  small mixed-shape piles for parity tests
 """
 from __future__ import annotations
@@ -536,6 +537,45 @@ def shard_batch(batch: SceneBatch, rank: int, world: int) -> SceneBatch:
                       batch.omega[idx], cons, num_scenes=s1 - s0, dt=batch.dt, substeps=batch.substeps,
                       pos_iters=batch.pos_iters, collisions=batch.collisions, gravity=batch.gravity,
                       steps=batch.steps)
+
+
+def domino_batch(num_scenes: int = 1024, seed: int = 0, min_dominoes: int = 16, max_dominoes: int = 64):
+    """Differentiation workload: `num_scenes` independent scenes, each a row of n ~ U{16..64}
+    dominoes (cube scaled (0.1, 1, 0.5): 0.2 x 2 x 1 m, density 1) spaced U(0.8, 1.2) m along x on
+    its own fixed floor, plus a thrown unit cube with v ~ N(0, 2) m/s (x component made positive
+    and raised by 4 so that it flies at the row) and w ~ N(0, 3) rad/s. dt 1/60, 20 substeps,
+    120 steps. Returns the batch, the body index of each scene's last domino, and a seeded loss
+    target per scene (the last domino's centre displaced by N(0, 0.5) m in x and z)."""
+    rng = np.random.default_rng(seed)
+    meshes = [M.MESHES[name]() for name in SHAPES]
+    rows = {k: [] for k in ("scene", "scale", "pos", "mass", "fixed", "vel", "omega")}
+    last, target = [], []
+    for s in range(num_scenes):
+        n = int(rng.integers(min_dominoes, max_dominoes + 1))
+        half = max(10.0, 0.7 * n + 5.0)
+        def add(scale, pos, mass, fixed, v=(0.0, 0.0, 0.0), w=(0.0, 0.0, 0.0)):
+            rows["scene"].append(s); rows["scale"].append(scale); rows["pos"].append(pos)
+            rows["mass"].append(mass); rows["fixed"].append(fixed); rows["vel"].append(v); rows["omega"].append(w)
+            return len(rows["scene"]) - 1
+        add((half, 0.5, 10.0), (0.0, -0.5, 0.0), 1.0, True)
+        x = 0.0
+        for i in range(n):
+            x += float(rng.uniform(0.8, 1.2))
+            e = add((0.1, 1.0, 0.5), (x, 1.0, 0.0), 0.2 * 2.0 * 1.0, False)
+        last.append(e)
+        target.append((x + rng.normal(0.0, 0.5), 1.0, rng.normal(0.0, 0.5)))
+        v = rng.normal(0.0, 2.0, size=3)
+        v[0] = abs(v[0]) + 4.0
+        w = rng.normal(0.0, 3.0, size=3)
+        add((0.5, 0.5, 0.5), (-1.0, 1.6, 0.0), 1.0, False, tuple(v), tuple(w))
+    N = len(rows["scene"])
+    batch = SceneBatch("dominoes%d" % num_scenes, meshes, np.asarray(rows["scene"], dtype=np.int32),
+                       np.zeros(N, dtype=np.int32), np.asarray(rows["scale"], dtype=np.float64),
+                       np.asarray(rows["pos"], dtype=np.float64), np.tile(np.array([0.0, 0.0, 0.0, 1.0]), (N, 1)),
+                       np.asarray(rows["mass"], dtype=np.float64), np.asarray(rows["fixed"], dtype=bool),
+                       np.full(N, 0.5), np.full(N, 0.3), np.zeros(N), np.asarray(rows["vel"], dtype=np.float64),
+                       np.asarray(rows["omega"], dtype=np.float64), [], num_scenes=num_scenes, steps=120)
+    return batch, np.asarray(last, dtype=np.int32), np.asarray(target, dtype=np.float64)
 
 
 def tower_batch(num_towers: int = 2048, n: int = 64, ratio: float = 100.0, seed: int = 0, substeps: int = 50) -> SceneBatch:
