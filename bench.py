@@ -23,6 +23,8 @@ Printed JSON line (rank 0):
   precision the precision-stress report: 128 towers of 64 cubes (masses 1:100, 50 substeps) run
             in the FP32 and the all-FP64 builds side by side for 300 frames (per-step error from
             identical states, trajectory divergence, tower drift, energy drift)
+  adjoint   grad/s of the adjoint (scene-gradients per second) on a bounded sample of the
+            differentiation workload: 152 of its 1024 domino scenes over 4 of its 120 frames
 --workload batched measures the batched form alone (its value becomes the line's value).
 --impl reference times that CPU implementation on every host core instead (one replica of the
 workload per core; the reference is single-threaded and keeps process-global state).
@@ -292,6 +294,7 @@ def run_ours(args):
 
     w.close()
     batched = measure_batched(args, dev, rank, world_size, value) if args.batched_scenes > 0 else None
+    adjoint = measure_adjoint(args, dev) if args.adjoint_scenes > 0 and rank == 0 else None
     precision = None
     if args.precision_towers > 0 and rank == 0:
         from rawphys import scenes as S
@@ -334,6 +337,7 @@ def run_ours(args):
                              "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_sweep_grid (position sweep)",
                              "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
                 "batched": batched,
+                "adjoint": adjoint,
                 "precision": precision,
                 "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                                  "sample": "%d frames of the same scene from the state the timed GPU frames start "
@@ -410,6 +414,45 @@ def measure_batched(args, dev, rank, world_size, plain_value):
     return out
 
 
+def measure_adjoint(args, dev):
+    """grad/s of the adjoint on a bounded sample of the differentiation workload (1024 domino rows of
+    16-64 with a thrown cube, loss |x_last - target|^2 after 120 steps, gradients with respect to
+    initial v / w, masses and friction, checkpoints every 10 steps): the first `adjoint_scenes` scenes
+    of the same generator over `adjoint_frames` frames. The adjoint runs one scene per GPU thread in
+    FP64; its time grows linearly with the frames and, above one scene per SM, with the scenes."""
+    import torch
+    import rawphys
+    from rawphys import scenes as S
+    batch, last, target = S.domino_batch(1024, seed=0)
+    keep = batch.scene < args.adjoint_scenes
+    idx = np.nonzero(keep)[0]
+    remap = -np.ones(batch.num_bodies, dtype=np.int64)
+    remap[idx] = np.arange(len(idx))
+    sub = S.SceneBatch(batch.name, batch.meshes, batch.scene[keep], batch.mesh[keep], batch.scale[keep], batch.pos[keep],
+                       batch.rot[keep], batch.mass[keep], batch.fixed[keep], batch.mus[keep], batch.mud[keep],
+                       batch.rest[keep], batch.vel[keep], batch.omega[keep], [], num_scenes=args.adjoint_scenes, steps=120)
+    w = rawphys.World(dev, "fp64")
+    w.load_batch(sub)
+    le = remap[last[:args.adjoint_scenes]].astype(np.int32)
+    K = min(10, args.adjoint_frames)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res = w.adjoint(args.adjoint_frames, le, target[:args.adjoint_scenes], checkpoint_every=K)
+    secs = time.perf_counter() - t0
+    prof = w.adjoint_profile()
+    w.close()
+    n = args.adjoint_scenes
+    return {"value": n / secs, "unit": "scene-gradients/s", "scenes": n, "frames": args.adjoint_frames,
+            "seconds": secs, "scene_frame_gradients_per_s": n * args.adjoint_frames / secs,
+            "workload": "bounded sample of the differentiation workload: the first %d of 1024 domino scenes (16-64 "
+                        "dominoes and a thrown cube each), %d of its 120 frames, dt=1/60, 20 substeps, collisions on, "
+                        "checkpoints every %d frames; loss |x_last_domino - target|^2, gradients with respect to every "
+                        "body's initial v, w, mass and static / dynamic friction; FP64 adjoint" % (n, args.adjoint_frames, K),
+            "full_workload_estimate_s": secs * (1024.0 / n) * (120.0 / args.adjoint_frames),
+            "slowest_scene_profile": prof, "loss_mean": float(np.mean(res["loss"])),
+            "gradient_check": "FP64 central differences, tests/test_gpu_adjoint.py (relative error <= 1e-3)"}
+
+
 def run_batched_only(args, dev, rank, world_size):
     """--workload batched: the batched form alone, as the line's own value."""
     import torch
@@ -443,6 +486,8 @@ def main():
     ap.add_argument("--precision-towers", type=int, default=128, help="0 skips the precision-stress report")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default launch configuration")
     ap.add_argument("--precision-frames", type=int, default=300)
+    ap.add_argument("--adjoint-scenes", type=int, default=152, help="0 skips the adjoint grad/s measurement")
+    ap.add_argument("--adjoint-frames", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -113,6 +113,7 @@ struct rp_world {
     DevBuf d_invm, d_I, d_Iinv, d_mat, d_radius, d_bound, d_fixed, d_col_start, d_force, d_torque;
     DevBuf d_colliders, d_shapes, d_shape_verts, d_face_normal, d_shape_verts_f, d_face_normal_f, d_face_elem_start, d_face_elem, d_csr_start, d_csr_data;
     DevBuf d_tverts, d_tnorms, d_ext;
+    DevBuf d_sort_key, d_sort_val, d_sort_hist, d_sort_hi;
     DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
@@ -398,6 +399,10 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(w->d_pair_count.ensure((size_t)S * 4));
     RP_CUDA(w->d_pairs.ensure(std::max<size_t>(P, 1) * 8));
     RP_CUDA(w->d_row_count.ensure(std::max<size_t>(N, 1) * 4));
+    RP_CUDA(w->d_sort_key.ensure(std::max<size_t>(2 * N, 1) * 4));
+    RP_CUDA(w->d_sort_val.ensure(std::max<size_t>(2 * N, 1) * 4));
+    RP_CUDA(w->d_sort_hist.ensure(256 * ((std::max<size_t>(N, 1) + 255) / 256) * 4));
+    RP_CUDA(w->d_sort_hi.ensure(std::max<size_t>(N, 1) * 4));
     RP_CUDA(w->d_uf_parent.ensure(std::max<size_t>(N, 1) * 4));
     RP_CUDA(w->d_island_awake.ensure(std::max<size_t>(N, 1)));
     RP_CUDA(w->d_node_body.ensure(std::max<size_t>(NN, 1) * 8));
@@ -516,6 +521,10 @@ WorldView<R> make_view(rp_world* w) {
     V.pair_count = w->d_pair_count.as<int32_t>();
     V.pairs = w->d_pairs.as<int2>();
     V.row_count = w->d_row_count.as<int32_t>();
+    V.sort_key = w->d_sort_key.as<uint32_t>();
+    V.sort_val = w->d_sort_val.as<int32_t>();
+    V.sort_hist = w->d_sort_hist.as<int32_t>();
+    V.sort_hi = w->d_sort_hi.as<float>();
     V.uf_parent = w->d_uf_parent.as<int32_t>();
     V.island_awake = w->d_island_awake.as<uint8_t>();
     V.node_body = w->d_node_body.as<int32_t>();

@@ -23,6 +23,7 @@
 #include "rp_world.h"
 #include "rp_narrow.cuh"
 #include "rp_solve.cuh"
+#include <type_traits>
 
 namespace rp {
 
@@ -167,9 +168,176 @@ __device__ __forceinline__ bool broad_reject(float4 fi, float4 fj) {
     return dx * dx + dy * dy + dz * dz > mx * mx;
 }
 
+// Order-preserving map of a float onto an unsigned key (negative values reversed).
+__device__ __forceinline__ uint32_t float_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Scenes of this many bodies take the sort-based broad phase when a grid group steps them (the upper
+// bound keeps a row's bitmap of second indices within the block's shared scratch).
+constexpr int SORTED_BROAD_MIN = 1024;
+constexpr int SORTED_BROAD_MAX = 65536;
+
+// Sort-based broad phase of one large scene on a grid group (broad.cpp:6-28). Every body gets the x
+// interval [x - r - 0.05, x + r + 0.05], rounded outwards to float; two bodies can pass the exact test
+// |p_i - p_j| <= r_i + r_j + 0.1 only if their intervals overlap. The bodies are sorted by the lower
+// end of their interval (LSD radix sort, four 8-bit digits, each pass a per-tile histogram, a group
+// scan and a stable tile scatter), then one warp per sorted body scans the bodies that follow it while
+// their interval starts before its interval ends, and applies the exact test (FP32 rejection first,
+// then the reference's FP64 arithmetic). Hits are counted per row (the lower body index), the counts
+// scanned into row offsets, the hits placed, and each row sorted by its second index: the pair list
+// and its order are the reference's.
+template <typename R>
+__device__ void broad_phase_sorted(const WorldView<R>& W, const GridGroup& g, int s, int* smem) {
+    __shared__ int s_cnt[WARPS_PER_BLOCK][256];
+    const int b0 = W.scene_body[s], n = W.scene_body[s + 1] - b0;
+    const int ntot = W.scene_body[W.num_scenes];
+    const int pcap = W.scene_pair_cap[s + 1] - W.scene_pair_cap[s];
+    int2* pairs = W.pairs + W.scene_pair_cap[s];
+    const int tiles = (n + BLOCK - 1) / BLOCK;
+    uint32_t* key[2] = {W.sort_key + b0, W.sort_key + ntot + b0};
+    int* val[2] = {W.sort_val + b0, W.sort_val + ntot + b0};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = g.rank(); i < n; i += g.size()) {
+        const double4_32a p = W.pos[b0 + i];
+        const double r = W.radius[b0 + i];
+        const double slack = 1e-6 * (1.0 + fabs(p.x) + r);
+        key[0][i] = float_key(__double2float_rd(p.x - r - 0.05 - slack));
+        val[0][i] = i;
+        W.sort_hi[b0 + i] = __double2float_ru(p.x + r + 0.05 + slack);
+        W.row_count[b0 + i] = 0;
+        W.body_tl_count[b0 + i] = 0;
+    }
+    g.sync();
+    int cur = 0;
+    for (int shift = 0; shift < 32; shift += 8) {
+        for (int t = g.block(); t < tiles; t += g.nblocks()) {
+            for (int d = threadIdx.x; d < 256; d += blockDim.x) s_cnt[0][d] = 0;
+            __syncthreads();
+            const int i = t * BLOCK + (int)threadIdx.x;
+            if (i < n) atomicAdd(&s_cnt[0][(key[cur][i] >> shift) & 255u], 1);
+            __syncthreads();
+            for (int d = threadIdx.x; d < 256; d += blockDim.x) W.sort_hist[d * tiles + t] = s_cnt[0][d];
+            __syncthreads();
+        }
+        g.sync();
+        group_exclusive_scan(g, W.sort_hist, 256 * tiles, W.scan_tmp, smem);
+        for (int t = g.block(); t < tiles; t += g.nblocks()) {
+            for (int d = lane; d < 256; d += 32) s_cnt[wid][d] = 0;
+            __syncthreads();
+            const int i = t * BLOCK + (int)threadIdx.x;
+            uint32_t k = 0;
+            int v = 0, d = -1;
+            if (i < n) { k = key[cur][i]; v = val[cur][i]; d = (int)((k >> shift) & 255u); }
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            if (d >= 0 && rank == 0) s_cnt[wid][d] = __popc(peers);
+            __syncthreads();
+            if (d >= 0) {
+                int before = 0;
+                for (int w2 = 0; w2 < wid; ++w2) before += s_cnt[w2][d];
+                const int pos = W.sort_hist[d * tiles + t] + before + rank;
+                key[cur ^ 1][pos] = k;
+                val[cur ^ 1][pos] = v;
+            }
+            __syncthreads();
+        }
+        g.sync();
+        cur ^= 1;
+    }
+    // sweep: count hits per row, scan, then place them
+    const int gw = g.rank() >> 5, nw = g.size() >> 5;
+    int total = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int i = gw; i < n; i += nw) {
+            const int a = val[0][i];
+            const uint32_t hik = float_key(W.sort_hi[b0 + a]);
+            const double4_32a pa = W.pos[b0 + a];
+            const double ra = W.radius[b0 + a];
+            const float4 fa = make_float4((float)pa.x, (float)pa.y, (float)pa.z, (float)ra + 0.05f);
+            for (int kb = i + 1; kb < n; kb += 32) {
+                const int k = kb + lane;
+                const bool in = k < n && key[0][k] <= hik;
+                if (in) {
+                    const int b = val[0][k];
+                    const double4_32a pb = W.pos[b0 + b];
+                    const double rb = W.radius[b0 + b];
+                    const float4 fb = make_float4((float)pb.x, (float)pb.y, (float)pb.z, (float)rb + 0.05f);
+                    if (!broad_reject(fa, fb) && broad_exact(pa, pb, ra, rb)) {
+                        const int lo = min(a, b), hi = max(a, b);
+                        if (pass == 0) {
+                            atomicAdd(&W.row_count[b0 + lo], 1);
+                        } else {
+                            const int pos = W.row_count[b0 + lo] + atomicAdd(&W.body_tl_count[b0 + lo], 1);
+                            if (pos < pcap) pairs[pos] = make_int2(b0 + lo, b0 + hi);
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, in)) break;
+            }
+        }
+        g.sync();
+        if (pass == 0) total = group_exclusive_scan(g, W.row_count + b0, n, W.scan_tmp, smem);
+    }
+    // each row in increasing second index: short rows by insertion sort, one thread each; long rows
+    // (a fixed floor or wall meets nearly every body) by one block each, through a bitmap of the row's
+    // second indices whose set bits are then written out in order
+    for (int a = g.rank(); a < n; a += g.size()) {
+        const int st = W.row_count[b0 + a], cnt = W.body_tl_count[b0 + a];
+        if (cnt > 32) continue;
+        const int en = min(st + cnt, pcap);
+        for (int x = st + 1; x < en; ++x) {
+            const int2 v = pairs[x];
+            int y = x - 1;
+            while (y >= st && pairs[y].y > v.y) { pairs[y + 1] = pairs[y]; --y; }
+            pairs[y + 1] = v;
+        }
+    }
+    uint32_t* bits = reinterpret_cast<uint32_t*>(&s_cnt[0][0]);   // n <= 65536: at most 2048 words
+    const int nwords = (n + 31) >> 5;
+    for (int a = g.block(); a < n; a += g.nblocks()) {
+        const int st = W.row_count[b0 + a], cnt = W.body_tl_count[b0 + a];
+        if (cnt <= 32) continue;
+        for (int k = threadIdx.x; k < nwords; k += blockDim.x) bits[k] = 0u;
+        __syncthreads();
+        const int en = min(st + cnt, pcap);
+        for (int e = st + (int)threadIdx.x; e < en; e += blockDim.x) {
+            const int v = pairs[e].y - b0;
+            atomicOr(&bits[v >> 5], 1u << (v & 31));
+        }
+        __syncthreads();
+        const int per = (nwords + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int w0 = min(nwords, (int)threadIdx.x * per), w1 = min(nwords, w0 + per);
+        int mine = 0;
+        for (int k = w0; k < w1; ++k) mine += __popc(bits[k]);
+        int tot;
+        int pos = st + block_incl_scan(mine, smem, tot) - mine;
+        for (int k = w0; k < w1; ++k) {
+            uint32_t m = bits[k];
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                m &= m - 1u;
+                if (pos < pcap) pairs[pos] = make_int2(b0 + a, b0 + (k << 5) + bit);
+                ++pos;
+            }
+        }
+        __syncthreads();
+    }
+    if (g.rank() == 0) {
+        W.pair_count[s] = total;
+        atomicAdd(&W.counters[5], (unsigned long long)total);
+        if (total > pcap) atomicOr(&W.status[s], (uint32_t)ST_PAIR_OVERFLOW);
+    }
+    g.sync();
+}
+
 template <typename R, class G>
 __device__ void broad_phase(const WorldView<R>& W, const G& g, int s, int* smem) {
     const int b0 = W.scene_body[s], n = W.scene_body[s + 1] - b0;
+    if constexpr (std::is_same<G, GridGroup>::value) {
+        if (n >= SORTED_BROAD_MIN && n <= SORTED_BROAD_MAX) { broad_phase_sorted(W, g, s, smem); return; }
+    }
     const int pcap = W.scene_pair_cap[s + 1] - W.scene_pair_cap[s];
     int2* pairs = W.pairs + W.scene_pair_cap[s];
     const int lane = threadIdx.x & 31;

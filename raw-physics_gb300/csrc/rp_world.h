@@ -128,6 +128,10 @@ struct WorldView {
     int32_t* pair_count;     // [S] pairs found this step
     int2* pairs;             // broad-phase pairs (global body indices), in reference order
     int32_t* row_count;      // [N] broad-phase counts per row (scan workspace)
+    uint32_t* sort_key;      // [2N] sort-based broad phase: radix-sort keys (ping-pong)
+    int32_t* sort_val;       // [2N] body indices travelling with the keys
+    int32_t* sort_hist;      // [256 * ceil(N / 256)] digit counts per tile of 256 keys
+    float* sort_hi;          // [N] upper end of each body's x interval
     int32_t* uf_parent;      // [N] union-find parents (global body indices)
     uint8_t* island_awake;   // [N] per-root flag
     int32_t* node_body;      // [2 * nodes] the node's two bodies (-1 when fixed)
