@@ -312,8 +312,8 @@ cudaError_t adjoint_launch(AdjointScene* d_scenes, int nscenes, const AdjointPar
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tpb = max(1, min(ADJ_BLOCK, (nscenes + sms - 1) / max(sms, 1)));
     const int blocks = (nscenes + tpb - 1) / tpb;
-    // reverse-sweep windows: up to 160 KB of shared memory per block, at most 4096 values a thread
-    const int win = min(4096, 20480 / tpb);
+    // reverse-sweep windows: 200 KB of shared memory per block, split between its threads
+    const int win = 25600 / tpb;
     const size_t smem = (size_t)win * tpb * sizeof(double);
     cudaError_t e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -178,6 +178,8 @@ __device__ __forceinline__ uint32_t float_key(float f) {
 // bound keeps a row's bitmap of second indices within the block's shared scratch).
 constexpr int SORTED_BROAD_MIN = 1024;
 constexpr int SORTED_BROAD_MAX = 65536;
+// Up to this many bodies one CTA does the radix sort alone.
+constexpr int SORT_ONE_CTA_MAX = 16384;
 
 // Sort-based broad phase of one large scene on a grid group (broad.cpp:6-28). Every body gets the x
 // interval [x - r - 0.05, x + r + 0.05], rounded outwards to float; two bodies can pass the exact test
@@ -210,41 +212,86 @@ __device__ void broad_phase_sorted(const WorldView<R>& W, const GridGroup& g, in
         W.body_tl_count[b0 + i] = 0;
     }
     g.sync();
-    int cur = 0;
-    for (int shift = 0; shift < 32; shift += 8) {
-        for (int t = g.block(); t < tiles; t += g.nblocks()) {
-            for (int d = threadIdx.x; d < 256; d += blockDim.x) s_cnt[0][d] = 0;
-            __syncthreads();
-            const int i = t * BLOCK + (int)threadIdx.x;
-            if (i < n) atomicAdd(&s_cnt[0][(key[cur][i] >> shift) & 255u], 1);
-            __syncthreads();
-            for (int d = threadIdx.x; d < 256; d += blockDim.x) W.sort_hist[d * tiles + t] = s_cnt[0][d];
-            __syncthreads();
-        }
-        g.sync();
-        group_exclusive_scan(g, W.sort_hist, 256 * tiles, W.scan_tmp, smem);
-        for (int t = g.block(); t < tiles; t += g.nblocks()) {
-            for (int d = lane; d < 256; d += 32) s_cnt[wid][d] = 0;
-            __syncthreads();
-            const int i = t * BLOCK + (int)threadIdx.x;
-            uint32_t k = 0;
-            int v = 0, d = -1;
-            if (i < n) { k = key[cur][i]; v = val[cur][i]; d = (int)((k >> shift) & 255u); }
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const int rank = __popc(peers & ((1u << lane) - 1u));
-            if (d >= 0 && rank == 0) s_cnt[wid][d] = __popc(peers);
-            __syncthreads();
-            if (d >= 0) {
-                int before = 0;
-                for (int w2 = 0; w2 < wid; ++w2) before += s_cnt[w2][d];
-                const int pos = W.sort_hist[d * tiles + t] + before + rank;
-                key[cur ^ 1][pos] = k;
-                val[cur ^ 1][pos] = v;
+    if (n <= SORT_ONE_CTA_MAX) {
+        // one CTA sorts (the radix passes then need block barriers only); the others wait once
+        if (g.block() == 0) {
+            __shared__ int s_base[256];
+            int cur = 0;
+            for (int shift = 0; shift < 32; shift += 8) {
+                s_base[threadIdx.x] = 0;
+                __syncthreads();
+                for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&s_base[(key[cur][i] >> shift) & 255u], 1);
+                __syncthreads();
+                int tot;
+                const int x = s_base[threadIdx.x];
+                const int incl = block_incl_scan(x, smem, tot);
+                s_base[threadIdx.x] = incl - x;
+                __syncthreads();
+                for (int t = 0; t < tiles; ++t) {
+                    for (int d = lane; d < 256; d += 32) s_cnt[wid][d] = 0;
+                    __syncthreads();
+                    const int i = t * BLOCK + (int)threadIdx.x;
+                    uint32_t k = 0;
+                    int v = 0, d = -1;
+                    if (i < n) { k = key[cur][i]; v = val[cur][i]; d = (int)((k >> shift) & 255u); }
+                    const unsigned peers = __match_any_sync(0xffffffffu, d);
+                    const int rank = __popc(peers & ((1u << lane) - 1u));
+                    if (d >= 0 && rank == 0) s_cnt[wid][d] = __popc(peers);
+                    __syncthreads();
+                    if (d >= 0) {
+                        int before = 0;
+                        for (int w2 = 0; w2 < wid; ++w2) before += s_cnt[w2][d];
+                        const int pos = s_base[d] + before + rank;
+                        key[cur ^ 1][pos] = k;
+                        val[cur ^ 1][pos] = v;
+                    }
+                    __syncthreads();
+                    int add = 0;
+                    for (int w2 = 0; w2 < WARPS_PER_BLOCK; ++w2) add += s_cnt[w2][threadIdx.x];
+                    s_base[threadIdx.x] += add;
+                    __syncthreads();
+                }
+                cur ^= 1;
             }
-            __syncthreads();
         }
         g.sync();
-        cur ^= 1;
+    } else {
+        int cur = 0;
+        for (int shift = 0; shift < 32; shift += 8) {
+            for (int t = g.block(); t < tiles; t += g.nblocks()) {
+                for (int d = threadIdx.x; d < 256; d += blockDim.x) s_cnt[0][d] = 0;
+                __syncthreads();
+                const int i = t * BLOCK + (int)threadIdx.x;
+                if (i < n) atomicAdd(&s_cnt[0][(key[cur][i] >> shift) & 255u], 1);
+                __syncthreads();
+                for (int d = threadIdx.x; d < 256; d += blockDim.x) W.sort_hist[d * tiles + t] = s_cnt[0][d];
+                __syncthreads();
+            }
+            g.sync();
+            group_exclusive_scan(g, W.sort_hist, 256 * tiles, W.scan_tmp, smem);
+            for (int t = g.block(); t < tiles; t += g.nblocks()) {
+                for (int d = lane; d < 256; d += 32) s_cnt[wid][d] = 0;
+                __syncthreads();
+                const int i = t * BLOCK + (int)threadIdx.x;
+                uint32_t k = 0;
+                int v = 0, d = -1;
+                if (i < n) { k = key[cur][i]; v = val[cur][i]; d = (int)((k >> shift) & 255u); }
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                if (d >= 0 && rank == 0) s_cnt[wid][d] = __popc(peers);
+                __syncthreads();
+                if (d >= 0) {
+                    int before = 0;
+                    for (int w2 = 0; w2 < wid; ++w2) before += s_cnt[w2][d];
+                    const int pos = W.sort_hist[d * tiles + t] + before + rank;
+                    key[cur ^ 1][pos] = k;
+                    val[cur ^ 1][pos] = v;
+                }
+                __syncthreads();
+            }
+            g.sync();
+            cur ^= 1;
+        }
     }
     // sweep: count hits per row, scan, then place them
     const int gw = g.rank() >> 5, nw = g.size() >> 5;

@@ -367,3 +367,27 @@ def test_autotune_keeps_results_and_state(ext_built, oracle_built):
         o.step(3)
         assert np.array_equal(w.get_state(), o.get_state()), (sc.name, choice)
         w.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sorted_broad_phase_grid_wide_sort(ext_built, oracle_built, precision):
+    """A single scene above one CTA's sort size (16384 bodies) takes the grid-wide radix passes of
+    the sort-based broad phase: 17000 small cubes on a jittered grid over a floor, about five pairs a
+    body plus the floor's row of 17000. Same pairs, same order as the reference."""
+    from rawphys import scenes as S
+    rng = np.random.default_rng(3)
+    b = S._Builder("grid17k")
+    S._floor(b, (60.0, 0.5, 60.0))
+    for i in range(17000):
+        x, z = i % 130, i // 130
+        p = (x * 0.45 - 29.0 + rng.uniform(-0.05, 0.05), 0.2 + rng.uniform(0.0, 0.3), z * 0.45 - 29.0 + rng.uniform(-0.05, 0.05))
+        b.hull_body("cube", (0.2, 0.2, 0.2), p, mass=0.064)
+    sc = b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=1)
+    o = oracle_built("port").load(sc)
+    w = ext_built.World(0, precision)
+    w.load(sc)
+    pairs = w.broad_pairs()
+    ref = o.broad_pairs()
+    assert len(ref) > 17000 * 3
+    assert np.array_equal(pairs, ref)
+    w.close()
