@@ -32,6 +32,29 @@ static rp_status fail(rp_status code, const std::string& msg) {
         if (e_ != cudaSuccess) return fail(RP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Page-locked host staging: copies from and to it run at full link bandwidth, asynchronously
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    ~HostBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        size_t want = n ? n : 16;
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -121,6 +144,7 @@ struct rp_world {
 
     // phase-major pipeline
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
+    HostBuf h_state;                               // pinned staging of the body state (rp_state_set / _get)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
@@ -578,20 +602,41 @@ StateSlices state_slices(rp_world* w) {
     return s;
 }
 
+// The body state's staging layout in the pinned buffer: pose arrays (double4 each), deactivation
+// times, the four velocity arrays in the working type, the awake flags.
+struct StateLayout {
+    size_t pos, rot, ppos, prot, deact, vel, om, pvel, pom, act, total;
+    StateLayout(size_t N, size_t R) {
+        pos = 0; rot = pos + 32 * N; ppos = rot + 32 * N; prot = ppos + 32 * N; deact = prot + 32 * N;
+        vel = deact + 8 * N; om = vel + 3 * R * N; pvel = om + 3 * R * N; pom = pvel + 3 * R * N; act = pom + 3 * R * N;
+        total = act + N;
+    }
+};
+
 rp_status upload_state(rp_world* w) {
     const size_t N = w->bodies.size(), R = w->rsize();
-    std::vector<double> pos(4 * N), rot(4 * N), ppos(4 * N), prot(4 * N), deact(N);
-    std::vector<double> vel(3 * N), om(3 * N), pvel(3 * N), pom(3 * N);
-    std::vector<uint8_t> act(N);
+    const StateLayout L(N, R);
+    RP_CUDA(w->h_state.ensure(L.total));
+    char* h = (char*)w->h_state.p;
+    double* pos = (double*)(h + L.pos);
+    double* rot = (double*)(h + L.rot);
+    double* ppos = (double*)(h + L.ppos);
+    double* prot = (double*)(h + L.prot);
+    double* deact = (double*)(h + L.deact);
+    uint8_t* act = (uint8_t*)(h + L.act);
+    auto put = [&](size_t off, size_t i, double v) {
+        if (R == 8) ((double*)(h + off))[i] = v;
+        else ((float*)(h + off))[i] = (float)v;
+    };
     for (size_t slot = 0; slot < N; ++slot) {
         const HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
         for (int k = 0; k < 3; ++k) {
             pos[4 * slot + (size_t)k] = b.pos[k];
             ppos[4 * slot + (size_t)k] = b.ppos[k];
-            vel[3 * slot + (size_t)k] = b.v[k];
-            om[3 * slot + (size_t)k] = b.w[k];
-            pvel[3 * slot + (size_t)k] = b.pv[k];
-            pom[3 * slot + (size_t)k] = b.pw[k];
+            put(L.vel, 3 * slot + (size_t)k, b.v[k]);
+            put(L.om, 3 * slot + (size_t)k, b.w[k]);
+            put(L.pvel, 3 * slot + (size_t)k, b.pv[k]);
+            put(L.pom, 3 * slot + (size_t)k, b.pw[k]);
         }
         pos[4 * slot + 3] = 0.0;
         ppos[4 * slot + 3] = 0.0;
@@ -601,68 +646,65 @@ rp_status upload_state(rp_world* w) {
     }
     cudaStream_t st = w->stream;
     w->h2d_bytes += N * (4 * 32 + 4 * 3 * R + 1 + 8);
-    RP_CUDA(upload(w->d_pos, pos, st));
-    RP_CUDA(upload(w->d_rot, rot, st));
-    RP_CUDA(upload(w->d_ppos, ppos, st));
-    RP_CUDA(upload(w->d_prot, prot, st));
-    RP_CUDA(upload(w->d_vel, as_working<double>(vel, R), st));
-    RP_CUDA(upload(w->d_omega, as_working<double>(om, R), st));
-    RP_CUDA(upload(w->d_pvel, as_working<double>(pvel, R), st));
-    RP_CUDA(upload(w->d_pomega, as_working<double>(pom, R), st));
-    RP_CUDA(upload(w->d_active, act, st));
-    RP_CUDA(upload(w->d_deact, deact, st));
-    RP_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
+    auto send = [&](DevBuf& d, size_t off, size_t bytes) -> cudaError_t {
+        cudaError_t e = d.ensure(bytes);
+        if (e != cudaSuccess || bytes == 0) return e;
+        return cudaMemcpyAsync(d.p, h + off, bytes, cudaMemcpyHostToDevice, st);
+    };
+    RP_CUDA(send(w->d_pos, L.pos, 32 * N));
+    RP_CUDA(send(w->d_rot, L.rot, 32 * N));
+    RP_CUDA(send(w->d_ppos, L.ppos, 32 * N));
+    RP_CUDA(send(w->d_prot, L.prot, 32 * N));
+    RP_CUDA(send(w->d_vel, L.vel, 3 * R * N));
+    RP_CUDA(send(w->d_omega, L.om, 3 * R * N));
+    RP_CUDA(send(w->d_pvel, L.pvel, 3 * R * N));
+    RP_CUDA(send(w->d_pomega, L.pom, 3 * R * N));
+    RP_CUDA(send(w->d_active, L.act, N));
+    RP_CUDA(send(w->d_deact, L.deact, 8 * N));
+    RP_CUDA(cudaStreamSynchronize(st));   // the staging buffer is refilled by the next call
     w->device_state_valid = true;
     return RP_OK;
-}
-
-// n working-type values (float or double) from the device, widened to double
-std::vector<double> fetch(const DevBuf& b, size_t n, size_t rsize, cudaStream_t st, cudaError_t& err) {
-    std::vector<double> out(n);
-    if (n == 0) return out;
-    if (rsize == 8) {
-        err = cudaMemcpyAsync(out.data(), b.p, n * 8, cudaMemcpyDeviceToHost, st);
-    } else {
-        std::vector<float> f(n);
-        err = cudaMemcpyAsync(f.data(), b.p, n * 4, cudaMemcpyDeviceToHost, st);
-        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
-        for (size_t i = 0; i < n; ++i) out[i] = f[i];
-    }
-    return out;
 }
 
 rp_status sync_state_to_host(rp_world* w) {
     if (!w->device_state_valid) return RP_OK;
     const size_t N = w->bodies.size(), R = w->rsize();
     cudaStream_t st = w->stream;
-    cudaError_t e = cudaSuccess;
-    std::vector<double> pos(4 * N), rot(4 * N), ppos(4 * N), prot(4 * N), deact(N);
-    std::vector<uint8_t> act(N);
+    const StateLayout L(N, R);
+    RP_CUDA(w->h_state.ensure(L.total));
+    char* h = (char*)w->h_state.p;
     if (N) {
-        RP_CUDA(cudaMemcpyAsync(pos.data(), w->d_pos.p, N * 32, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(rot.data(), w->d_rot.p, N * 32, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(ppos.data(), w->d_ppos.p, N * 32, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(prot.data(), w->d_prot.p, N * 32, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(deact.data(), w->d_deact.p, N * 8, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(act.data(), w->d_active.p, N, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.pos, w->d_pos.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.rot, w->d_rot.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.ppos, w->d_ppos.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.prot, w->d_prot.p, N * 32, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.deact, w->d_deact.p, N * 8, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.vel, w->d_vel.p, 3 * R * N, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.om, w->d_omega.p, 3 * R * N, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.pvel, w->d_pvel.p, 3 * R * N, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.pom, w->d_pomega.p, 3 * R * N, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(h + L.act, w->d_active.p, N, cudaMemcpyDeviceToHost, st));
     }
     w->d2h_bytes += N * (4 * 32 + 4 * 3 * R + 1 + 8);
-    std::vector<double> vel = fetch(w->d_vel, 3 * N, R, st, e);
-    if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
-    std::vector<double> om = fetch(w->d_omega, 3 * N, R, st, e);
-    std::vector<double> pvel = fetch(w->d_pvel, 3 * N, R, st, e);
-    std::vector<double> pom = fetch(w->d_pomega, 3 * N, R, st, e);
-    if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
     RP_CUDA(cudaStreamSynchronize(st));
+    const double* pos = (const double*)(h + L.pos);
+    const double* rot = (const double*)(h + L.rot);
+    const double* ppos = (const double*)(h + L.ppos);
+    const double* prot = (const double*)(h + L.prot);
+    const double* deact = (const double*)(h + L.deact);
+    const uint8_t* act = (const uint8_t*)(h + L.act);
+    auto get = [&](size_t off, size_t i) -> double {
+        return R == 8 ? ((const double*)(h + off))[i] : (double)((const float*)(h + off))[i];
+    };
     for (size_t slot = 0; slot < N; ++slot) {
         HostBody& b = w->bodies[(size_t)w->slot_to_entity[slot]];
         for (int k = 0; k < 3; ++k) {
             b.pos[k] = pos[4 * slot + (size_t)k];
             b.ppos[k] = ppos[4 * slot + (size_t)k];
-            b.v[k] = vel[3 * slot + (size_t)k];
-            b.w[k] = om[3 * slot + (size_t)k];
-            b.pv[k] = pvel[3 * slot + (size_t)k];
-            b.pw[k] = pom[3 * slot + (size_t)k];
+            b.v[k] = get(L.vel, 3 * slot + (size_t)k);
+            b.w[k] = get(L.om, 3 * slot + (size_t)k);
+            b.pv[k] = get(L.pvel, 3 * slot + (size_t)k);
+            b.pw[k] = get(L.pom, 3 * slot + (size_t)k);
         }
         for (int k = 0; k < 4; ++k) { b.rot[k] = rot[4 * slot + (size_t)k]; b.prot[k] = prot[4 * slot + (size_t)k]; }
         b.active = act[slot] ? 1.0 : 0.0;
