@@ -1656,23 +1656,23 @@ rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t substeps, uint3
                                 double* loss_out, double* grad_v, double* grad_w, double* grad_mass, double* grad_friction) {
     if (check_world(w) || !loss_entity || !target || !loss_out || !grad_v || !grad_w || !grad_mass)
         return fail(RP_ERR_INVALID, "null argument");
-    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     if (!(dt > 0.0) || substeps == 0 || iters == 0 || frames == 0 || checkpoint_every == 0)
         return fail(RP_ERR_INVALID, "bad step arguments");
+    const int S = w->num_scenes;
+    for (int s = 0; s < S; ++s) {
+        const int e = loss_entity[s];
+        if (e < 0 || e >= (int)w->bodies.size() || w->bodies[(size_t)e].scene != s)
+            return fail(RP_ERR_INVALID, "loss entity must belong to its scene");
+    }
     for (const HostBody& b : w->bodies)
         if (!b.forces.empty()) return fail(RP_ERR_STATE, "the adjoint covers gravity only: clear the pending forces");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
     RP_CUDA(cudaSetDevice(w->device));
     rp_status st = ensure_device(w);   // slots, the scene layout and the geometry
     if (st != RP_OK) return st;
     if (w->device_state_valid) {
         st = sync_state_to_host(w);
         if (st != RP_OK) return st;
-    }
-    const int S = w->num_scenes;
-    for (int s = 0; s < S; ++s) {
-        const int e = loss_entity[s];
-        if (e < 0 || e >= (int)w->bodies.size() || w->bodies[(size_t)e].scene != s)
-            return fail(RP_ERR_INVALID, "loss entity must belong to its scene");
     }
     // host copies by slot: start states, mass properties, materials, sleeping state
     const size_t N = w->bodies.size();

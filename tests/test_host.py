@@ -137,3 +137,37 @@ def test_scene_generators_are_deterministic():
     assert np.all(np.abs(p[:, 0]) < 20) and np.all(np.abs(p[:, 2]) < 20) and np.all((p[:, 1] > 0) & (p[:, 1] < 60))
     q = np.linalg.norm(a.rot, axis=1)
     assert np.allclose(q, 1.0)
+
+
+def test_adjoint_on_a_host_only_world_and_its_arguments(ext_built):
+    """The adjoint's argument checks run on the host: a host-only world reports RP_ERR_NO_DEVICE,
+    a loss entity outside its scene or a zero checkpoint spacing RP_ERR_INVALID."""
+    from rawphys import scenes as S
+    rp = ext_built
+    w = rp.World(-1, "fp64")
+    w.load(S.domino_scene(3, seed=0))
+    with pytest.raises(rp.RPError, match="RP_ERR_NO_DEVICE"):
+        w.adjoint(2, [1], np.zeros(3))
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.adjoint(2, [1], np.zeros(3), checkpoint_every=0)
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.adjoint(2, [17], np.zeros(3))                               # no such entity
+    prof = w.adjoint_profile()
+    assert prof["tape_entries"] == 0
+    w.close()
+
+
+def test_domino_batch_generator():
+    from rawphys import scenes as S
+    b, last, target = S.domino_batch(12, seed=4)
+    assert b.num_scenes == 12 and len(last) == 12 and target.shape == (12, 3)
+    sizes = np.bincount(b.scene, minlength=12)
+    assert np.all((sizes >= 16 + 2) & (sizes <= 64 + 2))          # floor + dominoes + thrown cube
+    for s in range(12):
+        idx = np.nonzero(b.scene == s)[0]
+        assert b.fixed[idx[0]] and not b.fixed[idx[1:]].any()        # the floor first
+        assert idx[0] < last[s] < idx[-1]                             # the last domino precedes the cube
+        assert np.allclose(b.scale[last[s]], (0.1, 1.0, 0.5))
+        assert b.vel[idx[-1], 0] >= 4.0                               # the cube flies at the row
+    b2, last2, target2 = S.domino_batch(12, seed=4)
+    assert np.array_equal(b.pos, b2.pos) and np.array_equal(target, target2)
