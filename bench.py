@@ -400,6 +400,24 @@ def measure_batched(args, dev, rank, world_size, plain_value):
     w.sync()
     w.set_timing(False)
     p1 = w.phase_times()
+    # end to end through the C ABI with host buffers: every frame uploads the whole batch's state,
+    # steps, and downloads it
+    st = w.get_state()
+    w.set_state(st)
+    w.step(1)
+    st = w.get_state()
+    b0 = w.transfer_bytes()
+    e2e_frames = 3
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_frames):
+        w.set_state(st)
+        w.step(1)
+        st = w.get_state()
+    e2e_wall = time.perf_counter() - t
+    b1 = w.transfer_bytes()
+    e2e = {"value": nd * batch.substeps * e2e_frames * world_size / e2e_wall, "unit": UNIT,
+           "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_frames, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_frames}
     value = nd * batch.substeps * args.batched_steps * world_size / (total_ms / 1e3)
     sizes = batch.scene_sizes()
     out = {"value": value, "unit": UNIT, "ms_per_step": total_ms / args.batched_steps, "steps": args.batched_steps,
@@ -415,7 +433,8 @@ def measure_batched(args, dev, rank, world_size, plain_value):
            "pairs_per_step": (c1[6] - c0[6]) / args.batched_steps,
            "contacts_per_step": (c1[5] - c0[5]) / args.batched_steps,
            "phase_ms_per_step": {k: round((p1[k] - p0[k]) / 2, 3) for k in p0},
-           "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches, "autotuned": tuned}
+           "e2e": e2e, "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches,
+           "autotuned": tuned}
     w.close()
     return out
 
@@ -471,7 +490,8 @@ def run_batched_only(args, dev, rank, world_size):
                            "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
                            "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
                            "phase_ms_per_step": b["phase_ms_per_step"]},
-                "gpu_launches": b["gpu_launches"], "clocks": b["clocks"], "device_status": b["device_status"]}
+                "gpu_launches": b["gpu_launches"], "e2e": b["e2e"], "clocks": b["clocks"],
+                "device_status": b["device_status"]}
         print(json.dumps(line), flush=True)
     if world_size > 1:
         torch.distributed.destroy_process_group()
