@@ -1406,8 +1406,10 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out, uint32_t cap
     RP_CUDA(cudaSetDevice(w->device));
     rp_status s = ensure_device(w);
     if (s != RP_OK) return s;
-    if (w->precision == RP_PRECISION_FP64) RP_CUDA(broad_f64(make_view<double>(w), scene, w->stream));
-    else RP_CUDA(broad_f32(make_view<float>(w), scene, w->stream));
+    // the step's own broad phase for this world: the grid (sort-based) for one large scene
+    const int gb = w->grid_mode ? w->num_sms : 0;
+    if (w->precision == RP_PRECISION_FP64) RP_CUDA(broad_f64(make_view<double>(w), scene, gb, w->stream));
+    else RP_CUDA(broad_f32(make_view<float>(w), scene, gb, w->stream));
     w->launches++;
     int32_t n = 0;
     RP_CUDA(cudaMemcpyAsync(&n, w->d_pair_count.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));

@@ -7,12 +7,22 @@
 
 namespace rp {
 
-// Broad phase of one scene with one CTA (known-answer entry point rp_broad_pairs).
+// Broad phase of one scene (known-answer entry point rp_broad_pairs), with the group the step uses
+// for it: one CTA for a scene of a batch, the cooperative grid (sort-based) for one large scene.
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) broad_kernel(WorldView<R> W, int s) {
     __shared__ int scan_smem[32];
     CtaGroup g;
     broad_phase(W, g, s, scan_smem);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) broad_grid_kernel(WorldView<R> W) {
+    __shared__ int scan_smem[32];
+    GridGroup g;
+    g.bar = W.barrier;
+    g.status = W.status;
+    broad_phase(W, g, 0, scan_smem);
 }
 
 // Narrowphase of one body pair with one warp (known-answer entry point rp_contacts): transform the
@@ -76,7 +86,11 @@ struct Launcher {
         return cudaGetLastError();
     }
 
-    static cudaError_t broad(const WorldView<R>& W, int s, cudaStream_t st) {
+    static cudaError_t broad(const WorldView<R>& W, int s, int grid_blocks, cudaStream_t st) {
+        if (grid_blocks > 0) {
+            void* args[] = {(void*)&W};
+            return cudaLaunchCooperativeKernel((const void*)broad_grid_kernel<R>, dim3(grid_blocks), dim3(BLOCK), args, 0, st);
+        }
         broad_kernel<R><<<1, BLOCK, 0, st>>>(W, s);
         return cudaGetLastError();
     }

@@ -8,7 +8,9 @@ int grid_blocks_per_sm_f32() { return Launcher<float, false>::grid_blocks_per_sm
 cudaError_t step_f32(const WorldView<float>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st) {
     return Launcher<float, false>::step(W, P, grid, blocks, st);
 }
-cudaError_t broad_f32(const WorldView<float>& W, int scene, cudaStream_t st) { return Launcher<float, false>::broad(W, scene, st); }
+cudaError_t broad_f32(const WorldView<float>& W, int scene, int grid_blocks, cudaStream_t st) {
+    return Launcher<float, false>::broad(W, scene, grid_blocks, st);
+}
 cudaError_t contacts_f32(const WorldView<float>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st) {
     return Launcher<float, false>::contacts(W, a, b, out, cap, count, st);
 }

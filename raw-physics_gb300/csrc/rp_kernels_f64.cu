@@ -8,7 +8,9 @@ int grid_blocks_per_sm_f64() { return Launcher<double, true>::grid_blocks_per_sm
 cudaError_t step_f64(const WorldView<double>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st) {
     return Launcher<double, true>::step(W, P, grid, blocks, st);
 }
-cudaError_t broad_f64(const WorldView<double>& W, int scene, cudaStream_t st) { return Launcher<double, true>::broad(W, scene, st); }
+cudaError_t broad_f64(const WorldView<double>& W, int scene, int grid_blocks, cudaStream_t st) {
+    return Launcher<double, true>::broad(W, scene, grid_blocks, st);
+}
 cudaError_t contacts_f64(const WorldView<double>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st) {
     return Launcher<double, true>::contacts(W, a, b, out, cap, count, st);
 }

@@ -31,7 +31,7 @@ struct PipeMarks {
     cudaError_t configure_##SUF();                                                                            \
     int grid_blocks_per_sm_##SUF();                                                                           \
     cudaError_t step_##SUF(const WorldView<R>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st); \
-    cudaError_t broad_##SUF(const WorldView<R>& W, int scene, cudaStream_t st);                               \
+    cudaError_t broad_##SUF(const WorldView<R>& W, int scene, int grid_blocks, cudaStream_t st);              \
     cudaError_t contacts_##SUF(const WorldView<R>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st); \
     cudaError_t pipe_configure_##SUF(PipeConfig& c, int sms);                                                 \
     cudaError_t pipe_frame_##SUF(const WorldView<R>& W, const StepParams& P, const PipeConfig& c, const PipeDims& d, \
