@@ -78,6 +78,8 @@ struct Launcher {
 
     static cudaError_t step(const WorldView<R>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st) {
         if (grid) {
+            cudaError_t e = cudaMemsetAsync(W.barrier, 0, sizeof(unsigned), st);   // grid barrier counter
+            if (e != cudaSuccess) return e;
             void* args[] = {(void*)&W, (void*)&P};
             return cudaLaunchCooperativeKernel((const void*)step_kernel_grid<R, EXACT>, dim3(blocks), dim3(BLOCK), args,
                                                smem_bytes(), st);
@@ -88,6 +90,8 @@ struct Launcher {
 
     static cudaError_t broad(const WorldView<R>& W, int s, int grid_blocks, cudaStream_t st) {
         if (grid_blocks > 0) {
+            cudaError_t e = cudaMemsetAsync(W.barrier, 0, sizeof(unsigned), st);   // grid barrier counter
+            if (e != cudaSuccess) return e;
             void* args[] = {(void*)&W};
             return cudaLaunchCooperativeKernel((const void*)broad_grid_kernel<R>, dim3(grid_blocks), dim3(BLOCK), args, 0, st);
         }

@@ -520,6 +520,9 @@ struct PipeLauncher {
                              cudaStream_t st, PipeMarks* marks) {
         cudaError_t e = cudaMemsetAsync(W.queue, 0, sizeof(int32_t), st);
         if (e != cudaSuccess) return e;
+        // the grid barrier's arrival counter starts every frame at zero (its cooperative kernels all
+        // run c.sms CTAs)
+        if (d.grid_mode && (e = cudaMemsetAsync(W.barrier, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
         auto mark = [&](int phase) -> cudaError_t {
             if (!marks || marks->n >= marks->cap) return cudaSuccess;
             marks->phase[marks->n] = phase;

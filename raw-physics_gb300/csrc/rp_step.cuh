@@ -39,24 +39,24 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     return v;
 }
 
+// Grid barrier of a cooperative launch: one arrival counter that only grows. The host zeroes it
+// before every frame (and before every other launch sequence that uses it), and every cooperative
+// kernel of a sequence has the same number of CTAs, so after k complete barriers the counter is
+// k * gridDim.x: a CTA arriving at count `old` waits until the count reaches the next multiple of
+// gridDim.x. One atomic per CTA and nothing else on the release path (no reset, no generation word).
 static __device__ __noinline__ void grid_barrier(unsigned* bar, uint32_t* status) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned gen = ld_acquire_gpu(&bar[1]);
-        __threadfence();
-        unsigned arrived = atomicAdd(&bar[0], 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        } else {
-            long long spins = 0;
-            while (ld_acquire_gpu(&bar[1]) == gen) {
-                __nanosleep(40);
-                if (++spins > BARRIER_SPIN_LIMIT) { atomicOr(status, (uint32_t)ST_BARRIER_TIMEOUT); break; }
-                // after one barrier has given up, later ones do not wait again
-                if ((spins & 1023) == 0 && (*(volatile uint32_t*)status & ST_BARRIER_TIMEOUT)) break;
-            }
+        const unsigned nb = gridDim.x;
+        __threadfence();                                   // this CTA's writes before its arrival
+        const unsigned old = atomicAdd(&bar[0], 1u);
+        const unsigned target = old - old % nb + nb;
+        long long spins = 0;
+        while ((int)(ld_acquire_gpu(&bar[0]) - target) < 0) {
+            __nanosleep(20);
+            if (++spins > BARRIER_SPIN_LIMIT) { atomicOr(status, (uint32_t)ST_BARRIER_TIMEOUT); break; }
+            // after one barrier has given up, later ones do not wait again
+            if ((spins & 1023) == 0 && (*(volatile uint32_t*)status & ST_BARRIER_TIMEOUT)) break;
         }
         __threadfence();
     }

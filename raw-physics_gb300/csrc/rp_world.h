@@ -171,7 +171,7 @@ struct WorldView {
     int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
     // ---- control ----------------------------------------------------------------------------
     uint32_t* status;        // [S] status bits per scene
-    unsigned int* barrier;   // [2] grid barrier counter / generation
+    unsigned int* barrier;   // [1] grid barrier arrival counter (zeroed before each launch sequence)
     unsigned long long* counters; // [32] diagnostics: gjk/epa iterations and cap hits, contacts, pair cycles
     unsigned long long* phase_ns; // [PHASES] time spent per phase of the step, seen by group rank 0
 };
