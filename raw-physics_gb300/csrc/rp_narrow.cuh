@@ -541,8 +541,20 @@ struct EpaFastSmem {
 
 __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, uchar4 f, V3<float>& n_out, float& d_out, int& status) {
     V3<float> a = poly[f.x], b = poly[f.y], c = poly[f.z];
-    V3<float> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
-    if (!(n.x != 0.f || n.y != 0.f || n.z != 0.f)) status |= ST_DEGENERATE;
+    const V3<float> e1 = vsub(b, a), e2 = vsub(c, a), cr = vcross(e1, e2);
+    V3<float> n;
+    if (vdot(cr, cr) > 1e-8f * vdot(e1, e1) * vdot(e2, e2)) {
+        n = vnorm(cr);
+    } else {
+        // A sliver face (|e1 x e2| <= 1e-4 |e1||e2|): FP32 resolves its normal only to about
+        // 6e-8 |e1||e2| / |e1 x e2|, or loses it entirely, so it is recomputed in FP64 from the same
+        // points. Only a normal that vanishes in FP64 too is the reference's degenerate face
+        // (epa.cpp:41 asserts on it).
+        const V3<double> A = v3cast<double>(a);
+        const V3<double> n64 = vnorm(vcross(vsub(v3cast<double>(b), A), vsub(v3cast<double>(c), A)));
+        if (!(n64.x != 0.0 || n64.y != 0.0 || n64.z != 0.0)) status |= ST_DEGENERATE;
+        n = v3cast<float>(n64);
+    }
     float d = vdot(n, a);
     if (d < -0.f) {
         n = vinv(n);
