@@ -136,6 +136,17 @@ rp_status rp_hull_create_from_topology(rp_world* w, const double* vertices, int3
                                        const int32_t* v2f_start, const int32_t* v2f, const int32_t* v2n_start,
                                        const int32_t* v2n, const int32_t* f2n_start, const int32_t* f2n,
                                        int32_t* out_hull);
+/* Hull preprocessing (no counterpart in the reference, which rebuilds every hull from its OBJ file at
+ * start-up). rp_hull_from_obj: a hull from an OBJ file's `v` and `f` lines (indices 1-based or
+ * negative; texture / normal indices ignored), one vertex per face corner in face order and positions
+ * stored as FP32 then scaled per axis in FP64, as obj_parse (src/render/obj.cpp:7-80) and
+ * examples_util.cpp:5-24 do; polygons are split as a fan, so only triangle files (the reference's
+ * own assets are) reproduce tinyobj's vertex order exactly. rp_hull_save writes a built hull's
+ * topology to a binary file (little-endian, checksummed); rp_hull_load restores it without
+ * rebuilding (RP_ERR_INVALID on a bad or corrupt file). */
+rp_status rp_hull_from_obj(rp_world* w, const char* path, const double scale[3], int32_t* out_hull);
+rp_status rp_hull_save(rp_world* w, int32_t hull, const char* path);
+rp_status rp_hull_load(rp_world* w, const char* path, int32_t* out_hull);
 /* Topology queries of a built hull (for tests): counts, then the arrays. */
 rp_status rp_hull_info(rp_world* w, int32_t hull, int32_t* num_vertices, int32_t* num_faces);
 /* One topology table of a hull in CSR form: which = 0 face boundary loops, 1 vertex->faces,

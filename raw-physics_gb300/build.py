@@ -1,14 +1,15 @@
 """Build the GB300 extension in place: raw-physics_gb300/librawphys_gb300.so.
 
-Nine translation units, compiled in parallel:
+Eleven translation units, compiled in parallel:
   csrc/rp_kernels_f32.cu   FP32 build of the persistent step kernels (nvcc, sm_103a)
   csrc/rp_kernels_f64.cu   all-FP64 build, no FMA contraction        (nvcc, sm_103a, -fmad=false)
   csrc/rp_pipe_f32.cu      FP32 build of the phase-major kernels     (nvcc, sm_103a)
   csrc/rp_pipe_f64.cu      all-FP64 phase-major kernels              (nvcc, sm_103a, -fmad=false)
   csrc/rp_noalloc.cu       static device scratch of the no-allocation contact query (nvcc)
-  csrc/rp_adjoint.cu       adjoint of the collision-free substep     (nvcc, sm_103a, -fmad=false)
+  csrc/rp_adjoint.cu       adjoint of the substep                    (nvcc, sm_103a, -fmad=false)
   csrc/rp_host.cpp         runtime + C ABI (include/rp.h)            (host compiler)
   csrc/rp_hull.cpp         hull topology and mass properties        (host compiler)
+  csrc/rp_hull_io.cpp      OBJ input and the binary hull cache       (host compiler)
   csrc/rp_shim.cpp         C++-mangled pbd_simulate drop-in          (host compiler)
 Host code is compiled with -ffp-contract=off so the set-up arithmetic keeps the reference's FP64
 rounding on both x86-64 and aarch64.
@@ -48,6 +49,7 @@ def _units():
         ("rp_adjoint.cu", cu_common + ["-fmad=false"]),
         ("rp_host.cpp", cxx),
         ("rp_hull.cpp", cxx),
+        ("rp_hull_io.cpp", cxx),
         ("rp_shim.cpp", cxx),
     ]
 

@@ -45,6 +45,9 @@ SIGNATURES = {
     "rp_hull_info": (_i, [_W, _i, _P(_i), _P(_i)]),
     "rp_hull_topology": (_i, [_W, _i, _i, _P(_i), _P(_i), _i, _P(_i), _P(_i)]),
     "rp_hull_geometry": (_i, [_W, _i, _P(_d), _P(_d)]),
+    "rp_hull_from_obj": (_i, [_W, C.c_char_p, _P(_d), _P(_i)]),
+    "rp_hull_save": (_i, [_W, _i, C.c_char_p]),
+    "rp_hull_load": (_i, [_W, C.c_char_p, _P(_i)]),
     "rp_hull_face": (_i, [_W, _i, _i, _P(_d), _P(_i), _i, _P(_i)]),
     "rp_entity_create": (_i, [_W, _i, _P(_d), _P(_d), _d, _i, _P(ColliderDesc), _u, _d, _d, _d, _P(_i)]),
     "rp_entity_set_velocity": (_i, [_W, _i, _P(_d), _P(_d)]),
@@ -151,6 +154,23 @@ class World:
         out = _i()
         self._check(self.lib.rp_hull_create(self.h, _dp(v), v.shape[0], idx.ctypes.data_as(_P(_u)), idx.shape[0],
                                             C.byref(out)))
+        return out.value
+
+    def hull_from_obj(self, path: str, scale=(1.0, 1.0, 1.0)) -> int:
+        """A hull from an OBJ file, as the reference's examples build theirs (rp_hull_from_obj)."""
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        out = _i()
+        self._check(self.lib.rp_hull_from_obj(self.h, os.fsencode(path), _dp(sc), C.byref(out)))
+        return out.value
+
+    def hull_save(self, hull: int, path: str) -> None:
+        """Write a built hull's topology to a binary cache file (rp_hull_save)."""
+        self._check(self.lib.rp_hull_save(self.h, hull, os.fsencode(path)))
+
+    def hull_load(self, path: str) -> int:
+        """A hull restored from a cache file written by hull_save (rp_hull_load)."""
+        out = _i()
+        self._check(self.lib.rp_hull_load(self.h, os.fsencode(path), C.byref(out)))
         return out.value
 
     def hull_faces(self, hull: int):

@@ -171,3 +171,65 @@ def test_domino_batch_generator():
         assert b.vel[idx[-1], 0] >= 4.0                               # the cube flies at the row
     b2, last2, target2 = S.domino_batch(12, seed=4)
     assert np.array_equal(b.pos, b2.pos) and np.array_equal(target, target2)
+
+
+def _cube_obj(quads=False, negative=False):
+    """A unit-half-extent cube as OBJ text: 8 positions, faces as triangles with v/vt/vn indices (or
+    as quads), optionally with negative (relative) indices."""
+    v = [(x, y, z) for x in (-1.0, 1.0) for y in (-1.0, 1.0) for z in (-1.0, 1.0)]
+    quads_ccw = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    lines = ["# test cube"] + ["v %.6f %.6f %.6f" % p for p in v] + ["vt 0 0", "vn 0 0 1"]
+    def ref(i):
+        return str(i - 8) if negative else str(i + 1)
+    tris = []
+    for q in quads_ccw:
+        if quads:
+            lines.append("f " + " ".join(ref(i) for i in q))
+        else:
+            for t in ((q[0], q[1], q[2]), (q[0], q[2], q[3])):
+                lines.append("f " + " ".join("%s/1/1" % ref(i) for i in t))
+                tris.append(t)
+    return "\n".join(lines) + "\n", np.asarray(v), tris
+
+
+def test_hull_from_obj_and_binary_cache(ext_built, tmp_path):
+    rp = ext_built
+    w = rp.World(-1, "fp64")
+    text, v, tris = _cube_obj()
+    obj = tmp_path / "cube.obj"
+    obj.write_text(text)
+    scale = (0.5, 0.25, 2.0)
+    h = w.hull_from_obj(str(obj), scale)
+    # the per-corner arrays obj_parse hands to collider_convex_hull_create: FP32 positions scaled in FP64
+    corners = np.array([v[i].astype(np.float32).astype(np.float64) * scale for t in tris for i in t])
+    assert w.hull(corners, np.arange(len(corners), dtype=np.uint32)) == h      # identical input, shared hull
+    nv, faces = w.hull_faces(h)
+    assert nv == 8 and len(faces) == 6                                         # coplanar triangles merged
+    # negative indices and quads (split as a fan) give the same solid
+    obj2 = tmp_path / "cube_neg_quads.obj"
+    obj2.write_text(_cube_obj(quads=True, negative=True)[0])
+    h2 = w.hull_from_obj(str(obj2), scale)
+    v2, n2, _ = w.hull_topology(h2)
+    v1, n1, _ = w.hull_topology(h)
+    assert sorted(map(tuple, v2)) == sorted(map(tuple, v1))
+    # binary cache: the restored hull has the same geometry and tables
+    cache = tmp_path / "cube.rphull"
+    w.hull_save(h, str(cache))
+    h3 = w.hull_load(str(cache))
+    assert h3 != h
+    a, b = w.hull_topology(h), w.hull_topology(h3)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for k in a[2]:
+        assert np.array_equal(a[2][k][0], b[2][k][0]) and np.array_equal(a[2][k][1], b[2][k][1])
+    # a damaged cache or a malformed OBJ is refused
+    raw = bytearray(cache.read_bytes())
+    raw[40] ^= 0xFF
+    bad = tmp_path / "bad.rphull"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.hull_load(str(bad))
+    bad_obj = tmp_path / "bad.obj"
+    bad_obj.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 9\n")
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.hull_from_obj(str(bad_obj))
+    w.close()
