@@ -26,6 +26,10 @@ static rp_status fail(rp_status code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
+
+// the same error reporting for the host units outside this file (rp_hull_io.cpp)
+rp_status report_error(rp_status code, const char* msg) { return fail(code, msg); }
+
 #define RP_CUDA(call)                                                                                        \
     do {                                                                                                     \
         cudaError_t e_ = (call);                                                                             \

@@ -18,7 +18,13 @@
 
 #include "rp.h"
 
+namespace rp {
+rp_status report_error(rp_status code, const char* msg);   // rp_host.cpp: sets rp_last_error
+}
+
 namespace {
+
+using rp::report_error;
 
 // File layout (little-endian): magic, version, six counts, then the arrays in this order, then an
 // FNV-1a 64-bit hash of every preceding byte.
@@ -83,8 +89,8 @@ bool obj_index(const char* tok, int32_t nverts, int32_t& out) {
 extern "C" {
 
 rp_status rp_hull_save(rp_world* w, int32_t hull, const char* path) {
-    if (!w || !path) return RP_ERR_INVALID;
-    if (!little_endian()) return RP_ERR_INVALID;
+    if (!w || !path) return report_error(RP_ERR_INVALID, "null argument");
+    if (!little_endian()) return report_error(RP_ERR_INVALID, "the hull cache format is little-endian");
     int32_t nv = 0, nf = 0;
     rp_status s = rp_hull_info(w, hull, &nv, &nf);
     if (s != RP_OK) return s;
@@ -107,58 +113,59 @@ rp_status rp_hull_save(rp_world* w, int32_t hull, const char* path) {
     const uint64_t h = fnv1a(out.data(), out.size());
     put(out, &h, 1);
     FILE* f = fopen(path, "wb");
-    if (!f) return RP_ERR_INVALID;
+    if (!f) return report_error(RP_ERR_INVALID, "cannot open the hull cache for writing");
     const bool ok = fwrite(out.data(), 1, out.size(), f) == out.size();
-    return (fclose(f) == 0 && ok) ? RP_OK : RP_ERR_INVALID;
+    return (fclose(f) == 0 && ok) ? RP_OK : report_error(RP_ERR_INVALID, "cannot write the hull cache");
 }
 
 rp_status rp_hull_load(rp_world* w, const char* path, int32_t* out_hull) {
-    if (!w || !path || !out_hull) return RP_ERR_INVALID;
-    if (!little_endian()) return RP_ERR_INVALID;
+    if (!w || !path || !out_hull) return report_error(RP_ERR_INVALID, "null argument");
+    if (!little_endian()) return report_error(RP_ERR_INVALID, "the hull cache format is little-endian");
     FILE* f = fopen(path, "rb");
-    if (!f) return RP_ERR_INVALID;
+    if (!f) return report_error(RP_ERR_INVALID, "cannot open the hull cache");
     std::vector<unsigned char> in;
     unsigned char buf[1 << 16];
     size_t got;
     while ((got = fread(buf, 1, sizeof(buf), f)) > 0) in.insert(in.end(), buf, buf + got);
     fclose(f);
-    if (in.size() < 8 + 4 + 24 + 8) return RP_ERR_INVALID;
+    if (in.size() < 8 + 4 + 24 + 8) return report_error(RP_ERR_INVALID, "hull cache too short");
     uint64_t h = 0;
     memcpy(&h, in.data() + in.size() - 8, 8);
-    if (h != fnv1a(in.data(), in.size() - 8)) return RP_ERR_INVALID;
+    if (h != fnv1a(in.data(), in.size() - 8)) return report_error(RP_ERR_INVALID, "hull cache checksum mismatch");
     in.resize(in.size() - 8);
     size_t off = 0;
     char magic[8];
     uint32_t version = 0;
     int32_t c[6];
-    if (!get(in, off, magic, 8) || memcmp(magic, kMagic, 8) != 0) return RP_ERR_INVALID;
-    if (!get(in, off, &version, 1) || version != kVersion) return RP_ERR_INVALID;
-    if (!get(in, off, c, 6)) return RP_ERR_INVALID;
+    if (!get(in, off, magic, 8) || memcmp(magic, kMagic, 8) != 0) return report_error(RP_ERR_INVALID, "not a hull cache");
+    if (!get(in, off, &version, 1) || version != kVersion) return report_error(RP_ERR_INVALID, "unknown hull cache version");
+    if (!get(in, off, c, 6)) return report_error(RP_ERR_INVALID, "hull cache truncated");
     for (int k = 0; k < 6; ++k)
-        if (c[k] < 0 || c[k] > kMaxElems) return RP_ERR_INVALID;
+        if (c[k] < 0 || c[k] > kMaxElems) return report_error(RP_ERR_INVALID, "hull cache counts out of range");
     const int32_t nv = c[0], nf = c[1];
-    if (nv <= 0 || nf <= 0) return RP_ERR_INVALID;
+    if (nv <= 0 || nf <= 0) return report_error(RP_ERR_INVALID, "hull cache counts out of range");
     std::vector<double> verts(3 * (size_t)nv), normals(3 * (size_t)nf);
-    if (!get(in, off, verts.data(), verts.size()) || !get(in, off, normals.data(), normals.size())) return RP_ERR_INVALID;
+    if (!get(in, off, verts.data(), verts.size()) || !get(in, off, normals.data(), normals.size()))
+        return report_error(RP_ERR_INVALID, "hull cache truncated");
     const int32_t rows[4] = {nf, nv, nv, nf};
     std::vector<int32_t> st[4], dt[4];
     for (int k = 0; k < 4; ++k) {
         st[k].resize((size_t)rows[k] + 1);
         dt[k].resize((size_t)(c[2 + k] > 0 ? c[2 + k] : 1));
         if (!get(in, off, st[k].data(), st[k].size()) || !get(in, off, dt[k].data(), (size_t)c[2 + k]))
-            return RP_ERR_INVALID;
-        if (st[k][0] != 0 || st[k].back() != c[2 + k]) return RP_ERR_INVALID;
+            return report_error(RP_ERR_INVALID, "hull cache truncated");
+        if (st[k][0] != 0 || st[k].back() != c[2 + k]) return report_error(RP_ERR_INVALID, "hull cache table inconsistent");
     }
-    if (off != in.size()) return RP_ERR_INVALID;
+    if (off != in.size()) return report_error(RP_ERR_INVALID, "hull cache has trailing bytes");
     // index ranges and row monotonicity are checked by rp_hull_create_from_topology
     return rp_hull_create_from_topology(w, verts.data(), nv, normals.data(), nf, st[0].data(), dt[0].data(), st[1].data(),
                                         dt[1].data(), st[2].data(), dt[2].data(), st[3].data(), dt[3].data(), out_hull);
 }
 
 rp_status rp_hull_from_obj(rp_world* w, const char* path, const double scale[3], int32_t* out_hull) {
-    if (!w || !path || !scale || !out_hull) return RP_ERR_INVALID;
+    if (!w || !path || !scale || !out_hull) return report_error(RP_ERR_INVALID, "null argument");
     FILE* f = fopen(path, "rb");
-    if (!f) return RP_ERR_INVALID;
+    if (!f) return report_error(RP_ERR_INVALID, "cannot open the OBJ file");
     std::vector<float> pos;            // the file's positions, as tinyobj stores them (FP32)
     std::vector<double> corners;       // one vertex per face corner, in face order (obj.cpp:45-80)
     std::string line;
@@ -194,7 +201,8 @@ rp_status rp_hull_from_obj(rp_world* w, const char* path, const double scale[3],
         }
     }
     fclose(f);
-    if (bad || corners.empty()) return RP_ERR_INVALID;
+    if (bad) return report_error(RP_ERR_INVALID, "malformed OBJ: a v line without three numbers or a bad face index");
+    if (corners.empty()) return report_error(RP_ERR_INVALID, "OBJ file without faces");
     const uint32_t n = (uint32_t)(corners.size() / 3);
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; ++i) idx[i] = i;

@@ -226,10 +226,10 @@ def test_hull_from_obj_and_binary_cache(ext_built, tmp_path):
     raw[40] ^= 0xFF
     bad = tmp_path / "bad.rphull"
     bad.write_bytes(bytes(raw))
-    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID.*checksum"):
         w.hull_load(str(bad))
     bad_obj = tmp_path / "bad.obj"
     bad_obj.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 9\n")
-    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID.*face index"):
         w.hull_from_obj(str(bad_obj))
     w.close()
