@@ -420,6 +420,17 @@ def measure_batched(args, dev, rank, world_size, plain_value):
            "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_frames, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_frames}
     value = nd * batch.substeps * args.batched_steps * world_size / (total_ms / 1e3)
     sizes = batch.scene_sizes()
+    # roofline of the batched form's dominant kernel, the position sweep (k_sweep_warp, one launch per
+    # substep): the same algorithmic bytes per contact and per solved pair as the plain form's
+    phase = {k: round((p1[k] - p0[k]) / 2, 3) for k in p0}
+    steps = args.batched_steps
+    alg_bytes = ((c1[5] - c0[5]) / steps * SWEEP_CONTACT_B + (c1[2] - c0[2]) / steps * SWEEP_NODE_B) / batch.substeps
+    launch_ms = phase["solve"] / (batch.substeps * batch.pos_iters)
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+    peak, peak_kind = measured_peak_hbm()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "kernel": "k_sweep_warp (position sweep, one warp per scene)",
+                "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms}
     out = {"value": value, "unit": UNIT, "ms_per_step": total_ms / args.batched_steps, "steps": args.batched_steps,
            "vs_plain_gpu": value / plain_value if plain_value else None,
            "workload": "%d independent scenes, dynamic bodies per scene log-uniform in [2, 512] (mean %.1f, max %d; "
@@ -432,7 +443,7 @@ def measure_batched(args, dev, rank, world_size, plain_value):
            "l2": "flushed (256 MiB write) before every timed frame",
            "pairs_per_step": (c1[6] - c0[6]) / args.batched_steps,
            "contacts_per_step": (c1[5] - c0[5]) / args.batched_steps,
-           "phase_ms_per_step": {k: round((p1[k] - p0[k]) / 2, 3) for k in p0},
+           "phase_ms_per_step": phase, "roofline": roofline,
            "e2e": e2e, "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches,
            "autotuned": tuned}
     w.close()
@@ -490,6 +501,7 @@ def run_batched_only(args, dev, rank, world_size):
                            "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
                            "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
                            "phase_ms_per_step": b["phase_ms_per_step"]},
+                "roofline": b["roofline"],
                 "gpu_launches": b["gpu_launches"], "e2e": b["e2e"], "clocks": b["clocks"],
                 "device_status": b["device_status"]}
         print(json.dumps(line), flush=True)
