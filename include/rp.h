@@ -140,8 +140,9 @@ rp_status rp_hull_create_from_topology(rp_world* w, const double* vertices, int3
  * start-up). rp_hull_from_obj: a hull from an OBJ file's `v` and `f` lines (indices 1-based or
  * negative; texture / normal indices ignored), one vertex per face corner in face order and positions
  * stored as FP32 then scaled per axis in FP64, as obj_parse (src/render/obj.cpp:7-80) and
- * examples_util.cpp:5-24 do; polygons are split as a fan, so only triangle files (the reference's
- * own assets are) reproduce tinyobj's vertex order exactly. rp_hull_save writes a built hull's
+ * examples_util.cpp:5-24 do, polygons triangulated by the ear clipping of the reference's OBJ
+ * loader (tinyobj, include/tiny_obj_loader.h) so that the corner order is the reference's.
+ * rp_hull_save writes a built hull's
  * topology to a binary file (little-endian, checksummed); rp_hull_load restores it without
  * rebuilding (RP_ERR_INVALID on a bad or corrupt file). */
 rp_status rp_hull_from_obj(rp_world* w, const char* path, const double scale[3], int32_t* out_hull);

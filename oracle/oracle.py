@@ -75,9 +75,10 @@ class Oracle:
                 "orc_hull_topology": (i, [i, i, i, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
                 "orc_hull_geometry": (i, [i, i, P(d), P(d), C.c_int32, C.c_int32, P(C.c_int32)]),
                 "orc_last_contacts": (u, [P(C.c_int32), P(d), u]),
+                "orc_obj_parse": (u, [C.c_char_p, P(C.c_float), u]),
             }
             for name, (res, args) in sig.items():
-                if not hasattr(lib, name):   # orc_last_contacts exists in the port only
+                if not hasattr(lib, name):   # orc_last_contacts: port only; orc_obj_parse: reference only
                     continue
                 f = getattr(lib, name)
                 f.restype = res
@@ -86,6 +87,15 @@ class Oracle:
         self.kind = kind
         self.lib = Oracle._cache[path]
         self.scene = None
+
+    def obj_corners(self, path: str) -> np.ndarray:
+        """Reference harness only: the face-corner positions (FP32) the reference's OBJ reader emits
+        for a file, in its order (obj_parse, src/render/obj.cpp:7-80)."""
+        f = self.lib.orc_obj_parse
+        n = f(os.fsencode(path), None, 0)
+        out = np.zeros((max(n, 1), 3), dtype=np.float32)
+        f(os.fsencode(path), out.ctypes.data_as(C.POINTER(C.c_float)), n)
+        return out[:n]
 
     # -- scene -----------------------------------------------------------------------------
     def load(self, scene) -> "Oracle":

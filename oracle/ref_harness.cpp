@@ -1,7 +1,8 @@
 // Oracle harness around the reference's own physics sources — TEST INFRASTRUCTURE ONLY.
 //
 // oracle/Makefile compiles this file together with the reference's src/physics/*.cpp,
-// src/entity.cpp, src/quaternion.cpp and src/util.cpp, taken from where they lie in the
+// src/entity.cpp, src/quaternion.cpp, src/util.cpp and src/render/obj.cpp (the OBJ reader, for
+// the hull-from-OBJ fixtures), taken from where they lie in the
 // reference checkout, into oracle/_ref/libref_harness.so. It implements oracle/harness.h by
 // calling the reference's public functions exactly as its example scenes do
 // (src/examples/stack.cpp:86-104, src/examples/examples_util.cpp:5-24).
@@ -18,6 +19,7 @@
 #include "physics/gjk.h"
 #include "physics/epa.h"
 #include "physics/clipping.h"
+#include "render/obj.h"
 #include <vector>
 #include <string.h>
 #include "harness.h"
@@ -352,6 +354,23 @@ int orc_gjk_epa(int e1, int e2, double* out) {
     if (!epa(&a->colliders[0], &b->colliders[0], &simplex, &normal, &pen)) return 2;
     out[0] = normal.x; out[1] = normal.y; out[2] = normal.z; out[3] = pen;
     return 1;
+}
+
+// The reference's OBJ reader (obj_parse, src/render/obj.cpp:7-80): the face-corner positions it
+// emits, 3 floats each, in its order; returns their number (only the first `cap` are written).
+uint32_t orc_obj_parse(const char* path, float* out, uint32_t cap) {
+    Vertex* vertices = nullptr;
+    u32* indices = nullptr;
+    obj_parse(path, &vertices, &indices);
+    const uint32_t n = (uint32_t)array_length(vertices);
+    for (uint32_t i = 0; i < n && i < cap; ++i) {
+        out[3 * i + 0] = vertices[i].position.x;
+        out[3 * i + 1] = vertices[i].position.y;
+        out[3 * i + 2] = vertices[i].position.z;
+    }
+    array_free(vertices);
+    array_free(indices);
+    return n;
 }
 
 }  // extern "C"

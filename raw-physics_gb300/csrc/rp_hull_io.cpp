@@ -8,11 +8,14 @@
 // same from the file's `v` and `f` lines; rp_hull_save writes a built hull's topology so that
 // rp_hull_load can restore it without the construction. Everything here goes through the public
 // C ABI (rp_hull_create, rp_hull_topology, rp_hull_geometry, rp_hull_create_from_topology).
+#include <float.h>
+#include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <cstddef>
 #include <string>
 #include <vector>
 
@@ -82,6 +85,74 @@ bool obj_index(const char* tok, int32_t nverts, int32_t& out) {
     if (i < 0 || i >= nverts) return false;
     out = (int32_t)i;
     return true;
+}
+
+// Crossing-number point-in-triangle test on the projected coordinates (the even-odd rule)
+bool inside_tri(const float* xs, const float* ys, float tx, float ty) {
+    bool in = false;
+    for (int i = 0, j = 2; i < 3; j = i++) {
+        if (((ys[i] > ty) != (ys[j] > ty)) && (tx < (xs[j] - xs[i]) * (ty - ys[i]) / (ys[j] - ys[i]) + xs[i])) in = !in;
+    }
+    return in;
+}
+
+// Triangles of one polygon face, as the OBJ loader the reference uses produces them (ear clipping on
+// the polygon projected onto the two axes its first non-degenerate corner spans most; an ear is a
+// corner turning with the polygon's orientation whose triangle holds none of the other remaining
+// corners). Arithmetic in FP32, the loader's number type. A triangle face comes out as it is.
+void triangulate(const std::vector<float>& pos, const std::vector<int32_t>& poly, std::vector<int32_t>& tris) {
+    const size_t n = poly.size();
+    auto P = [&](int32_t v, int a) { return pos[3 * (size_t)v + (size_t)a]; };
+    int ax0 = 1, ax1 = 2;
+    for (size_t k = 0; k < n; ++k) {
+        const int32_t a = poly[k], b = poly[(k + 1) % n], c = poly[(k + 2) % n];
+        const float e0x = P(b, 0) - P(a, 0), e0y = P(b, 1) - P(a, 1), e0z = P(b, 2) - P(a, 2);
+        const float e1x = P(c, 0) - P(b, 0), e1y = P(c, 1) - P(b, 1), e1z = P(c, 2) - P(b, 2);
+        const float cx = fabsf(e0y * e1z - e0z * e1y), cy = fabsf(e0z * e1x - e0x * e1z), cz = fabsf(e0x * e1y - e0y * e1x);
+        const float eps = FLT_EPSILON;
+        if (cx > eps || cy > eps || cz > eps) {
+            if (!(cx > cy && cx > cz)) {
+                ax0 = 0;
+                if (cz > cx && cz > cy) ax1 = 1;
+            }
+            break;
+        }
+    }
+    float area = 0.0f;
+    for (size_t k = 0; k < n; ++k) {
+        const int32_t a = poly[k], b = poly[(k + 1) % n];
+        area += (P(a, ax0) * P(b, ax1) - P(a, ax1) * P(b, ax0)) * 0.5f;
+    }
+    std::vector<int32_t> rest = poly;
+    size_t guess = 0, budget = n, last_size = n;
+    while (rest.size() > 3 && budget > 0) {
+        const size_t m = rest.size();
+        if (guess >= m) guess -= m;
+        if (last_size != m) {
+            last_size = m;
+            budget = m;
+        } else {
+            --budget;
+        }
+        int32_t c3[3];
+        float xs[3], ys[3];
+        for (int k = 0; k < 3; ++k) {
+            c3[k] = rest[(guess + (size_t)k) % m];
+            xs[k] = P(c3[k], ax0);
+            ys[k] = P(c3[k], ax1);
+        }
+        const float turn = (xs[1] - xs[0]) * (ys[2] - ys[1]) - (ys[1] - ys[0]) * (xs[2] - xs[1]);
+        if (turn * area < 0.0f) { ++guess; continue; }
+        bool covers = false;
+        for (size_t o = 3; o < m && !covers; ++o) {
+            const int32_t t = rest[(guess + o) % m];
+            covers = inside_tri(xs, ys, P(t, ax0), P(t, ax1));
+        }
+        if (covers) { ++guess; continue; }
+        tris.insert(tris.end(), c3, c3 + 3);
+        rest.erase(rest.begin() + (std::ptrdiff_t)((guess + 1) % m));
+    }
+    if (rest.size() == 3) tris.insert(tris.end(), rest.begin(), rest.end());
 }
 
 }  // namespace
@@ -191,13 +262,12 @@ rp_status rp_hull_from_obj(rp_world* w, const char* path, const double scale[3],
                 if (!obj_index(tok, (int32_t)(pos.size() / 3), i)) { bad = true; break; }
                 poly.push_back(i);
             }
-            if (bad || poly.size() < 3) { bad = true; break; }
-            // polygons as a fan (v0, vk, vk+1); triangle files, the reference's own assets, are taken as they are
-            for (size_t k = 1; k + 1 < poly.size(); ++k) {
-                const int32_t tri[3] = {poly[0], poly[k], poly[k + 1]};
-                for (int32_t v : tri)
-                    for (int a = 0; a < 3; ++a) corners.push_back((double)pos[3 * (size_t)v + (size_t)a] * scale[a]);
-            }
+            if (bad) break;
+            if (poly.size() < 3) continue;   // the loader skips faces of fewer than three corners
+            std::vector<int32_t> tris;
+            triangulate(pos, poly, tris);
+            for (int32_t v : tris)
+                for (int a = 0; a < 3; ++a) corners.push_back((double)pos[3 * (size_t)v + (size_t)a] * scale[a]);
         }
     }
     fclose(f);

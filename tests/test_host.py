@@ -233,3 +233,24 @@ def test_hull_from_obj_and_binary_cache(ext_built, tmp_path):
     with pytest.raises(rp.RPError, match="RP_ERR_INVALID.*face index"):
         w.hull_from_obj(str(bad_obj))
     w.close()
+
+
+def test_hull_from_obj_matches_the_reference_reader(ext_built, tmp_path):
+    """rp_hull_from_obj hands the hull builder the same face corners, in the same order, as the
+    reference's OBJ reader (obj_parse with its vendored tinyobj loader; fixtures made by
+    tests/golden/make_obj_golden.py): triangle files with texture / normal indices, quads, hexagons
+    and octagons (ear clipping), negative indices. Equal corners give the identical hull id."""
+    rp = ext_built
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "obj_corners.npz"))
+    names = sorted(k[: -len("_corners")] for k in g.files if k.endswith("_corners"))
+    assert len(names) >= 5
+    w = rp.World(-1, "fp64")
+    scale = (0.7, 1.3, 0.9)
+    for name in names:
+        path = tmp_path / (name + ".obj")
+        path.write_text(str(g[name + "_text"]))
+        h = w.hull_from_obj(str(path), scale)
+        ref = g[name + "_corners"].astype(np.float64) * np.asarray(scale)
+        assert w.hull(ref, np.arange(len(ref), dtype=np.uint32)) == h, name
+    w.close()
