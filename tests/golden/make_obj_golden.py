@@ -4,7 +4,9 @@ Runs obj_parse (raw-physics' src/render/obj.cpp, with the vendored tinyobj loade
 oracle/_ref/libref_harness.so by oracle/Makefile) on a few OBJ files written by `obj_cases()` —
 triangles with texture / normal indices, quads, hexagons, negative indices — and stores, per case,
 the OBJ text and the face-corner positions (FP32) the reader emits, in its order. rp_hull_from_obj
-must hand the same corners to the hull builder. Regenerate with
+must hand the same corners to the hull builder. Also writes cube_half.rphull: the hull cache file
+rp_hull_save produces for the triangulated cube of tri_cube scaled by 0.5 (the format's fixture).
+Regenerate with
     make -C oracle ref && python tests/golden/make_obj_golden.py
 """
 from __future__ import annotations
@@ -62,7 +64,22 @@ def obj_cases():
     }
 
 
+def write_cache_fixture() -> None:
+    sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
+    import rawphys
+    rawphys.load_library()
+    w = rawphys.World(-1, "fp64")
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "tri_cube.obj")
+        with open(path, "w") as f:
+            f.write(_tri_cube())
+        h = w.hull_from_obj(path, (0.5, 0.5, 0.5))
+        w.hull_save(h, os.path.join(HERE, "cube_half.rphull"))
+    w.close()
+
+
 def main() -> None:
+    write_cache_fixture()
     from oracle.oracle import Oracle, reference_available
     if not reference_available():
         raise SystemExit("the reference harness is not built: make -C oracle ref")

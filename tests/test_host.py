@@ -6,9 +6,12 @@ from __future__ import annotations
 import ctypes as C
 import os
 import re
+import sys
 
 import numpy as np
 import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
 
 from conftest import ROOT, golden
 from make_golden import SCENES
@@ -253,4 +256,27 @@ def test_hull_from_obj_matches_the_reference_reader(ext_built, tmp_path):
         h = w.hull_from_obj(str(path), scale)
         ref = g[name + "_corners"].astype(np.float64) * np.asarray(scale)
         assert w.hull(ref, np.arange(len(ref), dtype=np.uint32)) == h, name
+    w.close()
+
+
+def test_hull_cache_format_is_stable(ext_built, tmp_path):
+    """The hull cache format is fixed: the committed file (the triangulated cube of half-extent 0.5,
+    written by rp_hull_save; tests/golden/make_obj_golden.py) loads into the hull the same cube's
+    OBJ builds, and saving that hull again gives the same bytes."""
+    rp = ext_built
+    from conftest import GOLDEN
+    import make_obj_golden as mk
+    fixture = os.path.join(GOLDEN, "cube_half.rphull")
+    w = rp.World(-1, "fp64")
+    h = w.hull_load(fixture)
+    obj = tmp_path / "tri_cube.obj"
+    obj.write_text(mk._tri_cube())
+    h2 = w.hull_from_obj(str(obj), (0.5, 0.5, 0.5))
+    a, b = w.hull_topology(h), w.hull_topology(h2)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for k in a[2]:
+        assert np.array_equal(a[2][k][0], b[2][k][0]) and np.array_equal(a[2][k][1], b[2][k][1])
+    out = tmp_path / "again.rphull"
+    w.hull_save(h2, str(out))
+    assert out.read_bytes() == open(fixture, "rb").read()
     w.close()
