@@ -280,3 +280,20 @@ def test_hull_cache_format_is_stable(ext_built, tmp_path):
     w.hull_save(h2, str(out))
     assert out.read_bytes() == open(fixture, "rb").read()
     w.close()
+
+
+def test_obj_fixtures_match_the_live_reference_reader(tmp_path):
+    """Where the reference harness is built (the reference checkout is present), its OBJ reader still
+    gives the committed corners."""
+    from oracle.oracle import Oracle, reference_available
+    if not reference_available():
+        pytest.skip("reference harness not built (no reference checkout)")
+    from conftest import GOLDEN
+    import make_obj_golden as mk
+    g = np.load(os.path.join(GOLDEN, "obj_corners.npz"))
+    o = Oracle("ref")
+    for name, text in mk.obj_cases().items():
+        path = tmp_path / (name + ".obj")
+        path.write_text(text)
+        assert str(g[name + "_text"]) == text, name
+        assert np.array_equal(o.obj_corners(str(path)), g[name + "_corners"]), name
