@@ -297,3 +297,15 @@ def test_obj_fixtures_match_the_live_reference_reader(tmp_path):
         path.write_text(text)
         assert str(g[name + "_text"]) == text, name
         assert np.array_equal(o.obj_corners(str(path)), g[name + "_corners"]), name
+
+
+def test_bench_roofline_inputs():
+    """bench.py's roofline inputs: the peak (MEASURED_PEAKS.json, or the stated fallback) and the
+    position sweep's DRAM traffic per launch from its committed ncu summary."""
+    sys.path.insert(0, ROOT)
+    import bench
+    peak, kind = bench.measured_peak_hbm()
+    assert peak > 1000.0 and kind in ("measured", "fallback")
+    traffic = bench.profile_traffic()
+    assert traffic is not None and traffic > 0.0
+    assert bench.SWEEP_CONTACT_B > 0 and bench.SWEEP_NODE_B > 0
