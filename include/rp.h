@@ -18,6 +18,12 @@
  *   Entity fields read/written in place          rp_state_get / rp_state_set (snapshot/restore)
  *   broad_get_collision_pairs   (broad.h:11)      rp_broad_pairs
  *   colliders_get_contacts      (collider.h:55)   rp_contacts
+ *   obj_parse (src/render/obj.cpp:7) + examples_util_create_single_convex_hull_collider_array
+ *                               (examples_util.cpp:5) rp_hull_from_obj
+ *
+ * Beyond the reference: the adjoint of the step (rp_adjoint_trajectory), a hull topology cache
+ * (rp_hull_save / rp_hull_load), launch-mode control and an autotuner, a no-allocation contact
+ * query, and diagnostics.
  *
  * Entities are numbered in creation order (the order entity_get_all returns, entity.cpp:88).
  * A world holds one or more independent scenes; rp_simulate advances all of them in one launch
