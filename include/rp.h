@@ -243,15 +243,24 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out_pairs, uint32
  * the device narrowphase. out: RP_CONTACT_DOUBLES per contact. */
 rp_status rp_contacts(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
 /* rp_contacts without any allocation: no cudaMalloc / cudaFree and no host heap allocation in the
- * call. For callers that must not allocate mid-frame: a render or debug thread drawing contact
- * points while the simulation thread holds the device (a device allocation synchronises the whole
- * device and stalls it), or a caller with a fixed memory budget. The contacts are computed into a
- * static device scratch of at most 64 contacts and copied into out; cap > 64 is rejected with
- * RP_ERR_CAPACITY, a pair with more contacts reports its full count with the first cap written. The
- * world must already be built on the device (it has been stepped), else RP_ERR_STATE. The first call
- * on a device looks up the scratch's address (set-up) and should come before any stream capture.
- * Calls on the same device must not overlap: they share the scratch. No counterpart in the
- * reference. */
+ * call. For callers that must not allocate mid-frame: a frame loop that draws or logs contact points
+ * between steps (a device allocation synchronises the whole device and stalls the other streams on
+ * it), or a caller with a fixed memory budget. The contacts are computed into a static device scratch
+ * of at most 64 contacts and copied into out; cap > 64 is rejected with RP_ERR_CAPACITY, a pair with
+ * more contacts reports its full count with the first cap written (cap 0 only counts).
+ *
+ * Like every call on a world, it must be serialised with the other calls on the same world (it reads
+ * the world's buffers and its kernel rewrites the pair's transformed hull vertices); a caller that
+ * queries from a second thread takes its own lock around both threads' calls.
+ * The world must already be built on the device (it has been stepped), else RP_ERR_STATE. Host-side
+ * state edits since the last step (rp_entity_set_velocity) are uploaded first through the world's
+ * existing staging buffer, without allocating; an edit that changes the layout (a new entity,
+ * constraint or hull) needs a step first (RP_ERR_STATE says so).
+ * The first call on a device looks up the scratch's address (set-up) and should come before any
+ * stream capture; every call synchronises the world's stream, so none may be made while that stream is
+ * being captured. The address stays valid for the process's lifetime: a cudaDeviceReset while the
+ * library is loaded is not supported. Calls on the same device must not overlap: they share the
+ * scratch. No counterpart in the reference. */
 #define RP_NOALLOC_MAX_CONTACTS 64
 rp_status rp_contacts_noalloc(rp_world* w, int32_t e1, int32_t e2, double* out, uint32_t cap, uint32_t* count);
 /* The collision constraints of the last substep of the last rp_simulate call, in the reference's

@@ -23,11 +23,13 @@ _D3 = C.c_double * 3
 _D4 = C.c_double * 4
 
 
-def build(ref: bool = False) -> None:
-    """Compile the port (always) and, when the reference checkout is present, the reference."""
+def build(ref: bool = False, ref_dir: str | None = None) -> None:
+    """Compile the port (always) and, when the reference checkout is present, the reference
+    (from ref_dir, else the Makefile's REF_DIR default)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        extra = ["REF_DIR=" + os.path.abspath(ref_dir)] if ref_dir else []
+        subprocess.run(["make", "-s", "-C", HERE, "ref", *extra], check=True)
 
 
 def reference_available() -> bool:

@@ -1466,9 +1466,19 @@ rp_status rp_contacts_noalloc(rp_world* w, int32_t e1, int32_t e2, double* out, 
     if (cap > (uint32_t)NOALLOC_MAX_CONTACTS)
         return fail(RP_ERR_CAPACITY, "rp_contacts_noalloc: cap exceeds the static scratch (64 contacts per call)");
     if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
-    if (w->static_dirty || !w->device_state_valid || !w->d_pos.p)
-        return fail(RP_ERR_STATE, "rp_contacts_noalloc: the device world is not built; step the world (rp_simulate) first");
+    if (w->static_dirty || !w->d_pos.p)
+        return fail(RP_ERR_STATE, "rp_contacts_noalloc: the device world is not built (new entities, constraints or "
+                                  "hulls since the last step); step the world (rp_simulate) first");
     RP_CUDA(cudaSetDevice(w->device));
+    if (!w->device_state_valid) {
+        // host-side edits since the last step: re-upload them through the existing pinned staging
+        // buffer (no allocation); a staging buffer too small would need one, so that case is refused
+        const StateLayout L(w->bodies.size(), w->rsize());
+        if (!w->h_state.p || w->h_state.bytes < L.total)
+            return fail(RP_ERR_STATE, "rp_contacts_noalloc: host-side edits since the last step need a step first");
+        rp_status s = upload_state(w);
+        if (s != RP_OK) return s;
+    }
     double* scratch = nullptr;
     int* d_count = nullptr;
     RP_CUDA(noalloc_scratch(w->device, &scratch, &d_count));

@@ -5,7 +5,9 @@
 // is looked up once per device, the first time the query runs on it (with that device current); that
 // first call therefore does the set-up and should come before any stream capture. Nothing in the
 // scratch has to start at zero: the kernel writes the count and every contact it reports. There is
-// one scratch per device, so calls on the same device must not overlap (they would race on it).
+// one scratch per device, so calls on the same device must not overlap (they would race on it). The
+// cached address lives as long as the loaded module: a cudaDeviceReset while the library is loaded
+// would leave it stale, and is not supported.
 #include <cuda_runtime.h>
 #include <mutex>
 #include "rp_launch.h"
