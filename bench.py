@@ -1,36 +1,41 @@
 """Benchmark of the GB300 rigid-body step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload large4096|stack10|batched]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batched|large4096|stack10]
 
-Workload (default): the single large scene — 4096 convex bodies (cube / icosahedron / 32-segment
-cylinder / 42-vertex icosphere, scale U(0.5,1.5), density 1) in a fixed 40x40x60 m box, dt=1/60,
-20 substeps, 1 position iteration, FP32 build with FP64 poses; seeded synthetic data. The scene is
-first advanced `--settle` frames (untimed) so the timed frames see the falling / colliding regime,
-then W warm-up frames, then K timed frames. A "step" is one pbd_simulate frame.
+Headline workload (default, "batched"): 16384 independent scenes in one world, dynamic bodies per scene
+log-uniform in [2, 512] (about 1.65 M in all), shapes drawn from cube / icosahedron / 32-segment cylinder
+/ 42-vertex icosphere with scale U(0.5, 1.5), a quarter of the scenes with 8-64-link hinge or spherical
+chains; dt = 1/60, 20 substeps, 1 position iteration, FP32 arithmetic with FP64 poses; every frame is
+one replay of the captured phase-major CUDA graph. Seeded synthetic data. The batch is first advanced
+`--batched-settle` frames (untimed), then W warm-up frames, then K timed frames. A "step" is one
+pbd_simulate frame of every scene.
 
 Printed JSON line (rank 0):
   value     body-substeps/s = dynamic bodies x substeps x K / summed device time of the K frames
             (CUDA events on the world's stream; L2 flushed with a 256 MiB write before every frame)
-  e2e       the same metric through the C ABI with host buffers: every frame uploads the full body
-            state (rp_state_set), steps, and downloads it (rp_state_get), copies inside the timer
-  roofline  the dominant kernel (the position sweep, one launch per substep): its algorithmic
-            bytes per launch / its average duration from CUDA events around each phase, against
-            the measured HBM copy bandwidth
-  cpu_baseline  the oracle port (plain-C restatement of the reference, bit-exact to it) on one host
-            core, on a bounded sample of the same workload
-  batched   the batched form beside it: 16384 independent scenes of 2-512 bodies (a quarter with
-            hinge / spherical chains) in one world, one CUDA-graph replay per frame
-  precision the precision-stress report: 128 towers of 64 cubes (masses 1:100, 50 substeps) run
-            in the FP32 and the all-FP64 builds side by side for 300 frames (per-step error from
-            identical states, trajectory divergence, tower drift, energy drift)
+  e2e       the same metric through the C ABI with host buffers: every frame uploads the whole batch's
+            state from pinned host memory (rp_state_set), steps, and downloads it (rp_state_get); the
+            copies are inside the timer, the same L2 flush before every frame
+  step_err  per-step error of the first timed frame against the oracle (the FP64 restatement of the
+            reference, bit-exact to it) run from the same state, on a size-stratified sample of scenes:
+            position (m) and rotation angle (rad), median / p99 / max over the sampled dynamic bodies
+  roofline  the dominant kernel of the frame (from CUDA events around each phase) against the
+            measured HBM copy bandwidth: its algorithmic bytes per launch over its average duration
+  fp32_pipe FP32-pipe utilisation of GJK and EPA: algorithmic flops (device-counted support calls,
+            iterations and faces times the per-operation flop model) over time x nominal FP32 peak
+  cpu_baseline  the oracle port on one host core, on a bounded sample of the same workload
+  plain     the plain single-scene form beside it (4096 bodies, FP32 and the all-FP64 build), with its
+            own per-step error; vs_plain_gpu = batched / plain FP32
+  precision the precision-stress report: 128 towers of 64 cubes (masses 1:100, 50 substeps) run in the
+            FP32 and the all-FP64 builds side by side
   adjoint   grad/s of the adjoint (scene-gradients per second) on a bounded sample of the
-            differentiation workload: 152 of its 1024 domino scenes over 4 of its 120 frames
---workload batched measures the batched form alone (its value becomes the line's value).
---impl reference times that CPU implementation on every host core instead (one replica of the
-workload per core; the reference is single-threaded and keeps process-global state).
-Multi-GPU (torchrun): the single scene does not shard, so every rank steps its own replica
-("replicas only"); value is the sum over ranks of body-substeps over the slowest rank's time. The
-batched form shards by scene: every rank steps its own batch.
+            differentiation workload
+--workload large4096 / stack10 measure the plain form of that scene as the line's value.
+--impl reference times the reference's CPU algorithm (the oracle port, a bit-exact plain-C restatement
+of the reference) on every host core, on the same workload: a size-stratified sample of the batch's
+scenes, one process per core (the reference is single-threaded and keeps process-global state).
+Multi-GPU (torchrun): the batch shards by scene, every rank steps its own batch (weak scaling); the
+single scene does not shard ("replicas only").
 """
 from __future__ import annotations
 
@@ -49,13 +54,20 @@ sys.path.insert(0, ROOT)
 
 METRIC = "body-substeps/s batched vs plain GPU at ≤1e-4 m pos err vs FP64 CPU; grad/s"
 UNIT = "body-substeps/s"
-# Algorithmic bytes of the plain form (per substep): body state read + written, the pair list, and
-# every contact record written once and read by the position and velocity solves.
-STATE_READ_B, STATE_WRITE_B, PAIR_B, CONTACT_B = 160, 84, 16, 156
-# Algorithmic bytes of one position sweep (the dominant kernel): every contact record read (48 B)
-# and its two lambdas written back (8 B); per solved pair node, both bodies' pose read and written
-# (2 x 64 B) and their inverse mass and inertia read (2 x 28 B).
+# Algorithmic bytes of one position sweep: every contact record read (48 B) and its two lambdas
+# written back (8 B); per solved pair node, both bodies' pose read and written (2 x 64 B) and their
+# inverse mass and inertia read (2 x 28 B).
 SWEEP_CONTACT_B, SWEEP_NODE_B = 56, 2 * (64 + 64 + 28)
+# Algorithmic FP32 flops of the narrowphase (per device-counted operation): a support call is one dot
+# product and a compare per hull vertex (6 V); a GJK iteration's simplex update ~60; an EPA iteration
+# ~40 per new face plus 6 per face scanned.
+FLOP_SUPPORT_PER_VERT, FLOP_GJK_ITER, FLOP_EPA_ITER = 6, 60, 40 * 6 + 6 * 24
+NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
+BATCHED_WORKLOAD = ("batched16384: 16384 independent scenes, dynamic bodies per scene log-uniform in [2,512], "
+                    "cube/icosahedron/cylinder32/icosphere42 hulls at scale U(0.5,1.5), 25% of scenes with "
+                    "8-64-link hinge or spherical chains, dt=1/60, 20 substeps, 1 position iteration")
+PLAIN_WORKLOAD = ("large4096: one scene of 4096 dynamic bodies (cube/icosahedron/cylinder32/icosphere42, scale "
+                  "U(0.5,1.5)) in a 40x40x60 m box, dt=1/60, 20 substeps, 1 position iteration")
 
 
 def make_scene(name):
@@ -117,35 +129,144 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per position-sweep launch from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "pipeline_large4096.md")
+def profile_traffic(summary, kernel):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary (a line
+    `traffic_bytes_per_launch[<kernel>]: <bytes>`), or None with the reason."""
+    path = os.path.join(ROOT, "profiles", summary)
+    key = "traffic_bytes_per_launch[%s]:" % kernel
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
+            if line.startswith(key):
+                return float(line.split(":", 1)[1]), path
     except OSError:
-        pass
-    return None
+        return None, "missing " + path
+    return None, "no %s line in %s" % (key, path)
 
 
-def cpu_baseline_sample(scene, state, frames=3):
-    """The oracle port on one core: body-substeps/s over `frames` frames of the workload, started
-    from the state the timed GPU frames started from."""
-    from oracle.oracle import Oracle, build
-    build(ref=False)
+# ---------------------------------------------------------------------------------------------
+# Sampling of the batch for the CPU legs and the per-step error
+def stratified_scenes(batch, count):
+    """`count` scenes spread evenly over the batch's scenes sorted by body count (the sample has the
+    batch's size distribution, so its body-substeps/s stands for the whole batch's)."""
+    sizes = np.bincount(batch.scene, minlength=batch.num_scenes)
+    order = np.argsort(sizes, kind="stable")
+    pick = order[np.linspace(0, batch.num_scenes - 1, min(count, batch.num_scenes)).round().astype(int)]
+    return sorted(set(int(s) for s in pick))
+
+
+def oracle_frames(scene, state, frames):
+    """The oracle port: `frames` frames of `scene` from `state`; returns (end state, seconds, error bits)."""
+    from oracle.oracle import Oracle
     o = Oracle("port").load(scene)
     o.set_state(state)
     t = time.perf_counter()
     o.step(frames)
-    dt = time.perf_counter() - t
-    return scene.num_dynamic * scene.substeps * frames / dt, dt
+    return o.get_state(), time.perf_counter() - t, o.error_bits()
 
 
+# ---------------------------------------------------------------------------------------------
+# Reference arm: the reference's CPU algorithm on every host core
 _WORKER = {}
 
 
-def _ref_init(name, state):
+def _ref_pin(barrier):
+    """Pool initializer: every task below waits at this barrier once, so each of the pool's
+    processes takes exactly one task per map and keeps its own slice of the sample."""
+    _WORKER["barrier"] = barrier
+
+
+def _ref_load(job):
+    """Pool worker: keep its scenes of the batch sample and settle them on the CPU."""
+    sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle, build
+    build(ref=False)
+    scenes, settle = job
+    _WORKER["scenes"] = scenes
+    _WORKER["states"] = []
+    for _, sc in scenes:
+        o = Oracle("port").load(sc)
+        o.step(settle)
+        _WORKER["states"].append(o.get_state())
+    _WORKER["barrier"].wait()
+    return [s for s, _ in scenes]
+
+
+def _ref_frame(_):
+    """Pool worker: one frame of each of its own scenes from their settled states; returns
+    (body-substeps, seconds, its scene ids)."""
+    from oracle.oracle import Oracle
+    work, secs = 0, 0.0
+    for (_, sc), st in zip(_WORKER["scenes"], _WORKER["states"]):
+        o = Oracle("port").load(sc)
+        o.set_state(st)
+        t = time.perf_counter()
+        o.step(1)
+        secs += time.perf_counter() - t
+        work += sc.num_dynamic * sc.substeps
+    _WORKER["barrier"].wait()
+    return work, secs, [s for s, _ in _WORKER["scenes"]]
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle.oracle import build
+    from rawphys import scenes as S
+    build(ref=False)
+    cores = os.cpu_count() or 1
+    if args.workload != "batched":
+        return run_reference_plain(args, cores)
+    batch = S.batched_scenes(args.batched_scenes, seed=0)
+    picks = stratified_scenes(batch, args.ref_scenes)
+    sizes = np.bincount(batch.scene[~batch.fixed], minlength=batch.num_scenes)
+    # every core owns a fixed slice of the sample (balanced by bodies), settles it, then times frames
+    order = sorted(picks, key=lambda s: -int(sizes[s]))
+    slices = [[] for _ in range(cores)]
+    load = [0] * cores
+    for s in order:
+        k = int(np.argmin(load))
+        slices[k].append(s)
+        load[k] += int(sizes[s])
+    slices = [sl for sl in slices if sl]
+    ctx = mp.get_context("spawn")
+    jobs = [([(x, S.batch_scene(batch, x)) for x in sl], args.batched_settle) for sl in slices]
+    n = len(jobs)
+    barrier = ctx.Barrier(n)
+    with ctx.Pool(n, initializer=_ref_pin, initargs=(barrier,)) as pool:
+        owned = pool.map(_ref_load, jobs, chunksize=1)
+        assert sorted(x for o in owned for x in o) == sorted(picks)
+        for _ in range(args.warmup):
+            pool.map(_ref_frame, range(n), chunksize=1)
+        total, wall = 0, 0.0
+        for _ in range(args.steps):
+            res = pool.map(_ref_frame, range(n), chunksize=1)
+            assert sorted(x for _, _, o in res for x in o) == sorted(picks), "a process ran another's slice"
+            total += sum(b for b, _, _ in res)
+            # a step lasts as long as its slowest process spent inside the step calls (re-loading a
+            # scene into the single-scene harness between frames is not part of the reference's step)
+            wall += max(t for _, t, _ in res)
+    value = total / wall
+    nd_sample = int(sum(sizes[s] for s in picks))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": BATCHED_WORKLOAD},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
+                             "sample": "%d of the %d scenes, evenly spaced in body-count order (%d of %d dynamic "
+                                       "bodies), each settled %d frames on the CPU, then one frame of all of them per "
+                                       "step over %d processes (a step lasts as long as the slowest process's step "
+                                       "calls); oracle port, a bit-exact plain-C restatement of the reference "
+                                       "(-O2 -ffp-contract=off); the whole batch takes sum(N*S) / value per frame"
+                                       % (len(picks), batch.num_scenes, nd_sample, batch.num_dynamic,
+                                          args.batched_settle, n)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _plain_init(name, state):
     sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
     sys.path.insert(0, ROOT)
     from oracle.oracle import Oracle
@@ -155,7 +276,7 @@ def _ref_init(name, state):
     _WORKER["state"] = state
 
 
-def _ref_frame(frames):
+def _plain_frame(frames):
     o, scene = _WORKER["oracle"], _WORKER["scene"]
     o.set_state(_WORKER["state"])
     t = time.perf_counter()
@@ -163,64 +284,236 @@ def _ref_frame(frames):
     return scene.num_dynamic * scene.substeps * frames, time.perf_counter() - t
 
 
-def run_reference(args):
-    rank, world, _ = dist_info()
-    if rank != 0:
-        return
+def run_reference_plain(args, cores):
     import multiprocessing as mp
-    from oracle.oracle import Oracle, build
-    build(ref=False)
-    cores = os.cpu_count() or 1
+    from oracle.oracle import Oracle
     scene = make_scene(args.workload)
-    # the same settled frames the GPU arm times, settled by the CPU implementation itself
     o = Oracle("port").load(scene)
     o.step(args.settle)
     state = o.get_state()
-    frames = 1
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_ref_init, initargs=(args.workload, state)) as pool:
+    with ctx.Pool(cores, initializer=_plain_init, initargs=(args.workload, state)) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_frame, [frames] * cores)
+            pool.map(_plain_frame, [1] * cores)
         t = time.perf_counter()
         total = 0
         for _ in range(args.steps):
-            total += sum(b for b, _ in pool.map(_ref_frame, [frames] * cores))
+            total += sum(b for b, _ in pool.map(_plain_frame, [1] * cores))
         wall = time.perf_counter() - t
     value = total / wall
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
-            "config": {"workload": "%s: %d dynamic bodies, %d substeps, dt=1/60, 1 position iteration; frame %d "
-                                   "(after a %d-frame settle), one frame per core per step"
-                                   % (args.workload, scene.num_dynamic, scene.substeps, args.settle + 1, args.settle)},
+            "config": {"workload": PLAIN_WORKLOAD if args.workload == "large4096" else args.workload},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d replicas x %d frame(s) per step of the workload, oracle port (bit-exact "
-                                       "restatement of the reference, -O2 -ffp-contract=off)" % (cores, frames)},
+                             "sample": "%d replicas x 1 frame per step, frame %d after a %d-frame settle, oracle port"
+                                       % (cores, args.settle + 1, args.settle)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+# ---------------------------------------------------------------------------------------------
+# GPU arm
+def timed_frames(w, stream, flush, frames, clocks_gpu=None):
+    """Device time (ms) of each of `frames` frames, L2 flushed before each; optional clock samples."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    clk = ClockSampler(clocks_gpu) if clocks_gpu is not None else None
+    torch.cuda.synchronize()
+    if clk:
+        clk.__enter__()
+    for k in range(frames):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)              # evict L2 (129 MB) before each timed frame
+        ev[k][0].record(stream)
+        w.step(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__()
+    return [a.elapsed_time(b) for a, b in ev], (clk.summary() if clk else None)
+
+
+def phase_pass(w, start_state, frames):
+    """Per-phase ms per frame of `frames` frames from start_state (events after every phase)."""
+    w.set_state(start_state)
+    w.sync()
+    p0 = w.phase_times()
+    w.set_timing(True)
+    w.step(frames)
+    w.sync()
+    w.set_timing(False)
+    p1 = w.phase_times()
+    return {k: round((p1[k] - p0[k]) / frames, 4) for k in p0}
+
+
+def e2e_frames(w, stream, flush, start_state, frames):
+    """End to end through the C ABI with host buffers: per frame the whole state from pinned host
+    memory (rp_state_set), one step, the whole state back (rp_state_get); copies inside the timer."""
+    import torch
+    st = start_state
+    w.set_state(st)
+    w.step(1)
+    w.get_state()
+    b0 = w.transfer_bytes()
+    torch.cuda.synchronize()
+    wall = 0.0
+    for k in range(frames):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        w.set_state(st)
+        w.step(1)
+        st = w.get_state()
+        wall += time.perf_counter() - t
+    b1 = w.transfer_bytes()
+    return wall, (b1[0] - b0[0]) // frames, (b1[1] - b0[1]) // frames
+
+
+def narrow_flops(c0, c1, frames, verts_avg):
+    """Algorithmic FP32 flops per frame of GJK and of EPA from the device counters."""
+    gjk_iters = (c1[0] - c0[0]) / frames
+    epa_iters = (c1[1] - c0[1]) / frames
+    # every GJK iteration and every EPA iteration makes one Minkowski support call (two hull scans)
+    gjk = gjk_iters * (FLOP_GJK_ITER + 2 * FLOP_SUPPORT_PER_VERT * verts_avg)
+    epa = epa_iters * (FLOP_EPA_ITER + 2 * FLOP_SUPPORT_PER_VERT * verts_avg)
+    return gjk, epa
+
+
+def fp32_pipe(c0, c1, frames, phase, verts_avg):
+    gjk, epa = narrow_flops(c0, c1, frames, verts_avg)
+    out = {"peak_tflops": NOMINAL_FP32_TFLOPS, "peak_kind": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
+           "model": "support call 6 flop per hull vertex per hull, GJK 60 flop per iteration, EPA ~400 flop per "
+                    "iteration; counts from the device counters"}
+    for name, flops, key in (("k_gjk", gjk, "gjk"), ("k_epa", epa, "epa")):
+        ms = phase.get(key, 0.0)
+        ach = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+        out[name] = {"gflop_per_frame": flops / 1e9, "ms_per_frame": ms, "achieved_tflops": ach,
+                     "frac": ach / NOMINAL_FP32_TFLOPS}
+    return out
+
+
+def roofline_of(phase, c0, c1, frames, substeps, pos_iters, kernels, summary):
+    """Roofline object of the dominant kernel. The position sweep (one launch per substep and
+    iteration) has the HBM byte model above; other phases are reported with their share only."""
+    peak, peak_kind = measured_peak_hbm()
+    sweeps = substeps * pos_iters
+    alg_bytes = ((c1[5] - c0[5]) / frames * SWEEP_CONTACT_B + (c1[2] - c0[2]) / frames * SWEEP_NODE_B) / substeps
+    launch_ms = phase["solve"] / sweeps if sweeps else 0.0
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+    traffic, src = profile_traffic(summary, kernels["solve"])
+    frame_ms = sum(phase.values())
+    shares = {k: (v / frame_ms if frame_ms else 0.0) for k, v in phase.items()}
+    dom = max(phase, key=lambda k: phase[k])
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else 0.0,
+            "peak_kind": peak_kind, "traffic": traffic, "traffic_source": src, "kernel": kernels["solve"],
+            "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
+            "kernel_share_of_frame": shares.get("solve", 0.0), "dominant_phase": dom,
+            "phase_share": {k: round(v, 4) for k, v in shares.items()}}
+
+
+def measure_batched(args, dev, rank, world_size, with_oracle):
+    """The headline: the batched form (rawphys.scenes.batched_scenes), every frame one replay of the
+    captured phase-major graph. Weak scaling: every rank steps its own batch (seed = rank)."""
     import torch
     import rawphys
-    rank, world_size, local = dist_info()
-    if world_size > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        torch.cuda.set_device(local)
-    dev = local
-    torch.cuda.set_device(dev)
-    if args.workload == "batched":
-        run_batched_only(args, dev, rank, world_size)
-        return
-    stream = torch.cuda.Stream(dev)          # a capturable stream: frames replay from a CUDA graph
-    scene = make_scene(args.workload)
+    from rawphys import scenes as S
+    from rawphys.precision import step_error
+    batch = S.batched_scenes(args.batched_scenes, seed=rank)
+    stream = torch.cuda.Stream(dev)
     w = rawphys.World(dev, "fp32")
     w.set_stream(stream.cuda_stream)
+    w.load_batch(batch)
+    w.step(args.batched_settle)
+    tuned = w.autotune(frames=2) if args.autotune else None
+    w.step(args.warmup)
+    w.sync()
+    nd = batch.num_dynamic
+    start_state = w.get_state()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    w.degenerate_info()                       # clear: count what the timed frames meet
+    c0 = w.counters()
+    l0 = w.kernel_launches()
+    if world_size > 1:
+        torch.distributed.barrier()
+    ms, clocks = timed_frames(w, stream, flush, args.steps, clocks_gpu=dev)
+    if world_size > 1:
+        torch.distributed.barrier()
+    total_ms = float(sum(ms))
+    c1 = w.counters()
+    launches = w.kernel_launches() - l0
+    status = w.status()
+    degenerate = w.degenerate_info()
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = nd * batch.substeps * args.steps * world_size / (total_ms / 1e3)
+    phase = phase_pass(w, start_state, 2)
+    # the first timed frame again, from its start state: the GPU's answer for the per-step error
+    w.set_state(start_state)
+    w.step(1)
+    first = w.get_state()
+    e2e_wall, h2d, d2h = e2e_frames(w, stream, flush, start_state, args.e2e_frames)
+    e2e = {"value": nd * batch.substeps * args.e2e_frames * world_size / e2e_wall, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    w.close()
+    verts = np.array([m.positions.shape[0] for m in batch.meshes], dtype=np.float64)
+    verts_avg = float(np.mean(verts[batch.mesh]))
+    out = {"value": value, "total_ms": total_ms, "ms": ms, "clocks": clocks, "launches": launches, "status": status,
+           "degenerate_first": degenerate, "phase": phase, "e2e": e2e, "tuned": tuned, "nd": nd,
+           "roofline": roofline_of(phase, c0, c1, args.steps, batch.substeps, batch.pos_iters,
+                                   {"solve": "k_sweep_warp (position sweep, one warp per scene)"}, "pipeline_batched16384.md"),
+           "fp32_pipe": fp32_pipe(c0, c1, args.steps, phase, verts_avg),
+           "pairs_per_step": (c1[6] - c0[6]) / args.steps, "contacts_per_step": (c1[5] - c0[5]) / args.steps}
+    if with_oracle:
+        # the oracle on a size-stratified sample of scenes, one frame from the same start state:
+        # the per-step error of the GPU's frame, and the 1-core CPU baseline of the same work
+        picks = stratified_scenes(batch, args.err_scenes)
+        got, exp, dyn = [], [], []
+        cpu_work, cpu_secs, bits = 0, 0.0, 0
+        for s in picks:
+            idx = np.nonzero(batch.scene == s)[0]
+            sc = S.batch_scene(batch, s)
+            end, secs, eb = oracle_frames(sc, start_state[idx], 1)
+            got.append(first[idx])
+            exp.append(end)
+            dyn.append(~batch.fixed[idx])
+            cpu_work += sc.num_dynamic * sc.substeps
+            cpu_secs += secs
+            bits |= eb
+        out["step_err"] = step_error(np.concatenate(got), np.concatenate(exp), np.concatenate(dyn))
+        out["step_err"]["scenes"] = len(picks)
+        out["step_err"]["oracle_assert_bits"] = bits
+        out["cpu_baseline"] = {"value": cpu_work / cpu_secs, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "%d of the %d scenes, stratified by body count, one frame each from the state "
+                                         "the timed GPU frames start from; oracle port (bit-exact plain-C restatement "
+                                         "of the reference), %.1f s" % (len(picks), batch.num_scenes, cpu_secs)}
+    sizes = batch.scene_sizes()
+    out["workload_detail"] = ("%d scenes, dynamic bodies per scene mean %.1f max %d (%d in all), %d scenes with chains "
+                              "(%d joints); frames %d-%d after a %d-frame settle and %d warm-up frames"
+                              % (batch.num_scenes, sizes.mean(), sizes.max(), nd,
+                                 len({int(batch.scene[c.e1]) for c in batch.constraints}), len(batch.constraints),
+                                 args.batched_settle + args.warmup, args.batched_settle + args.warmup + args.steps,
+                                 args.batched_settle, args.warmup))
+    return out
+
+
+def measure_plain(args, dev, precision, steps, start_from=None, with_oracle=False):
+    """The plain form: one large scene (the cooperative grid path). Returns its device-timed rate, phase
+    split, roofline, e2e and (with_oracle) the per-step error of its first timed frame."""
+    import torch
+    import rawphys
+    from rawphys.precision import step_error
+    scene = make_scene(args.workload if args.workload != "batched" else "large4096")
+    stream = torch.cuda.Stream(dev)
+    w = rawphys.World(dev, precision)
+    w.set_stream(stream.cuda_stream)
     w.load(scene)
-    nd = scene.num_dynamic
-    # untimed: settle into the colliding regime, pick the launch configuration, then warm up
-    if args.settle:
+    if start_from is not None:
+        w.set_state(start_from)
+    elif args.settle:
         w.step(args.settle)
     tuned = w.autotune(frames=3) if args.autotune else None
     w.step(args.warmup)
@@ -229,224 +522,34 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     c0 = w.counters()
     l0 = w.kernel_launches()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world_size > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xff)              # evict L2 (129 MB) before each timed frame
-            ev[k][0].record(stream)
-            w.step(1)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
-    if world_size > 1:
-        torch.distributed.barrier()
-    ms = [a.elapsed_time(b) for a, b in ev]
+    ms, clocks = timed_frames(w, stream, flush, steps, clocks_gpu=dev)
+    launches = w.kernel_launches() - l0
+    c1 = w.counters()
     total_ms = float(sum(ms))
-    launches = w.kernel_launches() - l0
-    c1 = w.counters()
-    # phase breakdown: the same frames again, untimed by the bench, with an event after every phase
+    value = scene.num_dynamic * scene.substeps * steps / (total_ms / 1e3)
+    phase = phase_pass(w, start_state, min(steps, 5))
     w.set_state(start_state)
-    w.sync()
-    p0 = w.phase_times()
-    w.set_timing(True)
-    w.step(args.steps)
-    w.sync()
-    w.set_timing(False)
-    p1 = w.phase_times()
-    phase_ms = {k: round((p1[k] - p0[k]) / args.steps, 4) for k in p0}
-    # slowest rank
-    if world_size > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = nd * scene.substeps * args.steps * world_size / (total_ms / 1e3)
-    status = w.status()
-
-    # roofline of the dominant kernel, the position sweep (one launch per substep): algorithmic bytes
-    # per launch over its duration, both from the phase pass (CUDA events around each phase)
-    pairs_per_step = (c1[6] - c0[6]) / args.steps
-    contacts_per_step = (c1[5] - c0[5]) / args.steps
-    manifolds_per_step = (c1[2] - c0[2]) / args.steps
-    sweeps = scene.substeps * scene.pos_iters
-    alg_bytes = (contacts_per_step * SWEEP_CONTACT_B + manifolds_per_step * SWEEP_NODE_B) / scene.substeps
-    launch_ms = phase_ms["solve"] / sweeps
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
-    peak, peak_kind = measured_peak_hbm()
-    traffic = profile_traffic()
-
-    # end to end through the C ABI with host buffers, over the same frames the device-timed loop ran
-    # (from its start state; two untimed frames first)
-    st = start_state
-    for _ in range(2):
-        w.set_state(st)
-        w.step(1)
-        w.get_state()
-    st = start_state
-    b0 = w.transfer_bytes()
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    e2e_steps = max(3, args.steps // 2)
-    for _ in range(e2e_steps):
-        w.set_state(st)
-        w.step(1)
-        st = w.get_state()
-    e2e_wall = time.perf_counter() - t
-    b1 = w.transfer_bytes()
-    e2e = {"value": nd * scene.substeps * e2e_steps * world_size / e2e_wall, "unit": UNIT,
-           "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_steps, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_steps}
-
-    w.close()
-    batched = measure_batched(args, dev, rank, world_size, value) if args.batched_scenes > 0 else None
-    adjoint = measure_adjoint(args, dev) if args.adjoint_scenes > 0 and rank == 0 else None
-    precision = None
-    if args.precision_towers > 0 and rank == 0:
-        from rawphys import scenes as S
-        from rawphys.precision import precision_report
-        precision = precision_report(rawphys, S.tower_batch(args.precision_towers, n=64, seed=0),
-                                     frames=args.precision_frames, sample_every=max(1, args.precision_frames // 6),
-                                     device=dev)
-        precision["workload"] = ("%d towers of 64 unit cubes, masses alternating 1:100, 50 substeps, dt=1/60; FP32 build "
-                                 "against the all-FP64 build (bit-identical to the FP64 CPU oracle, tests/test_gpu_precision.py)"
-                                 % args.precision_towers)
-
-    if rank == 0:
-        cpu_v, cpu_t = cpu_baseline_sample(scene, start_state, frames=args.cpu_frames)
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-                "config": {"workload": "large single scene: %d dynamic bodies (cube/icosahedron/cylinder32/icosphere42, "
-                                       "scale U(0.5,1.5)) in a 40x40x60 m box, dt=1/60, %d substeps, 1 position iteration, "
-                                       "FP32 with FP64 poses; frames %d-%d after a %d-frame settle"
-                                       % (nd, scene.substeps, args.settle + args.warmup,
-                                          args.settle + args.warmup + args.steps, args.settle),
-                           "l2": "flushed (256 MiB write) before every timed frame",
-                           "parallelism": "replicas only" if world_size > 1 else "single scene, one GPU",
-                           "pairs_per_step": pairs_per_step, "contacts_per_step": contacts_per_step,
-                           "levels_per_step": (c1[7] - c0[7]) / args.steps,
-                           "gjk_iters_per_step": (c1[0] - c0[0]) / args.steps,
-                           "epa_calls_per_step": (c1[2] - c0[2]) / args.steps,
-                           "epa_iters_per_step": (c1[1] - c0[1]) / args.steps,
-                           "gjk_cap_hits_per_step": (c1[8] - c0[8]) / args.steps,
-                           "gjk_cycles_detected_per_step": (c1[18] - c0[18]) / args.steps,
-                           "epa_cap_hits_per_step": (c1[9] - c0[9]) / args.steps,
-                           "pair_cycles_max": c1[10],
-                           "pair_cycles_mean": (c1[11] - c0[11]) / max(1, c1[12] - c0[12]),
-                           "pairs_narrowphased_per_step": (c1[12] - c0[12]) / args.steps,
-                           "pairs_bounds_apart_per_step": (c1[13] - c0[13]) / args.steps,
-                           "gjk_epa_manifold_support_cycles_per_step": [(c1[k] - c0[k]) / args.steps for k in (14, 15, 16, 17)],
-                           "phase_ms_per_step": phase_ms, "autotuned": tuned},
-                "gpu_launches": launches,
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_sweep_grid (position sweep)",
-                             "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms},
-                "batched": batched,
-                "adjoint": adjoint,
-                "precision": precision,
-                "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
-                                 "sample": "%d frames of the same scene from the state the timed GPU frames start "
-                                           "from, oracle port (bit-exact restatement of the reference), %.1f s"
-                                           % (args.cpu_frames, cpu_t)},
-                "e2e": e2e, "clocks": clk.summary(), "device_status": status}
-        print(json.dumps(line), flush=True)
-    if world_size > 1:
-        torch.distributed.destroy_process_group()
-
-
-def measure_batched(args, dev, rank, world_size, plain_value):
-    """The batched form: many independent scenes of uneven size in one world (rawphys.scenes.
-    batched_scenes), every frame one replay of the captured phase-major graph. Weak scaling: every
-    rank steps its own batch (seed = rank)."""
-    import torch
-    import rawphys
-    from rawphys import scenes as S
-    batch = S.batched_scenes(args.batched_scenes, seed=rank)
-    stream = torch.cuda.Stream(dev)
-    w = rawphys.World(dev, "fp32")
-    w.set_stream(stream.cuda_stream)
-    w.load_batch(batch)
-    w.step(args.batched_settle)
-    tuned = w.autotune(frames=2) if args.autotune else None
-    w.step(3)
-    w.sync()
-    nd = batch.num_dynamic
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    c0 = w.counters()
-    l0 = w.kernel_launches()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.batched_steps)]
-    if world_size > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        for k in range(args.batched_steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xff)
-            ev[k][0].record(stream)
-            w.step(1)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
-    total_ms = float(sum(a.elapsed_time(b) for a, b in ev))
-    c1 = w.counters()
-    launches = w.kernel_launches() - l0
-    if world_size > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    p0 = w.phase_times()
-    w.set_timing(True)
-    w.step(2)
-    w.sync()
-    w.set_timing(False)
-    p1 = w.phase_times()
-    # end to end through the C ABI with host buffers: every frame uploads the whole batch's state,
-    # steps, and downloads it
-    st = w.get_state()
-    w.set_state(st)
     w.step(1)
-    st = w.get_state()
-    b0 = w.transfer_bytes()
-    e2e_frames = 3
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for _ in range(e2e_frames):
-        w.set_state(st)
-        w.step(1)
-        st = w.get_state()
-    e2e_wall = time.perf_counter() - t
-    b1 = w.transfer_bytes()
-    e2e = {"value": nd * batch.substeps * e2e_frames * world_size / e2e_wall, "unit": UNIT,
-           "h2d_bytes_per_step": (b1[0] - b0[0]) // e2e_frames, "d2h_bytes_per_step": (b1[1] - b0[1]) // e2e_frames}
-    value = nd * batch.substeps * args.batched_steps * world_size / (total_ms / 1e3)
-    sizes = batch.scene_sizes()
-    # roofline of the batched form's dominant kernel, the position sweep (k_sweep_warp, one launch per
-    # substep): the same algorithmic bytes per contact and per solved pair as the plain form's
-    phase = {k: round((p1[k] - p0[k]) / 2, 3) for k in p0}
-    steps = args.batched_steps
-    alg_bytes = ((c1[5] - c0[5]) / steps * SWEEP_CONTACT_B + (c1[2] - c0[2]) / steps * SWEEP_NODE_B) / batch.substeps
-    launch_ms = phase["solve"] / (batch.substeps * batch.pos_iters)
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
-    peak, peak_kind = measured_peak_hbm()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_kind": peak_kind, "kernel": "k_sweep_warp (position sweep, one warp per scene)",
-                "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms}
-    out = {"value": value, "unit": UNIT, "ms_per_step": total_ms / args.batched_steps, "steps": args.batched_steps,
-           "vs_plain_gpu": value / plain_value if plain_value else None,
-           "workload": "%d independent scenes, dynamic bodies per scene log-uniform in [2, 512] (mean %.1f, max %d; "
-                       "%d dynamic bodies in all), large-scene shape mix, %d scenes with 8-64-link hinge or spherical "
-                       "chains (%d joints), dt=1/60, %d substeps, FP32 with FP64 poses; frames %d-%d after a %d-frame "
-                       "settle" % (batch.num_scenes, sizes.mean(), sizes.max(), nd,
-                                   len({int(batch.scene[c.e1]) for c in batch.constraints}), len(batch.constraints),
-                                   batch.substeps, args.batched_settle + 3, args.batched_settle + 3 + args.batched_steps,
-                                   args.batched_settle),
-           "l2": "flushed (256 MiB write) before every timed frame",
-           "pairs_per_step": (c1[6] - c0[6]) / args.batched_steps,
-           "contacts_per_step": (c1[5] - c0[5]) / args.batched_steps,
-           "phase_ms_per_step": phase, "roofline": roofline,
-           "e2e": e2e, "clocks": clk.summary(), "device_status": w.status(), "gpu_launches": launches,
-           "autotuned": tuned}
+    first = w.get_state()
+    e2e_wall, h2d, d2h = e2e_frames(w, stream, flush, start_state, max(3, steps // 2))
+    status = w.status()
     w.close()
+    out = {"value": value, "unit": UNIT, "precision": precision, "ms_per_step": total_ms / steps, "steps": steps,
+           "clocks": clocks, "gpu_launches": launches, "device_status": status, "phase_ms_per_step": phase,
+           "autotuned": tuned, "start_state": start_state,
+           "e2e": {"value": scene.num_dynamic * scene.substeps * max(3, steps // 2) / e2e_wall, "unit": UNIT,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "roofline": roofline_of(phase, c0, c1, steps, scene.substeps, scene.pos_iters,
+                                   {"solve": "k_sweep_grid (position sweep, cooperative grid)"}, "pipeline_large4096.md"),
+           "pairs_per_step": (c1[6] - c0[6]) / steps, "contacts_per_step": (c1[5] - c0[5]) / steps,
+           "levels_per_step": (c1[7] - c0[7]) / steps}
+    if with_oracle:
+        end, secs, bits = oracle_frames(scene, start_state, 1)
+        out["step_err"] = step_error(first, end, ~scene.fixed)
+        out["step_err"]["oracle_assert_bits"] = bits
+        out["cpu_baseline"] = {"value": scene.num_dynamic * scene.substeps / secs, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "1 frame of the scene from the state the timed GPU frames start from, oracle "
+                                         "port, %.1f s" % secs}
     return out
 
 
@@ -454,8 +557,7 @@ def measure_adjoint(args, dev):
     """grad/s of the adjoint on a bounded sample of the differentiation workload (1024 domino rows of
     16-64 with a thrown cube, loss |x_last - target|^2 after 120 steps, gradients with respect to
     initial v / w, masses and friction, checkpoints every 10 steps): the first `adjoint_scenes` scenes
-    of the same generator over `adjoint_frames` frames. The adjoint runs one scene per GPU thread in
-    FP64; its time grows linearly with the frames and, above one scene per SM, with the scenes."""
+    of the same generator over `adjoint_frames` frames."""
     import torch
     import rawphys
     from rawphys import scenes as S
@@ -489,21 +591,88 @@ def measure_adjoint(args, dev):
             "gradient_check": "FP64 central differences, tests/test_gpu_adjoint.py (relative error <= 1e-3)"}
 
 
-def run_batched_only(args, dev, rank, world_size):
-    """--workload batched: the batched form alone, as the line's own value."""
+def run_ours(args):
     import torch
-    b = measure_batched(args, dev, rank, world_size, None)
+    import rawphys
+    rank, world_size, local = dist_info()
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = local
+    torch.cuda.set_device(dev)
+    if args.workload != "batched":
+        run_plain_only(args, dev, rank, world_size)
+        return
+    b = measure_batched(args, dev, rank, world_size, with_oracle=(rank == 0))
+    plain = {}
+    if rank == 0 and args.plain:
+        p32 = measure_plain(args, dev, "fp32", args.plain_steps, with_oracle=True)
+        p64 = measure_plain(args, dev, "fp64", max(3, args.plain_steps // 3), start_from=p32["start_state"])
+        for p in (p32, p64):
+            p.pop("start_state")
+        plain = {"workload": PLAIN_WORKLOAD + "; frames after a %d-frame settle" % args.settle,
+                 "fp32": p32, "fp64": p64, "fp32_over_fp64": p32["value"] / p64["value"]}
+    adjoint = measure_adjoint(args, dev) if args.adjoint_scenes > 0 and rank == 0 else None
+    precision = None
+    if args.precision_towers > 0 and rank == 0:
+        from rawphys import scenes as S
+        from rawphys.precision import precision_report
+        precision = precision_report(rawphys, S.tower_batch(args.precision_towers, n=64, seed=0),
+                                     frames=args.precision_frames, sample_every=max(1, args.precision_frames // 6),
+                                     device=dev)
+        precision["workload"] = ("%d towers of 64 unit cubes, masses alternating 1:100, 50 substeps, dt=1/60; FP32 build "
+                                 "against the all-FP64 build (bit-identical to the FP64 CPU oracle, tests/test_gpu_precision.py)"
+                                 % args.precision_towers)
     if rank == 0:
-        line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": world_size, "steps": b["steps"],
-                "warmup": 3, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-                "config": {"workload": b["workload"], "l2": b["l2"],
-                           "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
-                           "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
-                           "phase_ms_per_step": b["phase_ms_per_step"]},
+        line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": b["total_ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+                "config": {"workload": BATCHED_WORKLOAD},
+                "details": {"batch": b["workload_detail"], "l2": "flushed (256 MiB write) before every timed frame",
+                            "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
+                            "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
+                            "phase_ms_per_step": b["phase"], "autotuned": b["tuned"],
+                            "frame_ms": [round(x, 3) for x in b["ms"]]},
+                "gpu_launches": b["launches"],
+                "step_err": b.get("step_err"),
                 "roofline": b["roofline"],
-                "gpu_launches": b["gpu_launches"], "e2e": b["e2e"], "clocks": b["clocks"],
-                "device_status": b["device_status"]}
+                "fp32_pipe": b["fp32_pipe"],
+                "cpu_baseline": b.get("cpu_baseline"),
+                "e2e": b["e2e"], "clocks": b["clocks"], "device_status": b["status"],
+                "degenerate_first": b["degenerate_first"],
+                "vs_plain_gpu": b["value"] / plain["fp32"]["value"] if plain else None,
+                "plain": plain or None, "adjoint": adjoint, "precision": precision}
+        print(json.dumps(line), flush=True)
+    if world_size > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_plain_only(args, dev, rank, world_size):
+    """--workload large4096 / stack10: the plain form as the line's value (replicas under torchrun)."""
+    import torch
+    p = measure_plain(args, dev, "fp32", args.steps, with_oracle=(rank == 0))
+    total_ms = p["ms_per_step"] * args.steps
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    scene = make_scene(args.workload)
+    value = scene.num_dynamic * scene.substeps * args.steps * world_size / (total_ms / 1e3)
+    if rank == 0:
+        p.pop("start_state")
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+                "config": {"workload": PLAIN_WORKLOAD if args.workload == "large4096" else args.workload},
+                "details": {"parallelism": "replicas only" if world_size > 1 else "single scene, one GPU",
+                            "l2": "flushed (256 MiB write) before every timed frame",
+                            "phase_ms_per_step": p["phase_ms_per_step"], "autotuned": p["autotuned"],
+                            "pairs_per_step": p["pairs_per_step"], "contacts_per_step": p["contacts_per_step"],
+                            "levels_per_step": p["levels_per_step"]},
+                "gpu_launches": p["gpu_launches"], "step_err": p.get("step_err"), "roofline": p["roofline"],
+                "cpu_baseline": p.get("cpu_baseline"), "e2e": p["e2e"], "clocks": p["clocks"],
+                "device_status": p["device_status"]}
         print(json.dumps(line), flush=True)
     if world_size > 1:
         torch.distributed.destroy_process_group()
@@ -512,15 +681,18 @@ def run_batched_only(args, dev, rank, world_size):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--settle", type=int, default=120)
+    ap.add_argument("--settle", type=int, default=120, help="untimed frames before the plain form's timed frames")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="large4096", choices=["large4096", "stack10", "batched"])
-    ap.add_argument("--cpu-frames", type=int, default=2)
-    ap.add_argument("--batched-scenes", type=int, default=16384, help="0 skips the batched measurement")
-    ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--workload", default="batched", choices=["batched", "large4096", "stack10"])
+    ap.add_argument("--batched-scenes", type=int, default=16384)
     ap.add_argument("--batched-settle", type=int, default=20)
+    ap.add_argument("--e2e-frames", type=int, default=3)
+    ap.add_argument("--err-scenes", type=int, default=128, help="scenes of the batch the oracle checks")
+    ap.add_argument("--ref-scenes", type=int, default=256, help="scenes of the batch the reference arm runs")
+    ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the plain single-scene form")
+    ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--precision-towers", type=int, default=128, help="0 skips the precision-stress report")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default launch configuration")
     ap.add_argument("--precision-frames", type=int, default=300)

@@ -115,6 +115,13 @@ rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t num_substeps, u
                                 const int32_t* loss_entity, const double* target, double* loss_out, double* grad_v,
                                 double* grad_w, double* grad_mass, double* grad_friction);
 rp_status rp_world_set_mode(rp_world* w, int32_t mode);
+/* Bound of every device-side wait of this world (the grid barriers of a single large scene's
+ * cooperative kernels), in microseconds; 1 s by default, at most 60 s; 0 gives up at the first wait
+ * that finds its barrier incomplete. A wait that runs out abandons the frame: every CTA leaves the
+ * launch, the frame's remaining kernels return at once, rp_simulate restores the state it started
+ * from and returns RP_ERR_TIMEOUT (forces stay pending). The world stays usable. No counterpart in
+ * the reference, which has no device waits. */
+rp_status rp_world_set_wait_limit(rp_world* w, uint64_t microseconds);
 /* Autotuner (no counterpart in the reference): times `frames` frames of the world's current scenes
  * from their current state under each candidate launch configuration — launch mode, threads per
  * collider in the hull transform (4/8/16/32), and the sweep layout (levels swept by one CTA below
@@ -225,11 +232,20 @@ enum {
     RP_STATUS_CONTACT_OVERFLOW = 1 << 1,  /* contacts exceeded the scratch (the step is redone larger) */
     RP_STATUS_EPA_OVERFLOW = 1 << 2,      /* an EPA polytope outgrew its fixed storage; that pair was dropped */
     RP_STATUS_CLIP_OVERFLOW = 1 << 3,     /* a clipped polygon outgrew its fixed storage */
-    RP_STATUS_BARRIER_TIMEOUT = 1 << 4,   /* a bounded device barrier gave up */
+    RP_STATUS_BARRIER_TIMEOUT = 1 << 4,   /* a bounded device barrier gave up (rp_simulate undoes the call) */
     RP_STATUS_DEGENERATE = 1 << 5,        /* geometry the reference would reject with an assert */
     RP_STATUS_LEVEL_OVERFLOW = 1 << 6,    /* solver dependency depth exceeded its table */
-    RP_STATUS_EPA_NOT_CONVERGED = 1 << 8  /* informational: EPA hit its iteration cap (reference prints a warning) */
+    RP_STATUS_EPA_NOT_CONVERGED = 1 << 8, /* informational: EPA hit its iteration cap (reference prints a warning) */
+    /* which condition raised RP_STATUS_DEGENERATE (each comes with it) */
+    RP_STATUS_DEG_EPA_NORMAL = 1 << 9,    /* an EPA face whose normal vanishes (epa.cpp:41 asserts) */
+    RP_STATUS_DEG_EPA_COPLANAR = 1 << 10, /* an EPA face through the origin, every point in its plane (epa.cpp:72) */
+    RP_STATUS_DEG_SKEW = 1 << 11          /* edge-edge contact of parallel edges (clipping.cpp:279) */
 };
+/* The first degenerate condition the world met since the last call (the call clears it): out[0] its
+ * RP_STATUS_DEG_* bits (0: none), out[1] scene, out[2] / out[3] the pair's entities, out[4] the
+ * substep it was met in, counted from the world's last device build (phase-major and persistent
+ * forms). No counterpart in the reference, which aborts on these conditions. */
+rp_status rp_degenerate_info(rp_world* w, int64_t out[5]);
 
 /* -- state --------------------------------------------------------------------------------------- */
 rp_status rp_state_get(rp_world* w, double* out /* num_entities * RP_STATE_DOUBLES */);
@@ -283,11 +299,15 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
 rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */
 uint64_t  rp_kernel_launches(const rp_world* w);
-/* Device time per phase of the step kernel since creation, in ms, as seen by the first thread of
- * each scene's group (summed over scenes): [0] broad phase, [1] islands and sleeping, [2] solver
- * schedule, [3] predict, [4] hull transform, [5] narrowphase, [6] position solve, [7] velocity
- * update, [8] velocity solve. */
-rp_status rp_phase_times(rp_world* w, double out_ms[9]);
+/* Device time per phase of the step since creation, in ms (summed over frames): [0] broad phase,
+ * [1] islands and sleeping, [2] solver schedule, [3] predict, [4] hull transform, [5] narrowphase
+ * (persistent kernel: all of it; phase-major form: the cull kernel), [6] position solve, [7] velocity
+ * update, [8] velocity solve, [9] GJK, [10] EPA, [11] contact manifold (the phase-major form's
+ * narrowphase kernels). The phase-major form is timed with CUDA events after each kernel while
+ * timing is on (rp_set_timing; those frames run outside the CUDA graph); the persistent kernel with
+ * the global timer as seen by each scene's first thread. */
+#define RP_NUM_PHASES 12
+rp_status rp_phase_times(rp_world* w, double out_ms[RP_NUM_PHASES]);
 /* Bytes copied host->device (out[0]) and device->host (out[1]) by state and force transfers. */
 rp_status rp_transfer_bytes(rp_world* w, uint64_t out[2]);
 /* Average duration of the step kernel over the last rp_simulate, measured with CUDA events on the

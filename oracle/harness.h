@@ -74,6 +74,10 @@ void     orc_step(double dt, uint32_t num_substeps, uint32_t num_pos_iters, int 
  * order: entity pairs (2 each) and r1_lc[3] r2_lc[3] normal[3] lambda_n lambda_t (11 each). */
 uint32_t orc_last_contacts(int32_t* pairs, double* out, uint32_t cap);
 uint32_t orc_num_entities(void);
+/* Port only: which of the reference's assert conditions the steps since orc_reset met (0: none);
+ * bits 2 EPA face normal vanishes (epa.cpp:41), 4 EPA polytope coplanar with the origin (epa.cpp:72),
+ * 8 parallel skew lines (clipping.cpp:279), 1 any other. */
+int      orc_last_error(void);
 void     orc_get_state(double* out);
 void     orc_set_state(const double* in);
 

@@ -78,9 +78,10 @@ class Oracle:
                 "orc_hull_geometry": (i, [i, i, P(d), P(d), C.c_int32, C.c_int32, P(C.c_int32)]),
                 "orc_last_contacts": (u, [P(C.c_int32), P(d), u]),
                 "orc_obj_parse": (u, [C.c_char_p, P(C.c_float), u]),
+                "orc_last_error": (i, []),
             }
             for name, (res, args) in sig.items():
-                if not hasattr(lib, name):   # orc_last_contacts: port only; orc_obj_parse: reference only
+                if not hasattr(lib, name):   # orc_last_contacts / orc_last_error: port only; orc_obj_parse: reference only
                     continue
                 f = getattr(lib, name)
                 f.restype = res
@@ -89,6 +90,12 @@ class Oracle:
         self.kind = kind
         self.lib = Oracle._cache[path]
         self.scene = None
+
+    def error_bits(self) -> int:
+        """Port only: the reference assert conditions met since the scene was loaded (orc_last_error):
+        2 EPA face normal vanishes, 4 EPA polytope coplanar with the origin, 8 parallel skew lines,
+        1 any other."""
+        return int(self.lib.orc_last_error())
 
     def obj_corners(self, path: str) -> np.ndarray:
         """Reference harness only: the face-corner positions (FP32) the reference's OBJ reader emits

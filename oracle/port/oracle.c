@@ -34,7 +34,9 @@ static void iv_free(ivec* v) { free(v->a); v->a = NULL; v->n = v->cap = 0; }
 typedef struct { int x, y; } i2;
 typedef struct { int x, y, z; } i3;
 
-static int g_error = 0;
+static int g_error = 0;   /* bits: 1 other assert, 2 EPA face normal vanishes (epa.cpp:41),
+                           * 4 EPA polytope coplanar with the origin (epa.cpp:72), 8 parallel skew
+                           * lines (clipping.cpp:279) */
 
 /* ------------------------------------------------------------------------------------------ */
 /* Colliders (src/physics/collider.h:5-44) */
@@ -129,7 +131,7 @@ static face_t make_face(const tvec* tris, v3 normal) {
             e[j] = tmp;
         }
     }
-    if (n == 0 || e[0].x != e[n - 1].y) g_error = 1;
+    if (n == 0 || e[0].x != e[n - 1].y) g_error |= 1;
     face_t f;
     memset(&f, 0, sizeof(f));
     for (int i = 0; i < n; ++i) iv_push(&f.elements, e[i].x);
@@ -362,7 +364,7 @@ static m3 default_inertia(const collider_t* cs, int n, double mass) {
     }
     unsigned total = 0;
     for (int i = 0; i < n; ++i) {
-        if (cs[i].type != 1) { g_error = 1; return r; }
+        if (cs[i].type != 1) { g_error |= 1; return r; }
         total += (unsigned)cs[i].nv;
     }
     double mpv = mass / total;
@@ -418,7 +420,7 @@ int orc_entity_create(const double pos[3], const double rot[4], double mass, int
     } else {
         b->invm = 1.0 / mass;
         b->I = default_inertia(b->col, b->ncol, mass);
-        if (!m3_inverse(b->I, &b->Iinv)) g_error = 1;
+        if (!m3_inverse(b->I, &b->Iinv)) g_error |= 1;
     }
     b->fixed = fixed;
     b->active = 1;
@@ -562,7 +564,7 @@ static void simplex_add(simplex_t* s, v3 p) {
     case 1: s->b = s->a; s->a = p; break;
     case 2: s->c = s->b; s->b = s->a; s->a = p; break;
     case 3: s->d = s->c; s->c = s->b; s->b = s->a; s->a = p; break;
-    default: g_error = 1; break;
+    default: g_error |= 1; break;
     }
     s->num++;
 }
@@ -674,7 +676,7 @@ static int gjk(const collider_t* c1, const collider_t* c2, simplex_t* out) {
         case 2: hit = do_simplex_2(&s, &dir); break;
         case 3: hit = do_simplex_3(&s, &dir); break;
         case 4: hit = do_simplex_4(&s, &dir); break;
-        default: g_error = 1; return 0;
+        default: g_error |= 1; return 0;
         }
         if (hit) { *out = s; return 1; }
     }
@@ -691,7 +693,7 @@ static void vv_push(v3vec* v, v3 x) {
 static void face_normal_distance(i3 f, const v3* poly, int npoly, v3* out_n, double* out_d) {
     v3 a = poly[f.x], b = poly[f.y], c = poly[f.z];
     v3 n = v_norm(v_cross(v_sub(b, a), v_sub(c, a)));
-    if (!(n.x != 0.0 || n.y != 0.0 || n.z != 0.0)) g_error = 1;
+    if (!(n.x != 0.0 || n.y != 0.0 || n.z != 0.0)) g_error |= 2;
     const double TOL = 0.0;
     double d = v_dot(n, a);
     if (d < -TOL) {
@@ -707,7 +709,7 @@ static void face_normal_distance(i3 f, const v3* poly, int npoly, v3* out_n, dou
                 break;
             }
         }
-        if (!ok) g_error = 1;
+        if (!ok) g_error |= 4;
     }
     *out_n = n;
     *out_d = d;
@@ -916,7 +918,7 @@ static void convex_convex_manifold(const collider_t* h1, const collider_t* h2, v
         v3 dd1 = v_sub(h1->tv[e[1]], p1);
         v3 p2 = h2->tv[e[2]];
         v3 dd2 = v_sub(h2->tv[e[3]], p2);
-        if (!skew_lines(p1, dd1, p2, dd2, &l1, &l2)) { g_error = 1; return; }
+        if (!skew_lines(p1, dd1, p2, dd2, &l1, &l2)) { g_error |= 8; return; }
         contact_t c = {l1, l2, normal};
         cv_push(contacts, c);
     } else {
@@ -1033,7 +1035,7 @@ static double pos_dlambda(const pcpd_t* p, double h, double compliance, double l
     v3 n = V3(dx.x / c, dx.y / c, dx.z / c);
     double w1 = p->e1->invm + v_dot(v_cross(p->r1, n), m3_mulv(p->I1, v_cross(p->r1, n)));
     double w2 = p->e2->invm + v_dot(v_cross(p->r2, n), m3_mulv(p->I2, v_cross(p->r2, n)));
-    if (!(w1 + w2 != 0.0)) g_error = 1;
+    if (!(w1 + w2 != 0.0)) g_error |= 1;
     double til = compliance / (h * h);
     return (-c - til * lambda) / (w1 + w2 + til);
 }
@@ -1074,7 +1076,7 @@ static double ang_dlambda(const acpd_t* a, double h, double compliance, double l
     v3 n = V3(dq.x / th, dq.y / th, dq.z / th);
     double w1 = v_dot(n, m3_mulv(a->I1, n));
     double w2 = v_dot(n, m3_mulv(a->I2, n));
-    if (!(w1 + w2 != 0.0)) g_error = 1;
+    if (!(w1 + w2 != 0.0)) g_error |= 1;
     double til = compliance / (h * h);
     return (-th - til * lambda) / (w1 + w2 + til);
 }
@@ -1256,7 +1258,7 @@ static void solve_constraint(constraint_t* c, double h) {
     case C_MO: solve_mutual_orientation(c, h); break;
     case C_HINGE: solve_hinge(c, h); break;
     case C_SPH: solve_spherical(c, h); break;
-    default: g_error = 1; break;
+    default: g_error |= 1; break;
     }
 }
 

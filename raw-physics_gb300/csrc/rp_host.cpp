@@ -144,7 +144,7 @@ struct rp_world {
     DevBuf d_pair_count, d_pairs, d_row_count, d_uf_parent, d_island_awake, d_node_body, d_node_pred, d_node_level;
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
-        d_counters, d_phase, d_kat_out, d_kat_count;
+        d_counters, d_phase, d_kat_out, d_kat_count, d_deg;
 
     // phase-major pipeline
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
@@ -153,6 +153,7 @@ struct rp_world {
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
+    uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
     bool pipe_ready = false;
     PipeConfig pipe;
     PipeDims dims;
@@ -162,7 +163,7 @@ struct rp_world {
     StepParams graph_params = {};
     std::vector<cudaEvent_t> marks;   // phase events of a timed frame
     std::vector<int> mark_phase;
-    double phase_ms[PHASES] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double phase_ms[PHASES] = {};
 
     uint64_t launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
@@ -475,8 +476,8 @@ rp_status build_device(rp_world* w) {
         };
         std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
         RP_CUDA(upload(w->d_scene_order, order, st));
-        RP_CUDA(w->d_queue.ensure(16));
-        RP_CUDA(cudaMemsetAsync(w->d_queue.p, 0, 16, st));
+        RP_CUDA(w->d_queue.ensure(64));
+        RP_CUDA(cudaMemsetAsync(w->d_queue.p, 0, 64, st));
         w->dims.nbodies = (int)N;
         w->dims.ncolliders = (int)cols.size();
         w->dims.next = (int)E;
@@ -491,6 +492,8 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(cudaMemsetAsync(w->d_counters.p, 0, 256, st));
         RP_CUDA(w->d_phase.ensure(PHASES * 8));
         RP_CUDA(cudaMemsetAsync(w->d_phase.p, 0, PHASES * 8, st));
+        RP_CUDA(w->d_deg.ensure(32));
+        RP_CUDA(cudaMemsetAsync(w->d_deg.p, 0, 32, st));
     }
     RP_CUDA(w->d_status.ensure((size_t)S * 4));
     RP_CUDA(cudaMemsetAsync(w->d_status.p, 0, (size_t)S * 4, st));
@@ -590,6 +593,8 @@ WorldView<R> make_view(rp_world* w) {
     V.queue = w->d_queue.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
     V.solo_nodes = w->solo_nodes;
+    V.wait_ns = w->wait_ns;
+    V.deg_first = w->d_deg.as<int32_t>();
     return V;
 }
 
@@ -785,7 +790,7 @@ cudaError_t launch_pipeline(rp_world* w, const StepParams& P) {
     }
     if (w->timing) {
         // a timed frame runs without the graph, with an event after every phase
-        const int cap = 2 + P.num_substeps * 8;
+        const int cap = 2 + P.num_substeps * 12;
         while ((int)w->marks.size() < cap) {
             cudaEvent_t ev;
             e = cudaEventCreate(&ev);
@@ -1342,6 +1347,14 @@ rp_status rp_simulate(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
             if (s != RP_OK) return s;
             continue;
         }
+        if (bits & ST_BARRIER_TIMEOUT) {
+            // a bounded wait gave up and the frame was abandoned: restore the call's starting state
+            // and leave forces pending, as if the call had not run
+            s = snapshot(w, true);
+            if (s != RP_OK) return s;
+            RP_CUDA(cudaStreamSynchronize(w->stream));
+            return fail(RP_ERR_TIMEOUT, "a device-side wait exceeded its limit; the call was undone");
+        }
         w->status_accum |= bits;
         break;
     }
@@ -1349,7 +1362,6 @@ rp_status rp_simulate(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
     w->substeps += (uint64_t)nsteps * substeps;
     for (HostBody& b : w->bodies)
         if (!b.forces.empty()) { b.forces.clear(); w->forces_dirty = true; }
-    if (w->status_accum & ST_BARRIER_TIMEOUT) return fail(RP_ERR_TIMEOUT, "device barrier timed out");
     return RP_OK;
 }
 
@@ -1415,6 +1427,12 @@ rp_status rp_broad_pairs(rp_world* w, int32_t scene, uint32_t* out, uint32_t cap
     if (w->precision == RP_PRECISION_FP64) RP_CUDA(broad_f64(make_view<double>(w), scene, gb, w->stream));
     else RP_CUDA(broad_f32(make_view<float>(w), scene, gb, w->stream));
     w->launches++;
+    {
+        cudaError_t e;
+        const uint32_t bits = read_status(w, e);
+        if (e != cudaSuccess) return fail(RP_ERR_CUDA, cudaGetErrorString(e));
+        if (bits & ST_BARRIER_TIMEOUT) return fail(RP_ERR_TIMEOUT, "a device-side wait of the broad phase exceeded its limit");
+    }
     int32_t n = 0;
     RP_CUDA(cudaMemcpyAsync(&n, w->d_pair_count.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));
     RP_CUDA(cudaStreamSynchronize(w->stream));
@@ -1564,7 +1582,7 @@ rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]) {
 
 uint64_t rp_kernel_launches(const rp_world* w) { return w ? w->launches : 0; }
 
-rp_status rp_phase_times(rp_world* w, double out[9]) {
+rp_status rp_phase_times(rp_world* w, double out[RP_NUM_PHASES]) {
     if (check_world(w) || !out) return RP_ERR_INVALID;
     for (int k = 0; k < PHASES; ++k) out[k] = 0.0;
     for (int k = 0; k < PHASES; ++k) out[k] = w->phase_ms[k];
@@ -1971,6 +1989,32 @@ rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t substeps, uint3
 rp_status rp_adjoint_profile(rp_world* w, double out[6]) {
     if (check_world(w) || !out) return RP_ERR_INVALID;
     for (int k = 0; k < 6; ++k) out[k] = w->adj_prof[k];
+    return RP_OK;
+}
+
+rp_status rp_degenerate_info(rp_world* w, int64_t out[5]) {
+    if (check_world(w) || !out) return fail(RP_ERR_INVALID, "null argument");
+    for (int k = 0; k < 5; ++k) out[k] = k == 0 ? 0 : -1;
+    if (w->device < 0 || !w->d_deg.p) return RP_OK;
+    RP_CUDA(cudaSetDevice(w->device));
+    int32_t rec[8];
+    RP_CUDA(cudaMemcpyAsync(rec, w->d_deg.p, sizeof(rec), cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaMemsetAsync(w->d_deg.p, 0, sizeof(rec), w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    if (rec[0] == 0) return RP_OK;
+    out[0] = rec[0];
+    out[1] = rec[1];
+    out[2] = rec[2] >= 0 && rec[2] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[2]] : -1;
+    out[3] = rec[3] >= 0 && rec[3] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[3]] : -1;
+    out[4] = rec[4];
+    return RP_OK;
+}
+
+rp_status rp_world_set_wait_limit(rp_world* w, uint64_t microseconds) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (microseconds > 60000000ull) return fail(RP_ERR_INVALID, "wait limit above 60 s");
+    w->wait_ns = microseconds * 1000ull;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }   // the limit is a kernel argument
     return RP_OK;
 }
 

@@ -19,9 +19,11 @@ __global__ void __launch_bounds__(BLOCK) broad_kernel(WorldView<R> W, int s) {
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) broad_grid_kernel(WorldView<R> W) {
     __shared__ int scan_smem[32];
+    if (frame_abandoned(W.status)) return;
     GridGroup g;
     g.bar = W.barrier;
     g.status = W.status;
+    g.limit_ns = W.wait_ns;
     broad_phase(W, g, 0, scan_smem);
 }
 

@@ -338,7 +338,7 @@ __device__ void epa_face(NarrowSmem<R>& sm, int fi, int npoly) {
     V3<double> a = v3cast<double>(sm.u.epa.poly[f.x]), b = v3cast<double>(sm.u.epa.poly[f.y]),
                c = v3cast<double>(sm.u.epa.poly[f.z]);
     V3<double> n = vnorm(vcross(vsub(b, a), vsub(c, a)));
-    if (!(n.x != 0.0 || n.y != 0.0 || n.z != 0.0)) atomicOr(&sm.status, (int)ST_DEGENERATE);
+    if (!(n.x != 0.0 || n.y != 0.0 || n.z != 0.0)) atomicOr(&sm.status, (int)(ST_DEGENERATE | ST_DEG_EPA_NORMAL));
     double d = vdot(n, a);
     if (d < -0.0) {
         n = vinv(n);
@@ -353,7 +353,7 @@ __device__ void epa_face(NarrowSmem<R>& sm, int fi, int npoly) {
                 break;
             }
         }
-        if (!ok) atomicOr(&sm.status, (int)ST_DEGENERATE);
+        if (!ok) atomicOr(&sm.status, (int)(ST_DEGENERATE | ST_DEG_EPA_COPLANAR));
     }
     sm.u.epa.fn[fi] = n;
     sm.u.epa.fd[fi] = d;
@@ -552,7 +552,7 @@ __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, u
         // (epa.cpp:41 asserts on it).
         const V3<double> A = v3cast<double>(a);
         const V3<double> n64 = vnorm(vcross(vsub(v3cast<double>(b), A), vsub(v3cast<double>(c), A)));
-        if (!(n64.x != 0.0 || n64.y != 0.0 || n64.z != 0.0)) status |= ST_DEGENERATE;
+        if (!(n64.x != 0.0 || n64.y != 0.0 || n64.z != 0.0)) status |= ST_DEGENERATE | ST_DEG_EPA_NORMAL;
         n = v3cast<float>(n64);
     }
     float d = vdot(n, a);
@@ -569,7 +569,7 @@ __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, u
                 break;
             }
         }
-        if (!ok) status |= ST_DEGENERATE;
+        if (!ok) status |= ST_DEGENERATE | ST_DEG_EPA_COPLANAR;
     }
     n_out = n;
     d_out = d;
@@ -914,7 +914,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         R rB = -dd2.x * p2.x + dd2.x * p1.x - dd2.y * p2.y + dd2.y * p1.y - dd2.z * p2.z + dd2.z * p1.z;
         R den = (nA * mB) - (nB * mA);
         bool ok = den != (R)0;
-        if (!ok && lane == 0) atomicOr(&sm.status, (int)ST_DEGENERATE);
+        if (!ok && lane == 0) atomicOr(&sm.status, (int)(ST_DEGENERATE | ST_DEG_SKEW));
         R nn = ok ? ((rA * mB) - (rB * mA)) / den : (R)0;
         R mm = ok ? ((nA * rB) - (nB * rA)) / den : (R)0;
         V3<R> l1 = vadd(p1, vscale(mm, dd1));

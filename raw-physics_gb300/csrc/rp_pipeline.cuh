@@ -98,7 +98,11 @@ __device__ void emit_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int s, i
             atomicOr(&W.status[s], (uint32_t)ST_CONTACT_OVERFLOW);
             nc = 0;
         }
-        if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+        if (sm.status) {
+            atomicOr(&W.status[s], (uint32_t)sm.status);
+            const int2 pr = W.pairs[gp];
+            note_degenerate(W, (uint32_t)sm.status, s, pr.x, pr.y);
+        }
         tally += (unsigned long long)nc;
         W.pair_cstart[gp] = start;
         W.pair_ccount[gp] = nc;
@@ -140,6 +144,7 @@ __device__ void setup_scene(const WorldView<R>& W, const G& g, int s, double dt,
 
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_setup_cta(WorldView<R> W, double dt) {
+    if (frame_abandoned(W.status)) return;
     __shared__ int scan_smem[32];
     __shared__ int base_smem;
     CtaGroup g;
@@ -153,9 +158,11 @@ template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_setup_grid(WorldView<R> W, double dt) {
     __shared__ int scan_smem[32];
     __shared__ int base_smem;
+    if (frame_abandoned(W.status)) return;
     GridGroup g;
     g.bar = W.barrier;
     g.status = W.status;
+    g.limit_ns = W.wait_ns;
     setup_scene(W, g, 0, dt, scan_smem, &base_smem);
 }
 
@@ -163,6 +170,7 @@ __global__ void __launch_bounds__(BLOCK) k_setup_grid(WorldView<R> W, double dt)
 // Per-substep body phases
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbodies, int next, double h) {
+    if (frame_abandoned(W.status)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
     for (int b = t; b < nbodies; b += n) {
         predict_body<R, EXACT>(W, b, h);
@@ -173,13 +181,14 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
     for (int e = t; e < next; e += n)
         for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
     for (int s = t; s < W.num_scenes; s += n) W.contact_count[s] = 0;
-    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; }
+    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; }
 }
 
 // `group` threads per collider (a power of two up to 32; 8 by default: the typical hull has 8-64
 // vertices, so a whole warp per collider would leave most lanes idle).
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int ncolliders, int include_fixed, int group) {
+    if (frame_abandoned(W.status)) return;
     const int sub = threadIdx.x % group;
     const int gi = (blockIdx.x * blockDim.x + threadIdx.x) / group;
     const int ng = (gridDim.x * blockDim.x) / group;
@@ -194,6 +203,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int nc
 
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_velocity(WorldView<R> W, int nbodies, double h) {
+    if (frame_abandoned(W.status)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
     for (int b = t; b < nbodies; b += n) velocity_body<R, EXACT>(W, b, h);
 }
@@ -216,6 +226,7 @@ __device__ __forceinline__ void block_append(int32_t* list, int32_t* count, bool
 // general path (compound bodies, sphere colliders), which goes straight to the contact list.
 template <typename R>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled) {
+    if (frame_abandoned(W.status)) return;
     __shared__ int scan_smem[32];
     __shared__ int base_smem;
     const int n = W.queue[0];
@@ -248,6 +259,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
 // contact list; the list entries are gathered per warp and appended 32 at a time.
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK, 3) k_gjk(WorldView<R> W) {
+    if (frame_abandoned(W.status)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     GjkSmem<R>& sm = reinterpret_cast<GjkSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -309,6 +321,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 3) k_gjk(WorldView<R> W) {
 
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
+    if (frame_abandoned(W.status)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -350,7 +363,10 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             const int s = W.body_scene[a];
             if (lane == 0) {
                 if (!ok) atomicOr(&W.status[s], (uint32_t)ST_EPA_NOT_CONVERGED);
-                if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+                if (sm.status) {
+                    atomicOr(&W.status[s], (uint32_t)sm.status);
+                    note_degenerate(W, (uint32_t)sm.status, s, a, b);
+                }
                 if (ok) {
                     double* o = W.work_epa + 4 * (size_t)k;
                     o[0] = nrm.x; o[1] = nrm.y; o[2] = nrm.z; o[3] = pen;
@@ -370,6 +386,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
 
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
+    if (frame_abandoned(W.status)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -415,6 +432,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
 // Gauss–Seidel sweeps: one CTA per scene, or the whole cooperative grid on one large scene.
 template <typename R, bool EXACT, bool VELOCITY>
 __global__ void __launch_bounds__(BLOCK) k_sweep_cta(WorldView<R> W, double h) {
+    if (frame_abandoned(W.status)) return;
     CtaGroup g;
     for (int s = blockIdx.x; s < W.num_scenes; s += gridDim.x) {
         const int L = W.scene_levels[s];
@@ -431,6 +449,7 @@ constexpr int SWEEP_WARP_BLOCK = 128;
 
 template <typename R, bool EXACT, bool VELOCITY>
 __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h) {
+    if (frame_abandoned(W.status)) return;
     WarpGroup g;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -448,9 +467,11 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
 
 template <typename R, bool EXACT, bool VELOCITY>
 __global__ void __launch_bounds__(BLOCK) k_sweep_grid(WorldView<R> W, double h) {
+    if (frame_abandoned(W.status)) return;
     GridGroup g;
     g.bar = W.barrier;
     g.status = W.status;
+    g.limit_ns = W.wait_ns;
     const int L = W.scene_levels[0];
     sweep_levels<R, EXACT, VELOCITY>(W, g, 0, L, W.level_count, W.scene_node_cap[0], (R)h);
 }
@@ -543,16 +564,15 @@ struct PipeLauncher {
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
             }
             k_cull<R><<<c.cull_blocks, PIPE_BLOCK, 0, st>>>(W, P.enable_collisions);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_NARROW)) != cudaSuccess) return e;
             if (P.enable_collisions) {
                 k_gjk<R, EXACT><<<c.gjk_blocks, PIPE_BLOCK, gjk_smem(), st>>>(W);
-                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_GJK)) != cudaSuccess) return e;
                 k_epa<R, EXACT><<<c.epa_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
-                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_EPA)) != cudaSuccess) return e;
                 k_manifold<R, EXACT><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
-                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_MANIFOLD)) != cudaSuccess) return e;
             }
-            if ((e = mark(PH_NARROW)) != cudaSuccess) return e;
             for (int it = 0; it < P.num_pos_iters; ++it) {
                 if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, false>, c.sweep_grid_blocks, BLOCK, st, W, h);
                 else if (c.sweep_cta) k_sweep_cta<R, EXACT, false><<<d.num_scenes, BLOCK, 0, st>>>(W, h), e = cudaGetLastError();

@@ -29,8 +29,6 @@ namespace rp {
 
 constexpr int BLOCK = 256;
 constexpr int WARPS_PER_BLOCK = BLOCK / 32;
-constexpr long long BARRIER_SPIN_LIMIT = 20000000;   // ~1 s of polling, then give up with a status bit
-
 // ---------------------------------------------------------------------------------------------
 // Groups
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
@@ -39,28 +37,67 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// True once a bounded wait of this frame has given up (the status word of scene 0 carries the bit;
+// only the cooperative grid, which steps a world of one scene, waits at grid barriers). Every kernel
+// of the frame then returns at once, so no kernel works on data a skipped phase never wrote.
+__device__ __forceinline__ bool frame_abandoned(const uint32_t* status) {
+    return (*(const volatile uint32_t*)status & ST_BARRIER_TIMEOUT) != 0;
+}
+
 // Grid barrier of a cooperative launch: one arrival counter that only grows. The host zeroes it
 // before every frame (and before every other launch sequence that uses it), and every cooperative
 // kernel of a sequence has the same number of CTAs, so after k complete barriers the counter is
 // k * gridDim.x: a CTA arriving at count `old` waits until the count reaches the next multiple of
 // gridDim.x. One atomic per CTA and nothing else on the release path (no reset, no generation word).
-static __device__ __noinline__ void grid_barrier(unsigned* bar, uint32_t* status) {
+// The wait is bounded by limit_ns of the globaltimer (checked every 64 polls; 0 gives up at the first
+// check that finds the barrier incomplete), and it also ends when another CTA has given up. A CTA
+// that gives up sets ST_BARRIER_TIMEOUT and leaves the launch (every thread exits together), so it
+// never runs a phase on data the others have not finished; the CTAs still waiting for it give up in
+// turn, and the frame's later kernels return at once (frame_abandoned).
+static __device__ __noinline__ void grid_barrier(unsigned* bar, uint32_t* status, unsigned long long limit_ns) {
+    __shared__ int s_gave_up;
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned nb = gridDim.x;
         __threadfence();                                   // this CTA's writes before its arrival
         const unsigned old = atomicAdd(&bar[0], 1u);
         const unsigned target = old - old % nb + nb;
-        long long spins = 0;
-        while ((int)(ld_acquire_gpu(&bar[0]) - target) < 0) {
-            __nanosleep(20);
-            if (++spins > BARRIER_SPIN_LIMIT) { atomicOr(status, (uint32_t)ST_BARRIER_TIMEOUT); break; }
-            // after one barrier has given up, later ones do not wait again
-            if ((spins & 1023) == 0 && (*(volatile uint32_t*)status & ST_BARRIER_TIMEOUT)) break;
+        int gave_up = 0;
+        if ((int)(ld_acquire_gpu(&bar[0]) - target) < 0) {
+            if (limit_ns == 0) gave_up = 1;
+            const unsigned long long t0 = global_ns();
+            unsigned polls = 0;
+            while (!gave_up && (int)(ld_acquire_gpu(&bar[0]) - target) < 0) {
+                __nanosleep(32);
+                if ((++polls & 63u) == 0u && (global_ns() - t0 > limit_ns || frame_abandoned(status))) gave_up = 1;
+            }
         }
+        if (gave_up) atomicOr(status, (uint32_t)ST_BARRIER_TIMEOUT);
         __threadfence();
+        s_gave_up = gave_up;
     }
     __syncthreads();
+    if (s_gave_up) asm volatile("exit;");
+}
+
+// Records the first degenerate condition of the world (ST_DEG_* bits, scene, pair, substep) for
+// rp_degenerate_info; later ones only set status bits.
+template <typename R>
+__device__ __forceinline__ void note_degenerate(const WorldView<R>& W, uint32_t bits, int s, int a, int b) {
+    const uint32_t deg = bits & (uint32_t)ST_DEG_MASK;
+    if (deg == 0u || !W.deg_first) return;
+    if (atomicCAS(reinterpret_cast<unsigned*>(W.deg_first), 0u, deg) == 0u) {
+        W.deg_first[1] = s;
+        W.deg_first[2] = a;
+        W.deg_first[3] = b;
+        W.deg_first[4] = W.queue ? W.queue[4] : -1;
+    }
 }
 
 struct CtaGroup {
@@ -82,11 +119,12 @@ struct WarpGroup {   // one warp per scene (small scenes of a batch; barrier = _
 struct GridGroup {
     unsigned* bar;
     uint32_t* status;
+    unsigned long long limit_ns;
     __device__ int rank() const { return (int)(blockIdx.x * blockDim.x + threadIdx.x); }
     __device__ int size() const { return (int)(gridDim.x * blockDim.x); }
     __device__ int nblocks() const { return (int)gridDim.x; }
     __device__ int block() const { return (int)blockIdx.x; }
-    __device__ void sync() const { grid_barrier(bar, status); }
+    __device__ void sync() const { grid_barrier(bar, status, limit_ns); }
 };
 
 // Block-wide inclusive scan of one value per thread; smem must hold 32 ints.
@@ -840,7 +878,10 @@ __device__ void narrowphase(const WorldView<R>& W, const G& g, int s, NarrowSmem
                 atomicOr(&W.status[s], (uint32_t)ST_CONTACT_OVERFLOW);
                 nc = 0;
             }
-            if (sm.status) atomicOr(&W.status[s], (uint32_t)sm.status);
+            if (sm.status) {
+                atomicOr(&W.status[s], (uint32_t)sm.status);
+                note_degenerate(W, (uint32_t)sm.status, s, a, b);
+            }
             n_contacts += nc;
             W.pair_cstart[pbase + p] = start;
             W.pair_ccount[pbase + p] = nc;
@@ -956,12 +997,6 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
 // ---------------------------------------------------------------------------------------------
 // One full step of scene s by group g
 
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 // Level-by-level sweep of the Gauss–Seidel schedule. With a grid group, a run of consecutive
 // levels that each hold at most SOLO_NODES nodes is swept by CTA 0 alone, separated by
 // __syncthreads, while the other CTAs wait at one grid barrier: the dependent chain of small levels
@@ -1028,7 +1063,11 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
         for (int b = b0 + g.rank(); b < b1; b += g.size()) predict_body<R, EXACT>(W, b, h);
         for (int e = e0 + g.rank(); e < e1; e += g.size())
             for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
-        if (g.rank() == 0) { W.contact_count[s] = 0; W.work[s] = 0; }
+        if (g.rank() == 0) {
+            W.contact_count[s] = 0;
+            W.work[s] = 0;
+            if (s == 0) atomicAdd(&W.queue[4], 1);
+        }
         g.sync();
         mark(PH_PREDICT);
         if (P.enable_collisions) {
@@ -1071,9 +1110,11 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel_grid(WorldView<R> W, Ste
     __shared__ int scan_smem[32];
     NarrowSmem<R>* sms = reinterpret_cast<NarrowSmem<R>*>(dyn_smem);
     NarrowSmem<R>& sm = sms[threadIdx.x >> 5];
+    if (frame_abandoned(W.status)) return;
     GridGroup g;
     g.bar = W.barrier;
     g.status = W.status;
+    g.limit_ns = W.wait_ns;
     step_scene<R, EXACT>(W, g, 0, P, sm, scan_smem);
 }
 

@@ -18,10 +18,15 @@ enum : uint32_t {
     ST_CONTACT_OVERFLOW = 1u << 1,   // contact buffer exceeded its capacity
     ST_EPA_OVERFLOW = 1u << 2,       // EPA polytope outgrew its fixed per-warp storage
     ST_CLIP_OVERFLOW = 1u << 3,      // clipped polygon outgrew its per-warp storage
-    ST_BARRIER_TIMEOUT = 1u << 4,    // a bounded group barrier gave up (should never happen)
+    ST_BARRIER_TIMEOUT = 1u << 4,    // a bounded grid barrier gave up; the frame was abandoned
     ST_DEGENERATE = 1u << 5,         // input the reference would reject with an assert
     ST_LEVEL_OVERFLOW = 1u << 6,     // dependency depth exceeded the level table
     ST_EPA_NOT_CONVERGED = 1u << 8,  // informational: the reference prints "EPA did not converge."
+    // which degenerate condition set ST_DEGENERATE (each comes with it)
+    ST_DEG_EPA_NORMAL = 1u << 9,     // an EPA face whose normal vanishes (epa.cpp:41 asserts)
+    ST_DEG_EPA_COPLANAR = 1u << 10,  // an EPA face through the origin with every point in its plane (epa.cpp:72)
+    ST_DEG_SKEW = 1u << 11,          // edge-edge contact of parallel edges (clipping.cpp:279)
+    ST_DEG_MASK = ST_DEG_EPA_NORMAL | ST_DEG_EPA_COPLANAR | ST_DEG_SKEW,
 };
 
 // Collider kinds (Collider_Type, src/physics/collider.h:33-36)
@@ -57,8 +62,11 @@ struct Shape {               // one convex hull's topology (collider_convex_hull
 // Per-pair state between the narrowphase kernels of the phase-major pipeline
 enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3 };
 
-// Phases of the step kernel timed by group rank 0 (rp_phase_times)
-enum { PH_BROAD = 0, PH_ISLANDS, PH_SCHEDULE, PH_PREDICT, PH_TRANSFORM, PH_NARROW, PH_SOLVE, PH_VELOCITY, PH_VSOLVE, PHASES };
+// Phases of the step timed per frame (rp_phase_times). The persistent kernel times the whole
+// narrowphase as PH_NARROW; the phase-major form splits it into the cull (PH_NARROW), GJK, EPA and
+// contact-manifold kernels.
+enum { PH_BROAD = 0, PH_ISLANDS, PH_SCHEDULE, PH_PREDICT, PH_TRANSFORM, PH_NARROW, PH_SOLVE, PH_VELOCITY, PH_VSOLVE,
+       PH_GJK, PH_EPA, PH_MANIFOLD, PHASES };
 
 struct StepParams {          // the arguments of pbd_simulate_with_constraints
     double dt;
@@ -164,16 +172,20 @@ struct WorldView {
     int32_t* hit_list;           // [pair capacity] work items needing a manifold this substep (queue[3])
     R* work_simplex;             // [16 * pair capacity] GJK simplex of a hit (a, b, c, d)
     double* work_epa;            // [4 * pair capacity] EPA normal (FP64) and penetration of a hit
-    int32_t* queue;              // [4] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
-                                 //     [2] gjk_list length, [3] hit_list length
+    int32_t* queue;              // [16] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
+                                 //     [2] gjk_list length, [3] hit_list length, [4] substeps run since
+                                 //     the world was built (phase-major form)
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
     int32_t max_colliders_per_body;
     int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
     // ---- control ----------------------------------------------------------------------------
     uint32_t* status;        // [S] status bits per scene
     unsigned int* barrier;   // [1] grid barrier arrival counter (zeroed before each launch sequence)
+    unsigned long long wait_ns;   // bound of every device-side wait (grid barriers), nanoseconds
     unsigned long long* counters; // [32] diagnostics: gjk/epa iterations and cap hits, contacts, pair cycles
     unsigned long long* phase_ns; // [PHASES] time spent per phase of the step, seen by group rank 0
+    int32_t* deg_first;      // [8] first degenerate condition met: ST_DEG_* bits (0: none yet), scene,
+                             //     body slots a and b of the pair, substep (queue[4]) it was met in
 };
 
 }  // namespace rp

@@ -21,7 +21,8 @@ COLLIDER_SPHERE, COLLIDER_HULL = 0, 1
 ERRORS = {0: "RP_OK", -1: "RP_ERR_INVALID", -2: "RP_ERR_CUDA", -3: "RP_ERR_NO_DEVICE", -4: "RP_ERR_CAPACITY",
           -5: "RP_ERR_DEGENERATE", -6: "RP_ERR_TIMEOUT", -7: "RP_ERR_STATE"}
 STATUS_BITS = {1 << 0: "PAIR_OVERFLOW", 1 << 1: "CONTACT_OVERFLOW", 1 << 2: "EPA_OVERFLOW", 1 << 3: "CLIP_OVERFLOW",
-               1 << 4: "BARRIER_TIMEOUT", 1 << 5: "DEGENERATE", 1 << 6: "LEVEL_OVERFLOW", 1 << 8: "EPA_NOT_CONVERGED"}
+               1 << 4: "BARRIER_TIMEOUT", 1 << 5: "DEGENERATE", 1 << 6: "LEVEL_OVERFLOW", 1 << 8: "EPA_NOT_CONVERGED",
+               1 << 9: "DEG_EPA_NORMAL", 1 << 10: "DEG_EPA_COPLANAR", 1 << 11: "DEG_SKEW"}
 
 # every exported symbol of include/rp.h with its ctypes signature
 _d, _i, _u, _u64 = C.c_double, C.c_int32, C.c_uint32, C.c_uint64
@@ -72,6 +73,8 @@ SIGNATURES = {
     "rp_contacts": (_i, [_W, _i, _i, _P(_d), _u, _P(_u)]),
     "rp_counters": (_i, [_W, _P(_u64)]),
     "rp_world_set_mode": (_i, [_W, _i]),
+    "rp_world_set_wait_limit": (_i, [_W, _u64]),
+    "rp_degenerate_info": (_i, [_W, _P(C.c_int64)]),
     "rp_adjoint_profile": (_i, [_W, _P(_d)]),
     "rp_adjoint_trajectory": (_i, [_W, _d, _u, _u, _i, _u, _u, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d)]),
     "rp_autotune": (_i, [_W, _d, _u, _u, _i, _u, _P(_i)]),
@@ -415,6 +418,21 @@ class World:
         kernel per frame) or "auto"."""
         self._check(self.lib.rp_world_set_mode(self.h, self.MODES[mode]))
 
+    def degenerate_info(self):
+        """The first degenerate condition met since the last query (rp_degenerate_info): None, or
+        {"bits": [names], "scene", "pair": (e1, e2), "substep"}."""
+        out = np.zeros(5, dtype=np.int64)
+        self._check(self.lib.rp_degenerate_info(self.h, out.ctypes.data_as(_P(C.c_int64))))
+        if out[0] == 0:
+            return None
+        return {"bits": [v for k, v in STATUS_BITS.items() if int(out[0]) & k], "scene": int(out[1]),
+                "pair": (int(out[2]), int(out[3])), "substep": int(out[4])}
+
+    def set_wait_limit(self, microseconds: int):
+        """Bound of every device-side wait (grid barriers); a wait that runs out undoes the call and
+        raises RPError(RP_ERR_TIMEOUT)."""
+        self._check(self.lib.rp_world_set_wait_limit(self.h, int(microseconds)))
+
     def autotune(self, frames: int = 3) -> dict:
         """Pick the fastest launch configuration for the loaded scenes (results are identical under
         every configuration); returns the choice."""
@@ -434,10 +452,11 @@ class World:
     def kernel_launches(self) -> int:
         return int(self.lib.rp_kernel_launches(self.h))
 
-    PHASES = ("broad", "islands", "schedule", "predict", "transform", "narrow", "solve", "velocity", "vsolve")
+    PHASES = ("broad", "islands", "schedule", "predict", "transform", "narrow", "solve", "velocity", "vsolve", "gjk", "epa",
+              "manifold")
 
     def phase_times(self) -> dict:
-        out = (C.c_double * 9)()
+        out = (C.c_double * len(self.PHASES))()
         self._check(self.lib.rp_phase_times(self.h, out))
         return dict(zip(self.PHASES, out[:]))
 

@@ -98,3 +98,24 @@ def precision_report(rawphys, batch, frames: int = 300, sample_every: int = 50, 
             "top_body_horizontal_drift_m": tower_drift,
             "relative_energy_drift": drift,
             "samples": len(step_pos)}
+
+
+def rotation_angle(qa, qb):
+    """Angle (rad) of the rotation between unit quaternions, per row: 4 asin(|qa - s qb| / 2) with s
+    the sign of their dot product (accurate for small angles, unlike 2 acos(|qa . qb|))."""
+    s = np.where(np.sum(qa * qb, axis=1) < 0.0, -1.0, 1.0)[:, None]
+    return 4.0 * np.arcsin(np.minimum(1.0, 0.5 * np.linalg.norm(qa - s * qb, axis=1)))
+
+
+def step_error(got, expected, dynamic):
+    """Per-step error of one frame from identical states: position error |x - x_ref| (m) and rotation
+    angle between orientations (rad) over the dynamic bodies, as median, 99th percentile and max."""
+    pe = np.linalg.norm(got[dynamic, 0:3] - expected[dynamic, 0:3], axis=1)
+    re = rotation_angle(got[dynamic, 3:7], expected[dynamic, 3:7])
+
+    def summary(x):
+        if x.size == 0:
+            return {"median": 0.0, "p99": 0.0, "max": 0.0}
+        return {"median": float(np.median(x)), "p99": float(np.quantile(x, 0.99)), "max": float(np.max(x))}
+    return {"pos_m": summary(pe), "rot_rad": summary(re), "bodies": int(pe.size),
+            "within_1e-4": float(np.mean((pe <= 1e-4) & (re <= 1e-4))) if pe.size else 1.0}

@@ -391,3 +391,30 @@ def test_sorted_broad_phase_grid_wide_sort(ext_built, oracle_built, precision):
     assert len(ref) > 17000 * 3
     assert np.array_equal(pairs, ref)
     w.close()
+
+
+@pytest.mark.parametrize("mode", ["phased", "persistent"])
+def test_wait_limit_runs_out_undoes_the_call_and_world_recovers(ext_built, oracle_built, mode):
+    """Failure detection without a GPU fault: with the wait limit at 0 every grid barrier of the
+    cooperative launches gives up at its first incomplete check. The frame is abandoned (each CTA
+    leaves the launch, later kernels return at once), rp_simulate restores the starting state and
+    returns RP_ERR_TIMEOUT; with the default limit back the world steps exactly as the oracle."""
+    from rawphys import scenes as S
+    sc = S.large_scene(1024, seed=1)          # one scene of >= 256 bodies: the cooperative grid path
+    w = ext_built.World(0, "fp64")
+    w.set_mode(mode)
+    w.load(sc)
+    w.step(2)
+    start = w.get_state()
+    w.set_wait_limit(0)
+    with pytest.raises(ext_built.RPError, match="RP_ERR_TIMEOUT"):
+        w.step(1)
+    assert np.array_equal(w.get_state(), start), "a timed-out call must leave the state as it found it"
+    w.set_wait_limit(1_000_000)
+    w.step(1)
+    w.sync()
+    o = oracle_built("port").load(sc)
+    o.set_state(start)
+    o.step(1)
+    assert np.array_equal(w.get_state(), o.get_state())
+    w.close()

@@ -301,11 +301,39 @@ def test_obj_fixtures_match_the_live_reference_reader(tmp_path):
 
 def test_bench_roofline_inputs():
     """bench.py's roofline inputs: the peak (MEASURED_PEAKS.json, or the stated fallback) and the
-    position sweep's DRAM traffic per launch from its committed ncu summary."""
+    position sweep's DRAM traffic per launch from its committed ncu summary (a missing summary or
+    line is reported with its reason, never silently)."""
     sys.path.insert(0, ROOT)
     import bench
     peak, kind = bench.measured_peak_hbm()
     assert peak > 1000.0 and kind in ("measured", "fallback")
-    traffic = bench.profile_traffic()
-    assert traffic is not None and traffic > 0.0
+    traffic, src = bench.profile_traffic("pipeline_large4096.md", "k_sweep_grid (position sweep, cooperative grid)")
+    assert traffic is not None and traffic > 0.0, src
+    none, why = bench.profile_traffic("no_such_summary.md", "k")
+    assert none is None and "missing" in why
     assert bench.SWEEP_CONTACT_B > 0 and bench.SWEEP_NODE_B > 0
+
+
+def test_bench_sample_and_step_error():
+    """The bench's size-stratified scene sample keeps the batch's size range, and the per-step error
+    summary measures positions in metres and rotations as angles."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from rawphys import scenes as S
+    from rawphys.precision import rotation_angle, step_error
+    batch = S.batched_scenes(256, seed=0)
+    picks = bench.stratified_scenes(batch, 32)
+    sizes = np.bincount(batch.scene, minlength=batch.num_scenes)
+    assert len(picks) >= 30 and sizes[picks].min() == sizes.min() and sizes[picks].max() == sizes.max()
+    q = np.array([[0.0, 0.0, 0.0, 1.0]])
+    half = 0.5e-4
+    r = np.array([[np.sin(half), 0.0, 0.0, np.cos(half)]])
+    assert abs(rotation_angle(q, r)[0] - 1e-4) < 1e-12
+    assert abs(rotation_angle(q, -r)[0] - 1e-4) < 1e-12      # q and -q are the same rotation
+    a = np.zeros((3, 28))
+    a[:, 6] = 1.0
+    b = a.copy()
+    b[0, 0] = 3e-5
+    b[1, 1] = 2e-4
+    e = step_error(b, a, np.array([True, True, False]))
+    assert e["bodies"] == 2 and abs(e["pos_m"]["max"] - 2e-4) < 1e-15 and e["within_1e-4"] == 0.5
