@@ -424,6 +424,7 @@ def measure_batched(args, dev, rank, world_size, with_oracle):
     stream = torch.cuda.Stream(dev)
     w = rawphys.World(dev, "fp32")
     w.set_stream(stream.cuda_stream)
+    w.set_sweep_order(args.sweep_order)
     w.load_batch(batch)
     w.step(args.batched_settle)
     tuned = w.autotune(frames=2) if args.autotune else None
@@ -510,6 +511,8 @@ def measure_plain(args, dev, precision, steps, start_from=None, with_oracle=Fals
     stream = torch.cuda.Stream(dev)
     w = rawphys.World(dev, precision)
     w.set_stream(stream.cuda_stream)
+    if precision == "fp32":
+        w.set_sweep_order(args.sweep_order)
     w.load(scene)
     if start_from is not None:
         w.set_state(start_from)
@@ -629,7 +632,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": b["total_ms"] / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
                 "config": {"workload": BATCHED_WORKLOAD},
-                "details": {"batch": b["workload_detail"], "l2": "flushed (256 MiB write) before every timed frame",
+                "details": {"batch": b["workload_detail"], "sweep_order": args.sweep_order, "l2": "flushed (256 MiB write) before every timed frame",
                             "parallelism": "scenes sharded by rank (own batch per rank)" if world_size > 1 else "one GPU",
                             "pairs_per_step": b["pairs_per_step"], "contacts_per_step": b["contacts_per_step"],
                             "phase_ms_per_step": b["phase"], "autotuned": b["tuned"],
@@ -695,6 +698,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--precision-towers", type=int, default=128, help="0 skips the precision-stress report")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default launch configuration")
+    ap.add_argument("--sweep-order", default="reference", choices=["reference", "coloured"],
+                    help="Gauss-Seidel order of the constraint sweeps")
     ap.add_argument("--precision-frames", type=int, default=300)
     ap.add_argument("--adjoint-scenes", type=int, default=152, help="0 skips the adjoint grad/s measurement")
     ap.add_argument("--adjoint-frames", type=int, default=4)

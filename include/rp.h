@@ -115,6 +115,16 @@ rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t num_substeps, u
                                 const int32_t* loss_entity, const double* target, double* loss_out, double* grad_v,
                                 double* grad_w, double* grad_mass, double* grad_friction);
 rp_status rp_world_set_mode(rp_world* w, int32_t mode);
+/* Gauss–Seidel order of the constraint sweeps. RP_SWEEP_REFERENCE (default): the reference's serial
+ * order (pbd.cpp:615-620 and the velocity pass's loop), swept level by level over the substep's active
+ * constraints; results are the reference's (bit for bit in RP_PRECISION_FP64). RP_SWEEP_COLOURED:
+ * graph-coloured sweeps, constraints that share a dynamic body get different colours and the sweep
+ * runs colour by colour; a different Gauss–Seidel order with fewer dependent steps (a joint chain takes
+ * two or three colours instead of one step per link). Its results differ from the reference's by the
+ * reordering (measured per-step error against the FP64 oracle: bench.py's step_err); the autotuner
+ * then also picks the colouring's priority scheme. No counterpart in the reference. */
+enum { RP_SWEEP_REFERENCE = 0, RP_SWEEP_COLOURED = 1 };
+rp_status rp_world_set_sweep_order(rp_world* w, int32_t order);
 /* Bound of every device-side wait of this world (the grid barriers of a single large scene's
  * cooperative kernels), in microseconds; 1 s by default, at most 60 s; 0 gives up at the first wait
  * that finds its barrier incomplete. A wait that runs out abandons the frame: every CTA leaves the
@@ -295,6 +305,13 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
  * iteration cap and returned no collision), [19] EPA set-up cycles (hull staging, simplex load),
  * [20] EPA support-mapping cycles, [21] manifold set-up cycles, [22] contact write-out cycles,
  * [23] reserved (0). Cycle counters of the phase-major kernels are summed per warp. */
+/* The sweep schedules of the last substep of the last rp_simulate call for one scene: per solver
+ * node (the scene's external constraints, then its broad-phase pairs, in constraint order) its level
+ * (RP_SWEEP_REFERENCE) or colour (RP_SWEEP_COLOURED) in the position sweep (which = 0) or the
+ * velocity sweep (which = 1), -1 when the node does nothing there, and its two dynamic entities
+ * (-1 for a fixed body). *count receives the node count; level_out / bodies_out may be NULL. */
+rp_status rp_last_schedule(rp_world* w, int32_t scene, int32_t which, int32_t* level_out, int32_t* bodies_out,
+                           uint32_t cap, uint32_t* count);
 #define RP_NUM_COUNTERS 24
 rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]);
 /* Kernel launches issued by this world since creation (every launch of the CUDA extension). */

@@ -145,6 +145,7 @@ struct rp_world {
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
         d_counters, d_phase, d_kat_out, d_kat_count, d_deg;
+    DevBuf d_node_vpred, d_node_vlevel, d_vlevel_count, d_vlevel_fill, d_vlevel_nodes, d_scene_vlevels, d_act_list, d_act_count;
 
     // phase-major pipeline
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
@@ -154,6 +155,7 @@ struct rp_world {
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
+    int sweep_order = RP_SWEEP_REFERENCE;   // Gauss–Seidel order of the sweeps (rp_world_set_sweep_order)
     bool pipe_ready = false;
     PipeConfig pipe;
     PipeDims dims;
@@ -445,6 +447,14 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(w->d_scan_tmp.ensure(4096 * 4));
     RP_CUDA(w->d_level_nodes.ensure(std::max<size_t>(NN, 1) * 4));
     RP_CUDA(w->d_scene_levels.ensure((size_t)S * 4));
+    RP_CUDA(w->d_node_vpred.ensure(std::max<size_t>(NN, 1) * 8));
+    RP_CUDA(w->d_node_vlevel.ensure(std::max<size_t>(NN, 1) * 4));
+    RP_CUDA(w->d_vlevel_count.ensure((size_t)S * (size_t)(w->max_levels + 1) * 4));
+    RP_CUDA(w->d_vlevel_fill.ensure((size_t)S * (size_t)(w->max_levels + 1) * 4));
+    RP_CUDA(w->d_vlevel_nodes.ensure(std::max<size_t>(NN, 1) * 4));
+    RP_CUDA(w->d_scene_vlevels.ensure((size_t)S * 4));
+    RP_CUDA(w->d_act_list.ensure(std::max<size_t>(2 * NN, 1) * 4));
+    RP_CUDA(w->d_act_count.ensure((size_t)S * 8));
     RP_CUDA(w->d_scene_nodes.ensure((size_t)S * 4));
     RP_CUDA(w->d_pair_cstart.ensure(std::max<size_t>(P, 1) * 4));
     RP_CUDA(w->d_pair_ccount.ensure(std::max<size_t>(P, 1) * 4));
@@ -499,6 +509,15 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(cudaMemsetAsync(w->d_status.p, 0, (size_t)S * 4, st));
     RP_CUDA(cudaMemsetAsync(w->d_pair_count.p, 0, (size_t)S * 4, st));
     RP_CUDA(cudaMemsetAsync(w->d_scene_levels.p, 0, (size_t)S * 4, st));
+    RP_CUDA(cudaMemsetAsync(w->d_scene_vlevels.p, 0, (size_t)S * 4, st));
+    {   // level tables start at zero; each substep's schedule clears what the previous one used
+        const size_t lt = (size_t)S * (size_t)(w->max_levels + 1) * 4;
+        RP_CUDA(cudaMemsetAsync(w->d_level_count.p, 0, lt, st));
+        RP_CUDA(cudaMemsetAsync(w->d_level_fill.p, 0, lt, st));
+        RP_CUDA(cudaMemsetAsync(w->d_vlevel_count.p, 0, lt, st));
+        RP_CUDA(cudaMemsetAsync(w->d_vlevel_fill.p, 0, lt, st));
+    }
+    RP_CUDA(cudaMemsetAsync(w->d_act_count.p, 0, (size_t)S * 8, st));
     w->static_dirty = false;
     w->forces_dirty = true;
     // upload the host state
@@ -577,6 +596,15 @@ WorldView<R> make_view(rp_world* w) {
     V.contacts = w->d_contacts.as<R>();
     V.ext_lambda = w->d_ext_lambda.as<double>();
     V.max_levels = w->max_levels;
+    V.node_vpred = w->d_node_vpred.as<int32_t>();
+    V.node_vlevel = w->d_node_vlevel.as<int32_t>();
+    V.vlevel_count = w->d_vlevel_count.as<int32_t>();
+    V.vlevel_fill = w->d_vlevel_fill.as<int32_t>();
+    V.vlevel_nodes = w->d_vlevel_nodes.as<int32_t>();
+    V.scene_vlevels = w->d_scene_vlevels.as<int32_t>();
+    V.act_list = w->d_act_list.as<int32_t>();
+    V.act_count = w->d_act_count.as<int32_t>();
+    V.sweep_order = w->sweep_order;
     V.status = w->d_status.as<uint32_t>();
     V.barrier = w->d_barrier.as<unsigned int>();
     V.counters = w->d_counters.as<unsigned long long>();
@@ -2007,6 +2035,44 @@ rp_status rp_degenerate_info(rp_world* w, int64_t out[5]) {
     out[2] = rec[2] >= 0 && rec[2] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[2]] : -1;
     out[3] = rec[3] >= 0 && rec[3] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[3]] : -1;
     out[4] = rec[4];
+    return RP_OK;
+}
+
+rp_status rp_last_schedule(rp_world* w, int32_t scene, int32_t which, int32_t* level_out, int32_t* bodies_out,
+                           uint32_t cap, uint32_t* count) {
+    if (check_world(w) || scene < 0 || scene >= w->num_scenes || (which != 0 && which != 1) || !count)
+        return fail(RP_ERR_INVALID, "bad argument");
+    if (w->device < 0 || !w->d_scene_nodes.p || w->static_dirty) return fail(RP_ERR_STATE, "no step has run");
+    RP_CUDA(cudaSetDevice(w->device));
+    int32_t nn = 0;
+    RP_CUDA(cudaMemcpyAsync(&nn, w->d_scene_nodes.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    *count = (uint32_t)nn;
+    const int32_t nbase = w->scene_node_cap[(size_t)scene];
+    const uint32_t m = std::min<uint32_t>((uint32_t)nn, cap);
+    if (m == 0) return RP_OK;
+    std::vector<int32_t> lev(m), bod(2 * (size_t)m);
+    const DevBuf& L = which ? w->d_node_vlevel : w->d_node_level;
+    RP_CUDA(cudaMemcpyAsync(lev.data(), L.as<int32_t>() + nbase, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaMemcpyAsync(bod.data(), w->d_node_body.as<int32_t>() + 2 * (size_t)nbase, 2 * (size_t)m * 4,
+                            cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    for (uint32_t k = 0; k < m; ++k) {
+        if (level_out) level_out[k] = lev[k];
+        if (bodies_out)
+            for (int j = 0; j < 2; ++j) {
+                const int32_t b = bod[2 * (size_t)k + (size_t)j];
+                bodies_out[2 * (size_t)k + (size_t)j] = b >= 0 ? w->slot_to_entity[(size_t)b] : -1;
+            }
+    }
+    return RP_OK;
+}
+
+rp_status rp_world_set_sweep_order(rp_world* w, int32_t order) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (order != RP_SWEEP_REFERENCE && order != RP_SWEEP_COLOURED) return fail(RP_ERR_INVALID, "bad sweep order");
+    w->sweep_order = order;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }   // the order is a kernel argument
     return RP_OK;
 }
 

@@ -180,7 +180,11 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
     }
     for (int e = t; e < next; e += n)
         for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
-    for (int s = t; s < W.num_scenes; s += n) W.contact_count[s] = 0;
+    for (int s = t; s < W.num_scenes; s += n) {
+        W.contact_count[s] = 0;
+        W.act_count[2 * s] = 0;
+        W.act_count[2 * s + 1] = 0;
+    }
     if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; }
 }
 
@@ -431,24 +435,24 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
 // ---------------------------------------------------------------------------------------------
 // Gauss–Seidel sweeps: one CTA per scene, or the whole cooperative grid on one large scene.
 template <typename R, bool EXACT, bool VELOCITY>
-__global__ void __launch_bounds__(BLOCK) k_sweep_cta(WorldView<R> W, double h) {
+__global__ void __launch_bounds__(BLOCK) k_sweep_cta(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
     CtaGroup g;
     for (int s = blockIdx.x; s < W.num_scenes; s += gridDim.x) {
-        const int L = W.scene_levels[s];
-        const int* lstart = W.level_count + s * (W.max_levels + 1);
-        sweep_levels<R, EXACT, VELOCITY>(W, g, s, L, lstart, W.scene_node_cap[s], (R)h);
+        if (!VELOCITY && resched_first) resched(W, g, s);
+        sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
         __syncthreads();
     }
 }
 
 // One warp per scene: a scene's levels are mostly a few nodes wide, so a warp (barrier: __syncwarp)
 // sweeps them as fast as a CTA would while many more scenes are in flight per SM. Warps take scenes
-// from a counter (queue[1], zeroed before the launch) in decreasing-size order.
+// from a counter (queue[1], zeroed before the launch) in decreasing-size order. The first position
+// sweep of a substep builds the substep's schedules first (resched).
 constexpr int SWEEP_WARP_BLOCK = 128;
 
 template <typename R, bool EXACT, bool VELOCITY>
-__global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h) {
+__global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
     WarpGroup g;
     const int lane = threadIdx.x & 31;
@@ -458,22 +462,21 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= W.num_scenes) break;
         const int s = W.scene_order[i];
-        const int L = W.scene_levels[s];
-        const int* lstart = W.level_count + s * (W.max_levels + 1);
-        sweep_levels<R, EXACT, VELOCITY>(W, g, s, L, lstart, W.scene_node_cap[s], (R)h);
+        if (!VELOCITY && resched_first) resched(W, g, s);
+        sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
         __syncwarp();
     }
 }
 
 template <typename R, bool EXACT, bool VELOCITY>
-__global__ void __launch_bounds__(BLOCK) k_sweep_grid(WorldView<R> W, double h) {
+__global__ void __launch_bounds__(BLOCK) k_sweep_grid(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
     GridGroup g;
     g.bar = W.barrier;
     g.status = W.status;
     g.limit_ns = W.wait_ns;
-    const int L = W.scene_levels[0];
-    sweep_levels<R, EXACT, VELOCITY>(W, g, 0, L, W.level_count, W.scene_node_cap[0], (R)h);
+    if (!VELOCITY && resched_first) resched(W, g, 0);
+    sweep_levels<R, EXACT, VELOCITY>(W, g, 0, (R)h);
 }
 
 }  // namespace rp
@@ -530,10 +533,10 @@ struct PipeLauncher {
     }
 
     template <bool VELOCITY>
-    static cudaError_t sweep_warp(const WorldView<R>& W, const PipeConfig& c, cudaStream_t st, double h) {
+    static cudaError_t sweep_warp(const WorldView<R>& W, const PipeConfig& c, cudaStream_t st, double h, int first) {
         cudaError_t e = cudaMemsetAsync(W.queue + 1, 0, sizeof(int32_t), st);
         if (e != cudaSuccess) return e;
-        k_sweep_warp<R, EXACT, VELOCITY><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h);
+        k_sweep_warp<R, EXACT, VELOCITY><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h, first);
         return cudaGetLastError();
     }
 
@@ -574,17 +577,18 @@ struct PipeLauncher {
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_MANIFOLD)) != cudaSuccess) return e;
             }
             for (int it = 0; it < P.num_pos_iters; ++it) {
-                if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, false>, c.sweep_grid_blocks, BLOCK, st, W, h);
-                else if (c.sweep_cta) k_sweep_cta<R, EXACT, false><<<d.num_scenes, BLOCK, 0, st>>>(W, h), e = cudaGetLastError();
-                else e = sweep_warp<false>(W, c, st, h);
+                const int first = it == 0 ? 1 : 0;   // the substep's schedules are built by its first sweep
+                if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, false>, c.sweep_grid_blocks, BLOCK, st, W, h, first);
+                else if (c.sweep_cta) k_sweep_cta<R, EXACT, false><<<d.num_scenes, BLOCK, 0, st>>>(W, h, first), e = cudaGetLastError();
+                else e = sweep_warp<false>(W, c, st, h, first);
                 if (e != cudaSuccess) return e;
             }
             if ((e = mark(PH_SOLVE)) != cudaSuccess) return e;
             k_velocity<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, h);
             if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_VELOCITY)) != cudaSuccess) return e;
-            if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, true>, c.vsweep_grid_blocks, BLOCK, st, W, h);
-            else if (c.sweep_cta) k_sweep_cta<R, EXACT, true><<<d.num_scenes, BLOCK, 0, st>>>(W, h), e = cudaGetLastError();
-            else e = sweep_warp<true>(W, c, st, h);
+            if (d.grid_mode) e = coop(k_sweep_grid<R, EXACT, true>, c.vsweep_grid_blocks, BLOCK, st, W, h, 0);
+            else if (c.sweep_cta) k_sweep_cta<R, EXACT, true><<<d.num_scenes, BLOCK, 0, st>>>(W, h, 0), e = cudaGetLastError();
+            else e = sweep_warp<true>(W, c, st, h, 0);
             if (e != cudaSuccess || (e = mark(PH_VSOLVE)) != cudaSuccess) return e;
         }
         return cudaSuccess;

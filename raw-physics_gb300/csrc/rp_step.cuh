@@ -534,7 +534,9 @@ __device__ void islands(const WorldView<R>& W, const G& g, int s, double dt) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Order-preserving colouring of the Gauss–Seidel sweep.
+// The frame's solver nodes (external constraints, then broad-phase pairs, in the reference's
+// constraint order): each node's dynamic bodies, and every dynamic body's timeline (the nodes that
+// touch it, in constraint order). The per-substep schedules below are built from these.
 template <typename R, class G>
 __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
     const int b0 = W.scene_body[s], nb = W.scene_body[s + 1] - b0;
@@ -544,14 +546,9 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
     const int nbase = W.scene_node_cap[s];
     const int nn = ne + np;
     int* nbody = W.node_body + 2 * nbase;
-    int* npred = W.node_pred + 2 * nbase;
-    int* nlev = W.node_level + nbase;
     int* tl = W.body_tl + 2 * nbase;
-    int* lcount = W.level_count + s * (W.max_levels + 1);
-    int* lfill = W.level_fill + s * (W.max_levels + 1);
     for (int b = g.rank(); b < nb; b += g.size()) W.body_tl_count[b0 + b] = 0;
-    for (int l = g.rank(); l <= W.max_levels; l += g.size()) { lcount[l] = 0; lfill[l] = 0; }
-    if (g.rank() == 0) { W.scene_levels[s] = 0; W.scene_nodes[s] = nn; }
+    if (g.rank() == 0) W.scene_nodes[s] = nn;
     g.sync();
     for (int k = g.rank(); k < nn; k += g.size()) {
         int a, c;
@@ -565,9 +562,6 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
         int bc = (live && !W.fixed[c] && c != a) ? c : -1;
         nbody[2 * k] = ba;
         nbody[2 * k + 1] = bc;
-        npred[2 * k] = -1;
-        npred[2 * k + 1] = -1;
-        nlev[k] = live ? 0 : -1;
         if (ba >= 0) atomicAdd(&W.body_tl_count[ba], 1);
         if (bc >= 0) atomicAdd(&W.body_tl_count[bc], 1);
     }
@@ -587,7 +581,7 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
         }
     }
     g.sync();
-    // sort every timeline (short: a body's broad-phase degree) and link predecessors
+    // sort every timeline (short: a body's broad-phase degree) into constraint order
     for (int b = g.rank(); b < nb; b += g.size()) {
         int st = W.body_tl_start[b0 + b], cnt = W.body_tl_count[b0 + b];
         int* t = tl + st;
@@ -596,61 +590,280 @@ __device__ void schedule(const WorldView<R>& W, const G& g, int s, int* smem) {
             while (j >= 0 && t[j] > key) { t[j + 1] = t[j]; --j; }
             t[j + 1] = key;
         }
-        for (int i = 1; i < cnt; ++i) {
-            int k = t[i];
-            int side = (nbody[2 * k] == b0 + b) ? 0 : 1;
-            npred[2 * k + side] = t[i - 1];
-        }
     }
     g.sync();
-    // longest-path levels by monotone relaxation
-    // three rotating "changed" flags: the one reset in round r was last read in round r-2
-    int* flag = lfill + W.max_levels - 2;
-    if (g.rank() == 0) { flag[0] = 0; flag[1] = 0; flag[2] = 0; }
-    g.sync();
-    for (int round = 0; round < W.max_levels; ++round) {
-        if (g.rank() == 0) flag[(round + 1) % 3] = 0;
-        bool changed = false;
-        for (int k = g.rank(); k < nn; k += g.size()) {
-            int lk = nlev[k];
-            if (lk < 0) continue;
-            int p0 = npred[2 * k], p1 = npred[2 * k + 1];
-            int l0 = p0 >= 0 ? ((volatile int*)nlev)[p0] : -1;
-            int l1 = p1 >= 0 ? ((volatile int*)nlev)[p1] : -1;
-            int nl = max(l0, l1) + 1;
-            if (nl > lk) { ((volatile int*)nlev)[k] = nl; changed = true; }
-        }
-        if (changed) flag[round % 3] = 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Per-substep schedules of the two Gauss–Seidel sweeps, built after the substep's narrowphase.
+//
+// A node is active in the position sweep (schedule 0) when it is an external constraint or a pair
+// with contacts this substep, and in the velocity sweep (schedule 1) when it is a pair with contacts;
+// every other node is a no-op there (solve_node / vsolve_node return at once). An active node's
+// predecessor on each of its dynamic bodies is the previous active node of that body's timeline.
+//
+// Reference order (SWEEP_REFERENCE): a node's level is the longest path to it over those links.
+// Nodes of one level share no dynamic body, and nodes that share one keep their constraint order,
+// so sweeping level by level reproduces the reference's serial sweep (pbd.cpp:615-620, 646-740)
+// exactly; leaving the no-op nodes out of the chains only removes waits that did nothing.
+//
+// Coloured order (SWEEP_COLOURED): a proper colouring of the active nodes (nodes sharing a dynamic
+// body get different colours) by Jones–Plassmann rounds with hashed priorities: an uncoloured node
+// whose uncoloured neighbours all have lower priority takes the smallest colour its neighbours do
+// not use. Sweeping colour by colour is a Gauss–Seidel sweep in another order (not the reference's),
+// with far fewer dependent steps: a joint chain takes two or three colours instead of one level per
+// link.
+enum { SWEEP_REFERENCE = 0, SWEEP_COLOURED = 1 };
+constexpr int COLOUR_WORDS = 2;                  // colours 0..127 from the mask; beyond, 128 + round
+constexpr int RESCHED_ONE_CTA = 8192;            // grid group: at most this many active nodes relax on one CTA
+
+__device__ __forceinline__ uint32_t node_priority(int k, int salt) {
+    uint32_t x = (uint32_t)k * 0x9E3779B1u + (uint32_t)salt * 0x85EBCA77u;
+    x ^= x >> 15;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    return x;
+}
+
+// "Does any thread of the relaxing sub-group see a change?" and a barrier of that sub-group.
+struct SubWarp {
+    __device__ int rank() const { return (int)(threadIdx.x & 31); }
+    __device__ int size() const { return 32; }
+    __device__ bool any(bool c, int*) const {
+        __syncwarp();   // orders the lanes' writes of this round before the next round's reads
+        return __any_sync(0xffffffffu, c) != 0;
+    }
+    __device__ void sync() const { __syncwarp(); }
+};
+struct SubBlock {
+    __device__ int rank() const { return (int)threadIdx.x; }
+    __device__ int size() const { return (int)blockDim.x; }
+    __device__ bool any(bool c, int*) const { return __syncthreads_or(c) != 0; }
+    __device__ void sync() const { __syncthreads(); }
+};
+struct SubGrid {   // the whole cooperative grid; `flags`: three words of global scratch, zeroed
+    GridGroup g;
+    mutable int round = 0;
+    __device__ int rank() const { return g.rank(); }
+    __device__ int size() const { return g.size(); }
+    __device__ bool any(bool c, int* flags) const {
+        // three rotating flags: the one cleared in round r was last read in round r - 2
+        if (g.rank() == 0) flags[(round + 1) % 3] = 0;
+        if (c) flags[round % 3] = 1;
         g.sync();
-        if (((volatile int*)flag)[round % 3] == 0) break;
-        if (round == W.max_levels - 1 && g.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW);
+        const bool r = ((volatile int*)flags)[round % 3] != 0;
+        ++round;
+        return r;
     }
-    g.sync();
-    // bucket nodes by level
+    __device__ void sync() const { g.sync(); }
+};
+
+template <typename R>
+struct SchedView {   // one of the two schedules of scene s
+    int* pred;       // [2 * nodes] (scene base applied)
+    int* lev;        // [nodes]
+    int* count;      // [max_levels + 1]
+    int* fill;       // [max_levels + 1]; the last three words are relaxation flags
+    int* nodes;      // [nodes] (scene base applied)
+    int* list;       // [nodes] active nodes, unordered
+    int* levels;     // number of levels of the scene
+    int* active;     // number of active nodes of the scene
+};
+
+template <typename R>
+__device__ __forceinline__ SchedView<R> sched_view(const WorldView<R>& W, int s, int which) {
+    const int nbase = W.scene_node_cap[s];
+    SchedView<R> v;
+    v.pred = (which ? W.node_vpred : W.node_pred) + 2 * nbase;
+    v.lev = (which ? W.node_vlevel : W.node_level) + nbase;
+    v.count = (which ? W.vlevel_count : W.level_count) + s * (W.max_levels + 1);
+    v.fill = (which ? W.vlevel_fill : W.level_fill) + s * (W.max_levels + 1);
+    v.nodes = (which ? W.vlevel_nodes : W.level_nodes) + nbase;
+    v.list = W.act_list + (size_t)which * W.scene_node_cap[W.num_scenes] + nbase;
+    v.levels = (which ? W.scene_vlevels : W.scene_levels) + s;
+    v.active = W.act_count + 2 * s + which;
+    return v;
+}
+
+// Levels (reference order) or colours (coloured order) of one schedule's active nodes, by sub-group q.
+template <typename R, class Q>
+__device__ void relax_schedule(const WorldView<R>& W, const Q& q, int s, const SchedView<R>& v, int n, int order) {
+    const int nbase = W.scene_node_cap[s];
+    const int* nbody = W.node_body + 2 * nbase;
+    const int* tl = W.body_tl + 2 * nbase;
+    volatile int* lev = v.lev;
+    int* flags = v.fill + W.max_levels - 2;
+    if (order == SWEEP_REFERENCE) {
+        for (int round = 0;; ++round) {
+            bool changed = false;
+            for (int i = q.rank(); i < n; i += q.size()) {
+                const int k = v.list[i];
+                const int p0 = v.pred[2 * k], p1 = v.pred[2 * k + 1];
+                const int l0 = p0 >= 0 ? lev[p0] : -1, l1 = p1 >= 0 ? lev[p1] : -1;
+                const int nl = max(l0, l1) + 1;
+                if (nl > lev[k]) { lev[k] = nl; changed = true; }
+            }
+            if (!q.any(changed, flags)) break;
+            if (round >= W.max_levels) {
+                if (q.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW);
+                break;
+            }
+        }
+        return;
+    }
+    // coloured: lev = -2 while uncoloured
+    for (int round = 0;; ++round) {
+        bool pending = false;
+        for (int i = q.rank(); i < n; i += q.size()) {
+            const int k = v.list[i];
+            if (lev[k] != -2) continue;
+            const uint32_t pk = node_priority(k, s);
+            uint32_t used[COLOUR_WORDS] = {0u, 0u};
+            bool ready = true;
+            for (int side = 0; side < 2 && ready; ++side) {
+                const int b = nbody[2 * k + side];
+                if (b < 0) continue;
+                const int st = W.body_tl_start[b], cnt = W.body_tl_count[b];
+                for (int t = 0; t < cnt; ++t) {
+                    const int j = tl[st + t];
+                    if (j == k) continue;
+                    const int lj = lev[j];
+                    if (lj == -1) continue;                       // not active in this schedule
+                    if (lj == -2) {
+                        const uint32_t pj = node_priority(j, s);
+                        if (pj > pk || (pj == pk && j > k)) { ready = false; break; }
+                    } else if (lj < 32 * COLOUR_WORDS) {
+                        used[lj >> 5] |= 1u << (lj & 31);
+                    }
+                }
+            }
+            if (!ready) { pending = true; continue; }
+            int c = -1;
+            for (int wd = 0; wd < COLOUR_WORDS && c < 0; ++wd)
+                if (~used[wd]) c = 32 * wd + __ffs(~used[wd]) - 1;
+            if (c < 0) c = 32 * COLOUR_WORDS + round;             // every small colour taken
+            lev[k] = c;
+        }
+        if (!q.any(pending, flags)) break;
+        if (round >= W.max_levels - 32 * COLOUR_WORDS - 4) {
+            if (q.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW);
+            break;
+        }
+    }
+}
+
+// Buckets one schedule's active nodes by level / colour into v.nodes, by sub-group q.
+template <typename R, class Q>
+__device__ void bucket_schedule(const WorldView<R>& W, const Q& q, int s, const SchedView<R>& v, int n, bool count_levels) {
     int maxl = -1;
-    for (int k = g.rank(); k < nn; k += g.size()) {
-        int l = nlev[k];
-        if (l < 0) continue;
-        if (l >= W.max_levels - 3) { atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW); continue; }
-        atomicAdd(&lcount[l], 1);
+    for (int i = q.rank(); i < n; i += q.size()) {
+        const int l = v.lev[v.list[i]];
+        if (l < 0 || l >= W.max_levels - 3) { atomicOr(&W.status[s], (uint32_t)ST_LEVEL_OVERFLOW); continue; }
+        atomicAdd(&v.count[l], 1);
         maxl = max(maxl, l);
     }
-    if (maxl >= 0) atomicMax(&W.scene_levels[s], maxl + 1);
-    g.sync();
-    if (g.rank() == 0) {
-        // exclusive prefix over the (few) levels; lfill doubles as the per-level fill counter
-        int L = W.scene_levels[s], acc = 0;
-        atomicAdd(&W.counters[6], (unsigned long long)L);
-        for (int l = 0; l <= L; ++l) { int c = lcount[l]; lcount[l] = acc; acc += c; }
+    if (maxl >= 0) atomicMax(v.levels, maxl + 1);
+    q.sync();
+    if (q.rank() == 0) {
+        const int L = *v.levels;
+        if (count_levels) atomicAdd(&W.counters[6], (unsigned long long)L);
+        int acc = 0;
+        for (int l = 0; l <= L; ++l) { const int c = v.count[l]; v.count[l] = acc; acc += c; }
     }
-    g.sync();
-    for (int k = g.rank(); k < nn; k += g.size()) {
-        int l = nlev[k];
+    q.sync();
+    for (int i = q.rank(); i < n; i += q.size()) {
+        const int k = v.list[i];
+        const int l = v.lev[k];
         if (l < 0 || l >= W.max_levels - 3) continue;
-        int slot = atomicAdd(&lfill[l], 1);
-        W.level_nodes[nbase + lcount[l] + slot] = k;
+        v.nodes[v.count[l] + atomicAdd(&v.fill[l], 1)] = k;
+    }
+    q.sync();
+}
+
+// Both per-substep schedules of scene s by group g (run after the substep's narrowphase, before the
+// position sweep; the per-scene active counters were zeroed by the substep's predict phase).
+template <typename R, class G>
+__device__ void resched(const WorldView<R>& W, const G& g, int s) {
+    const int b0 = W.scene_body[s], nb = W.scene_body[s + 1] - b0;
+    const int ne = W.scene_ext[s + 1] - W.scene_ext[s];
+    const int nbase = W.scene_node_cap[s];
+    const int pbase = W.scene_pair_cap[s];
+    const int nn = W.scene_nodes[s];
+    const int* nbody = W.node_body + 2 * nbase;
+    const int* tl = W.body_tl + 2 * nbase;
+    const int order = W.sweep_order;
+    const int unset = order == SWEEP_COLOURED ? -2 : 0;
+    const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
+    // the level tables are zero beyond the previous substep's levels (zeroed when the world is built)
+    const int used0 = min(*(volatile int*)v0.levels + 1, W.max_levels), used1 = min(*(volatile int*)v1.levels + 1, W.max_levels);
+    for (int l = g.rank(); l <= used0; l += g.size()) { v0.count[l] = 0; v0.fill[l] = 0; }
+    for (int l = g.rank(); l <= used1; l += g.size()) { v1.count[l] = 0; v1.fill[l] = 0; }
+    // predecessor links along every dynamic body's timeline
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        const int st = W.body_tl_start[b0 + b], cnt = W.body_tl_count[b0 + b];
+        int prev0 = -1, prev1 = -1;
+        for (int i = 0; i < cnt; ++i) {
+            const int k = tl[st + i];
+            const int side = nbody[2 * k] == b0 + b ? 0 : 1;
+            const bool contacts = k >= ne && W.pair_ccount[pbase + k - ne] > 0;
+            if (k < ne || contacts) { v0.pred[2 * k + side] = prev0; prev0 = k; }
+            if (contacts) { v1.pred[2 * k + side] = prev1; prev1 = k; }
+        }
+    }
+    // activity per node, the sides without a dynamic body, and the two active lists
+    for (int k = g.rank(); k < nn; k += g.size()) {
+        const bool live = nbody[2 * k] >= 0 || nbody[2 * k + 1] >= 0;
+        const bool contacts = live && k >= ne && W.pair_ccount[pbase + k - ne] > 0;
+        const bool a0 = live && (k < ne || contacts);
+        v0.lev[k] = a0 ? unset : -1;
+        v1.lev[k] = contacts ? unset : -1;
+        for (int side = 0; side < 2; ++side)
+            if (nbody[2 * k + side] < 0) { v0.pred[2 * k + side] = -1; v1.pred[2 * k + side] = -1; }
+        if (a0) v0.list[atomicAdd(v0.active, 1)] = k;
+        if (contacts) v1.list[atomicAdd(v1.active, 1)] = k;
     }
     g.sync();
+    const int n0 = *(volatile int*)v0.active, n1 = *(volatile int*)v1.active;
+    if (g.rank() == 0) { *v0.levels = 0; *v1.levels = 0; }
+    if constexpr (std::is_same<G, GridGroup>::value) {
+        if (n0 + n1 <= RESCHED_ONE_CTA) {
+            if (g.block() == 0) {
+                SubBlock q;
+                if (n0 + n1 > 0) {
+                    relax_schedule(W, q, s, v0, n0, order);
+                    relax_schedule(W, q, s, v1, n1, order);
+                }
+                bucket_schedule(W, q, s, v0, n0, true);
+                bucket_schedule(W, q, s, v1, n1, false);
+            }
+        } else {
+            SubGrid q{g};
+            if (g.rank() == 0) {
+                int* f0 = v0.fill + W.max_levels - 2;
+                int* f1 = v1.fill + W.max_levels - 2;
+                f0[0] = f0[1] = f0[2] = 0;
+                f1[0] = f1[1] = f1[2] = 0;
+            }
+            g.sync();
+            relax_schedule(W, q, s, v0, n0, order);
+            relax_schedule(W, q, s, v1, n1, order);
+            bucket_schedule(W, q, s, v0, n0, true);
+            bucket_schedule(W, q, s, v1, n1, false);
+        }
+        g.sync();
+    } else if constexpr (std::is_same<G, WarpGroup>::value) {
+        SubWarp q;
+        relax_schedule(W, q, s, v0, n0, order);
+        relax_schedule(W, q, s, v1, n1, order);
+        bucket_schedule(W, q, s, v0, n0, true);
+        bucket_schedule(W, q, s, v1, n1, false);
+    } else {
+        SubBlock q;
+        relax_schedule(W, q, s, v0, n0, order);
+        relax_schedule(W, q, s, v1, n1, order);
+        bucket_schedule(W, q, s, v0, n0, true);
+        bucket_schedule(W, q, s, v1, n1, false);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1004,15 +1217,18 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
 constexpr int SOLO_NODES = 2 * BLOCK;   // default of WorldView::solo_nodes
 
 template <typename R, bool EXACT, bool VELOCITY, class G>
-__device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, int L, const int* lstart, int nbase, R hR) {
+__device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, R hR) {
+    const SchedView<R> v = sched_view(W, s, VELOCITY ? 1 : 0);
+    const int L = *(volatile int*)v.levels;
+    const int* lstart = v.count;
     const int solo = W.solo_nodes > 0 ? W.solo_nodes : SOLO_NODES;
     int l = 0;
     while (l < L) {
         int cnt = lstart[l + 1] - lstart[l];
         if (g.nblocks() == 1 || cnt > solo) {
             for (int i = lstart[l] + g.rank(); i < lstart[l + 1]; i += g.size()) {
-                if (VELOCITY) vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
-                else solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                if (VELOCITY) vsolve_node<R, EXACT>(W, s, v.nodes[i], hR);
+                else solve_node<R, EXACT>(W, s, v.nodes[i], hR);
             }
             g.sync();
             ++l;
@@ -1023,8 +1239,8 @@ __device__ void sweep_levels(const WorldView<R>& W, const G& g, int s, int L, co
         if (g.block() == 0) {
             for (int k = l; k < l2; ++k) {
                 for (int i = lstart[k] + (int)threadIdx.x; i < lstart[k + 1]; i += blockDim.x) {
-                    if (VELOCITY) vsolve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
-                    else solve_node<R, EXACT>(W, s, W.level_nodes[nbase + i], hR);
+                    if (VELOCITY) vsolve_node<R, EXACT>(W, s, v.nodes[i], hR);
+                    else solve_node<R, EXACT>(W, s, v.nodes[i], hR);
                 }
                 __syncthreads();
             }
@@ -1055,9 +1271,6 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
     mark(PH_ISLANDS);
     schedule(W, g, s, smem);
     mark(PH_SCHEDULE);
-    const int L = W.scene_levels[s];
-    const int nbase = W.scene_node_cap[s];
-    const int* lstart = W.level_count + s * (W.max_levels + 1);
     const int e0 = W.scene_ext[s], e1 = W.scene_ext[s + 1];
     for (int sub = 0; sub < P.num_substeps; ++sub) {
         for (int b = b0 + g.rank(); b < b1; b += g.size()) predict_body<R, EXACT>(W, b, h);
@@ -1067,6 +1280,8 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
             W.contact_count[s] = 0;
             W.work[s] = 0;
             if (s == 0) atomicAdd(&W.queue[4], 1);
+            W.act_count[2 * s] = 0;
+            W.act_count[2 * s + 1] = 0;
         }
         g.sync();
         mark(PH_PREDICT);
@@ -1081,12 +1296,14 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
         }
         g.sync();
         mark(PH_NARROW);
-        for (int it = 0; it < P.num_pos_iters; ++it) sweep_levels<R, EXACT, false>(W, g, s, L, lstart, nbase, hR);
+        resched(W, g, s);
+        mark(PH_SCHEDULE);
+        for (int it = 0; it < P.num_pos_iters; ++it) sweep_levels<R, EXACT, false>(W, g, s, hR);
         mark(PH_SOLVE);
         for (int b = b0 + g.rank(); b < b1; b += g.size()) velocity_body<R, EXACT>(W, b, h);
         g.sync();
         mark(PH_VELOCITY);
-        sweep_levels<R, EXACT, true>(W, g, s, L, lstart, nbase, hR);
+        sweep_levels<R, EXACT, true>(W, g, s, hR);
         mark(PH_VSOLVE);
     }
 }

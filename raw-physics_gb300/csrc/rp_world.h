@@ -148,11 +148,22 @@ struct WorldView {
     int32_t* body_tl_count;  // [N] timeline lengths / fill counters
     int32_t* body_tl_start;  // [N+1] timeline CSR starts (per scene relative to node base)
     int32_t* body_tl;        // [2 * nodes] timeline entries
+    // the substep's two sweep schedules (resched): position sweep (node_pred, node_level, level_*,
+    // scene_levels) and velocity sweep (node_vpred, node_vlevel, vlevel_*, scene_vlevels)
     int32_t* level_count;    // [S * (max_levels+1)] nodes per level, then prefix
     int32_t* level_fill;     // [S * (max_levels+1)] fill counters; the last three words are flags
     int32_t* scan_tmp;       // [grid blocks] group-scan partial sums
     int32_t* level_nodes;    // [nodes] nodes sorted by level
     int32_t* scene_levels;   // [S] number of levels
+    int32_t* node_vpred;     // [2 * nodes]
+    int32_t* node_vlevel;    // [nodes]
+    int32_t* vlevel_count;   // [S * (max_levels+1)]
+    int32_t* vlevel_fill;    // [S * (max_levels+1)]
+    int32_t* vlevel_nodes;   // [nodes]
+    int32_t* scene_vlevels;  // [S]
+    int32_t* act_list;       // [2 * nodes] active nodes of each schedule (position, then velocity)
+    int32_t* act_count;      // [2 * S] their counts (zeroed by the substep's predict phase)
+    int32_t sweep_order;     // SWEEP_REFERENCE (the reference's serial order) or SWEEP_COLOURED
     int32_t* scene_nodes;    // [S] number of live nodes (ext + pairs)
     int32_t* pair_cstart;    // [pairs] first contact of each pair
     int32_t* pair_ccount;    // [pairs]

@@ -74,6 +74,8 @@ SIGNATURES = {
     "rp_counters": (_i, [_W, _P(_u64)]),
     "rp_world_set_mode": (_i, [_W, _i]),
     "rp_world_set_wait_limit": (_i, [_W, _u64]),
+    "rp_world_set_sweep_order": (_i, [_W, _i]),
+    "rp_last_schedule": (_i, [_W, _i, _i, _P(_i), _P(_i), _u, _P(_u)]),
     "rp_degenerate_info": (_i, [_W, _P(C.c_int64)]),
     "rp_adjoint_profile": (_i, [_W, _P(_d)]),
     "rp_adjoint_trajectory": (_i, [_W, _d, _u, _u, _i, _u, _u, _P(_i), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d)]),
@@ -427,6 +429,24 @@ class World:
             return None
         return {"bits": [v for k, v in STATUS_BITS.items() if int(out[0]) & k], "scene": int(out[1]),
                 "pair": (int(out[2]), int(out[3])), "substep": int(out[4])}
+
+    SWEEP_ORDERS = {"reference": 0, "coloured": 1}
+
+    def last_schedule(self, scene: int = 0, which: int = 0):
+        """(levels (n,), bodies (n, 2)) of the last substep's position (which=0) or velocity (1)
+        sweep schedule: per solver node its level / colour (-1: no-op) and its dynamic entities."""
+        n = _u()
+        self._check(self.lib.rp_last_schedule(self.h, scene, which, None, None, 0, C.byref(n)))
+        lev = np.zeros(max(n.value, 1), dtype=np.int32)
+        bod = np.zeros(2 * max(n.value, 1), dtype=np.int32)
+        self._check(self.lib.rp_last_schedule(self.h, scene, which, lev.ctypes.data_as(_P(_i)), bod.ctypes.data_as(_P(_i)),
+                                              n.value, C.byref(n)))
+        return lev[: n.value], bod[: 2 * n.value].reshape(-1, 2)
+
+    def set_sweep_order(self, order: str):
+        """Gauss-Seidel order of the sweeps: "reference" (the reference's serial order, the default)
+        or "coloured" (graph-coloured; results differ from the reference's by the reordering)."""
+        self._check(self.lib.rp_world_set_sweep_order(self.h, self.SWEEP_ORDERS[order]))
 
     def set_wait_limit(self, microseconds: int):
         """Bound of every device-side wait (grid barriers); a wait that runs out undoes the call and

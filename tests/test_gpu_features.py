@@ -418,3 +418,51 @@ def test_wait_limit_runs_out_undoes_the_call_and_world_recovers(ext_built, oracl
     o.step(1)
     assert np.array_equal(w.get_state(), o.get_state())
     w.close()
+
+
+def _check_schedule(lev, bod, ne, which, order):
+    """The properties a sweep schedule must have: velocity sweeps hold no external constraint; in
+    reference order every active node's level is one more than the latest earlier active node on
+    either of its bodies (so shared-body nodes keep constraint order and levels are as short as that
+    allows); in coloured order no two active nodes of one colour share a dynamic body."""
+    act = lev >= 0
+    if which == 1:
+        assert not act[:ne].any(), "an external constraint in the velocity sweep"
+    if order == "reference":
+        last = {}
+        for k in np.nonzero(act)[0]:
+            bs = [int(b) for b in bod[k] if b >= 0]
+            expect = 1 + max([last.get(b, -1) for b in bs] + [-1])
+            assert lev[k] == expect, (k, lev[k], expect)
+            for b in bs:
+                last[b] = int(lev[k])
+    else:
+        for c in np.unique(lev[act]):
+            bs = bod[(lev == c)].ravel()
+            bs = bs[bs >= 0]
+            assert len(bs) == len(np.unique(bs)), "colour %d: two constraints share a body" % c
+    return int(lev.max()) + 1 if act.any() else 0
+
+
+@pytest.mark.parametrize("order", ["reference", "coloured"])
+def test_sweep_schedules_are_valid(ext_built, order):
+    """The per-substep sweep schedules (built after each substep's narrowphase from the constraints
+    that act in it) of a pile and of a hinge chain, in both Gauss-Seidel orders."""
+    from rawphys import scenes as S
+    parts = [S.random_pile_scene(16, seed=4), S.chain_scene(24, "hinge", seed=2)]
+    w = ext_built.World(0, "fp32")
+    w.set_sweep_order(order)
+    for i, sc in enumerate(parts):
+        w.load(sc, scene_id=0 if i == 0 else w.new_scene())
+    w.simulate(1.0 / 60.0, 20, 1, True, 12)
+    depth = {}
+    for s, sc in enumerate(parts):
+        for which in (0, 1):
+            lev, bod = w.last_schedule(s, which)
+            depth[(s, which)] = _check_schedule(lev, bod, len(sc.constraints), which, order)
+    assert depth[(0, 0)] > 0 and depth[(1, 0)] > 0
+    if order == "coloured":
+        assert depth[(1, 0)] <= 6, "a chain needs a few colours, not one per link"
+    else:
+        assert depth[(1, 0)] >= 23, "reference order keeps one step per chain link"
+    w.close()
