@@ -537,7 +537,8 @@ def measure_plain(args, dev, precision, steps, start_from=None, with_oracle=Fals
     e2e_wall, h2d, d2h = e2e_frames(w, stream, flush, start_state, max(3, steps // 2))
     status = w.status()
     w.close()
-    out = {"value": value, "unit": UNIT, "precision": precision, "ms_per_step": total_ms / steps, "steps": steps,
+    dropin = dropin_e2e(args, scene, start_state, flush, max(3, steps // 2)) if precision == "fp32" else None
+    out = {"value": value, "unit": UNIT, "precision": precision, "e2e_dropin": dropin, "ms_per_step": total_ms / steps, "steps": steps,
            "clocks": clocks, "gpu_launches": launches, "device_status": status, "phase_ms_per_step": phase,
            "autotuned": tuned, "start_state": start_state,
            "e2e": {"value": scene.num_dynamic * scene.substeps * max(3, steps // 2) / e2e_wall, "unit": UNIT,
@@ -554,6 +555,46 @@ def measure_plain(args, dev, precision, steps, start_from=None, with_oracle=Fals
                                "sample": "1 frame of the scene from the state the timed GPU frames start from, oracle "
                                          "port, %.1f s" % secs}
     return out
+
+
+def dropin_e2e(args, scene, start_state, flush, frames):
+    """The same metric through the reference's own entry point: the C++-mangled pbd_simulate over
+    Entity** (rawphys.compat builds the caller's structs), as a reference caller runs a frame: add
+    gravity with entity_add_force semantics, call pbd_simulate (FP32 default), clear the forces. Each
+    call writes every entity's state and transformed hulls back into the caller's structs; the L2 is
+    flushed before every call; only the call is timed."""
+    import ctypes as C
+    import torch
+    import rawphys
+    from rawphys import compat
+    lib = C.CDLL(rawphys.LIB_PATH)
+    lib.rp_compat_reset()
+    lib.rp_compat_world.restype = C.c_void_p
+    sim, _ = compat.dropin(lib)
+    callers = compat.build_callers(scene)
+    callers.set_state(start_state)
+    for _ in range(2):
+        callers.add_gravity(scene.gravity)
+        sim(scene.dt, callers.array, scene.substeps, scene.pos_iters, int(scene.collisions))
+        callers.clear_forces()
+    tb0 = (C.c_uint64 * 2)()
+    rawphys.load_library().rp_transfer_bytes(C.c_void_p(lib.rp_compat_world()), tb0)
+    wall = 0.0
+    for k in range(frames):
+        callers.add_gravity(scene.gravity)
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sim(scene.dt, callers.array, scene.substeps, scene.pos_iters, int(scene.collisions))
+        wall += time.perf_counter() - t
+        callers.clear_forces()
+    tb1 = (C.c_uint64 * 2)()
+    rawphys.load_library().rp_transfer_bytes(C.c_void_p(lib.rp_compat_world()), tb1)
+    lib.rp_compat_reset()
+    return {"value": scene.num_dynamic * scene.substeps * frames / wall, "unit": UNIT,
+            "h2d_bytes_per_step": (tb1[0] - tb0[0]) // frames, "d2h_bytes_per_step": (tb1[1] - tb0[1]) // frames,
+            "call": "pbd_simulate(dt, Entity**, 20, 1, true), C++-mangled, FP32 default; state written back and "
+                    "transformed hulls refreshed every call"}
 
 
 def measure_adjoint(args, dev):

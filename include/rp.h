@@ -261,6 +261,16 @@ rp_status rp_degenerate_info(rp_world* w, int64_t out[5]);
 rp_status rp_state_get(rp_world* w, double* out /* num_entities * RP_STATE_DOUBLES */);
 rp_status rp_state_set(rp_world* w, const double* in);
 
+/* colliders_update (src/physics/collider.h:51, collider.cpp:409-446) of every entity's hull colliders
+ * at its current pose, computed on the device in FP64 with the reference's arithmetic (for worlds of
+ * either precision): vertices_out receives 3 doubles per hull vertex, normals_out 3 per hull face
+ * (unit), entity by entity in creation order, collider by collider (sphere colliders take no room).
+ * rp_transformed_hulls_size gives the two counts. This is the caller prelude the reference's examples
+ * run on the host before every step (src/examples/stack.cpp:88-91); the pbd_simulate drop-in uses it
+ * to refresh its callers' transformed geometry. */
+rp_status rp_transformed_hulls_size(rp_world* w, uint64_t* num_vertices, uint64_t* num_normals);
+rp_status rp_transformed_hulls(rp_world* w, double* vertices_out, double* normals_out);
+
 /* -- diagnostics and known-answer entry points --------------------------------------------------- */
 /* broad_get_collision_pairs of one scene on the current state: entity-index pairs in the reference's
  * order. *count receives the total even when it exceeds cap. */

@@ -18,9 +18,17 @@
  *
  * Contract (as the reference's): the caller owns the entities; dt <= 0 is a no-op; every Entity
  * field the reference writes (pose, velocities, previous pose and velocities, active,
- * deactivation_time) is written back, and so are the colliders' transformed vertices and normals
- * (at the final pose). The external constraints are read only. Errors the reference would assert
- * on are reported on stderr and leave the entities untouched.
+ * deactivation_time) is written back, and so are the colliders' transformed vertices and normals.
+ * The external constraints are read only. Errors the reference would assert on are reported on
+ * stderr and leave the entities untouched.
+ * Transformed geometry: every entity's is written at its final pose (colliders_update computed on
+ * the device in FP64), which is what the callers' own colliders_update before the next call computes
+ * (src/examples/stack.cpp:88-91). The reference leaves it at the last substep's predicted pose, and
+ * only for the bodies of that substep's live pairs (pbd.cpp:598-599); nothing in its step reads it
+ * before recomputing it. RP_SHIM_COLLIDERS=none skips the refresh.
+ * Transfers: the entities' state is uploaded only when the caller changed it since the last call
+ * wrote it back, and forces that are exactly the examples' gravity (0, -g / inverse_mass, 0) at the
+ * origin stay on the device as the world's gravity; everything else is uploaded per call.
  * Environment: RP_SHIM_PRECISION=fp64 selects the all-FP64 kernels (default fp32), RP_SHIM_DEVICE
  * the CUDA device (default 0).
  */
@@ -140,6 +148,9 @@ void pbd_simulate_with_constraints(double dt, Entity** entities, Constraint* ext
 extern "C" {
 /* Releases the drop-in's device world (it is rebuilt on the next call). */
 void rp_compat_reset(void);
+/* The drop-in's device world (NULL before the first call), for diagnostics through include/rp.h
+ * (rp_transfer_bytes, rp_counters, ...). */
+struct rp_world* rp_compat_world(void);
 }
 #endif
 #endif

@@ -145,6 +145,10 @@ struct rp_world {
     DevBuf d_tl_count, d_tl_start, d_tl, d_level_count, d_level_fill, d_scan_tmp, d_level_nodes, d_scene_levels,
         d_scene_nodes, d_pair_cstart, d_pair_ccount, d_contact_count, d_work, d_contacts, d_ext_lambda, d_status, d_barrier,
         d_counters, d_phase, d_kat_out, d_kat_count, d_deg;
+    DevBuf d_hull_v, d_hull_n;   // rp_transformed_hulls output (device)
+    HostBuf h_hull;              // and its pinned staging
+    std::vector<int64_t> hull_v_off, hull_n_off;   // per entity: first vertex / normal in entity order
+    int64_t hull_nv = 0, hull_nn = 0;              // totals (vertices, normals) over every hull collider
     DevBuf d_node_vpred, d_node_vlevel, d_vlevel_count, d_vlevel_fill, d_vlevel_nodes, d_scene_vlevels, d_act_list, d_act_count;
 
     // phase-major pipeline
@@ -333,6 +337,18 @@ rp_status build_device(rp_world* w) {
         }
     }
     col_start[N] = (int32_t)cols.size();
+    // entity-order offsets of each entity's transformed geometry (rp_transformed_hulls)
+    w->hull_v_off.assign(N + 1, 0);
+    w->hull_n_off.assign(N + 1, 0);
+    for (size_t e = 0; e < N; ++e) {
+        int64_t nv = 0, nf = 0;
+        for (const rp_collider_desc& d : w->bodies[e].cols)
+            if (d.type == RP_COLLIDER_HULL) { nv += w->hulls[(size_t)d.hull]->nv(); nf += w->hulls[(size_t)d.hull]->nf(); }
+        w->hull_v_off[e + 1] = w->hull_v_off[e] + nv;
+        w->hull_n_off[e + 1] = w->hull_n_off[e] + nf;
+    }
+    w->hull_nv = tv;
+    w->hull_nn = tn;
     // body constants
     std::vector<double> invm(N), I6(6 * N), Ii6(6 * N), mat(4 * N), rad(N);
     std::vector<uint8_t> fixedv(N);
@@ -2035,6 +2051,61 @@ rp_status rp_degenerate_info(rp_world* w, int64_t out[5]) {
     out[2] = rec[2] >= 0 && rec[2] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[2]] : -1;
     out[3] = rec[3] >= 0 && rec[3] < (int32_t)w->slot_to_entity.size() ? w->slot_to_entity[(size_t)rec[3]] : -1;
     out[4] = rec[4];
+    return RP_OK;
+}
+
+rp_status rp_transformed_hulls_size(rp_world* w, uint64_t* num_vertices, uint64_t* num_normals) {
+    if (check_world(w) || !num_vertices || !num_normals) return fail(RP_ERR_INVALID, "null argument");
+    int64_t nv = 0, nn = 0;
+    for (const HostBody& b : w->bodies)
+        for (const rp_collider_desc& d : b.cols)
+            if (d.type == RP_COLLIDER_HULL) { nv += w->hulls[(size_t)d.hull]->nv(); nn += w->hulls[(size_t)d.hull]->nf(); }
+    *num_vertices = (uint64_t)nv;
+    *num_normals = (uint64_t)nn;
+    return RP_OK;
+}
+
+rp_status rp_transformed_hulls(rp_world* w, double* vertices_out, double* normals_out) {
+    if (check_world(w) || !vertices_out || !normals_out) return fail(RP_ERR_INVALID, "null argument");
+    if (w->device < 0) return fail(RP_ERR_NO_DEVICE, "host-only world");
+    if (w->bodies.empty()) return RP_OK;
+    RP_CUDA(cudaSetDevice(w->device));
+    rp_status s = ensure_device(w);
+    if (s != RP_OK) return s;
+    const size_t vb = (size_t)std::max<int64_t>(w->hull_nv, 1) * 24, nb = (size_t)std::max<int64_t>(w->hull_nn, 1) * 24;
+    RP_CUDA(w->d_hull_v.ensure(vb));
+    RP_CUDA(w->d_hull_n.ensure(nb));
+    RP_CUDA(w->h_hull.ensure(vb + nb));
+    WorldHullsArgs a;
+    a.colliders = w->d_colliders.as<Collider>();
+    a.col_body = w->d_col_body.as<int32_t>();
+    a.shapes = w->d_shapes.as<Shape>();
+    a.shape_verts = w->d_shape_verts.as<double>();
+    a.face_normal = w->d_face_normal.as<double>();
+    a.pos = w->d_pos.as<double4_32a>();
+    a.rot = w->d_rot.as<double4_32a>();
+    a.ncolliders = w->dims.ncolliders;
+    a.vertices_out = w->d_hull_v.as<double>();
+    a.normals_out = w->d_hull_n.as<double>();
+    RP_CUDA(world_hulls(a, w->stream));
+    w->launches++;
+    char* h = (char*)w->h_hull.p;
+    RP_CUDA(cudaMemcpyAsync(h, a.vertices_out, (size_t)w->hull_nv * 24, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaMemcpyAsync(h + vb, a.normals_out, (size_t)w->hull_nn * 24, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    w->d2h_bytes += (uint64_t)(w->hull_nv + w->hull_nn) * 24;
+    // device order is slot order (bodies grouped by scene); the output is in entity order
+    const double* hv = (const double*)h;
+    const double* hn = (const double*)(h + vb);
+    int64_t sv = 0, sn = 0;
+    for (size_t slot = 0; slot < w->bodies.size(); ++slot) {
+        const size_t e = (size_t)w->slot_to_entity[slot];
+        const int64_t nv = w->hull_v_off[e + 1] - w->hull_v_off[e], nn = w->hull_n_off[e + 1] - w->hull_n_off[e];
+        std::memcpy(vertices_out + 3 * w->hull_v_off[e], hv + 3 * sv, (size_t)nv * 24);
+        std::memcpy(normals_out + 3 * w->hull_n_off[e], hn + 3 * sn, (size_t)nn * 24);
+        sv += nv;
+        sn += nn;
+    }
     return RP_OK;
 }
 

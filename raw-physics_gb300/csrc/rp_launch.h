@@ -117,6 +117,24 @@ size_t adjoint_contact_bytes(bool tape);
 size_t adjoint_clip_bytes(bool tape);
 size_t adjoint_epa_bytes();
 
+// colliders_update (collider.cpp:409-446) of every hull collider at its body's current pose, in FP64
+// with the reference's arithmetic (built with -fmad=false in rp_kernels_f64.cu): world-space vertices
+// and unit face normals at each collider's transformed-geometry offsets (tv_off / tn_off, 3 doubles
+// each). Works for worlds of either precision: it reads only FP64 poses and shapes.
+struct WorldHullsArgs {
+    const Collider* colliders;
+    const int32_t* col_body;
+    const Shape* shapes;
+    const double* shape_verts;
+    const double* face_normal;
+    const double4_32a* pos;
+    const double4_32a* rot;
+    int ncolliders;
+    double* vertices_out;
+    double* normals_out;
+};
+cudaError_t world_hulls(const WorldHullsArgs& a, cudaStream_t st);
+
 // No-allocation contact query: contacts per call held by its static device scratch (rp_noalloc.cu).
 constexpr int NOALLOC_MAX_CONTACTS = 64;
 cudaError_t noalloc_scratch(int device, double** contacts, int** count);

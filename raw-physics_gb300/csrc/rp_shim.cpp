@@ -3,8 +3,11 @@
 // Each call: (1) if the set of entities, their colliders, mass properties or the external
 // constraints changed since the last call, rebuild the device world from the caller's own data
 // (hull topology forwarded as-is, mass properties as stored in the entities); (2) upload the
-// entities' state and this frame's forces; (3) run the step on the GPU; (4) write the results back
-// into the Entity structs and refresh the colliders' transformed geometry.
+// entities' state only when the caller changed it since the last call wrote it back, and the
+// frame's forces only when they are not the examples' plain gravity (0, -g / inverse_mass, 0) at the
+// origin, which is kept on the device as the world's gravity instead; (3) run the step on the GPU;
+// (4) write the results back into the Entity structs and refresh the colliders' transformed geometry
+// from the device (colliders_update at the final pose, computed there in FP64).
 #include "../../include/rp_compat.h"
 #include "../../include/rp.h"
 
@@ -25,6 +28,9 @@ size_t la_len(const T* a) {   // light_array length (include/light_array.h:72)
 rp_world* g_world = nullptr;
 std::vector<double> g_signature;
 std::map<uint64_t, int32_t> g_entity_of_id;
+std::vector<double> g_written;      // the state the last call wrote back (the device still holds it)
+double g_gravity = 0.0;             // gravity the device world applies (0: forces are uploaded)
+std::vector<double> g_hull_v, g_hull_n;   // staging of rp_transformed_hulls
 
 void report(const char* what) { std::fprintf(stderr, "raw-physics GB300 drop-in: %s: %s\n", what, rp_last_error()); }
 
@@ -171,52 +177,67 @@ bool build(Entity** es, size_t n, const Constraint* cons, size_t nc) {
     return true;
 }
 
-// colliders_update (collider.cpp:409-438) at the entity's final pose
-void refresh_colliders(Entity* e) {
-    const rpc_quat& q = e->world_rotation;
-    double m[3][3];
-    m[0][0] = 1.0 - 2.0 * q.y * q.y - 2.0 * q.z * q.z;
-    m[1][0] = 2.0 * q.x * q.y + 2.0 * q.w * q.z;
-    m[2][0] = 2.0 * q.x * q.z - 2.0 * q.w * q.y;
-    m[0][1] = 2.0 * q.x * q.y - 2.0 * q.w * q.z;
-    m[1][1] = 1.0 - (2.0 * q.x * q.x) - (2.0 * q.z * q.z);
-    m[2][1] = 2.0 * q.y * q.z + 2.0 * q.w * q.x;
-    m[0][2] = 2.0 * q.x * q.z + 2.0 * q.w * q.y;
-    m[1][2] = 2.0 * q.y * q.z - 2.0 * q.w * q.x;
-    m[2][2] = 1.0 - (2.0 * q.x * q.x) - (2.0 * q.y * q.y);
-    const double t[3] = {e->world_position.x, e->world_position.y, e->world_position.z};
-    for (size_t c = 0; c < la_len(e->colliders); ++c) {
-        rpc_collider* col = &e->colliders[c];
-        if (col->type == 0) { col->sphere.center = e->world_position; continue; }
-        rpc_hull& h = col->convex_hull;
-        for (size_t i = 0; i < la_len(h.vertices); ++i) {
-            const rpc_vec3 v = h.vertices[i];
-            double o[3];
-            for (int r = 0; r < 3; ++r) o[r] = v.x * m[r][0] + v.y * m[r][1] + v.z * m[r][2] + 1.0 * t[r];
-            h.transformed_vertices[i].x = o[0];
-            h.transformed_vertices[i].y = o[1];
-            h.transformed_vertices[i].z = o[2];
-        }
-        for (size_t f = 0; f < la_len(h.faces); ++f) {
-            const rpc_vec3 nn = h.faces[f].normal;
-            double o[3];
-            for (int r = 0; r < 3; ++r) o[r] = m[r][0] * nn.x + m[r][1] * nn.y + m[r][2] * nn.z;
-            double l = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
-            if (l != 0.0) { o[0] /= l; o[1] /= l; o[2] /= l; }
-            h.transformed_faces[f].normal.x = o[0];
-            h.transformed_faces[f].normal.y = o[1];
-            h.transformed_faces[f].normal.z = o[2];
+// The caller's forces when every dynamic entity carries exactly the examples' gravity force,
+// entity_add_force(e, 0, (0, -g * 1 / inverse_mass, 0)) (src/examples/stack.cpp:93-96), for one g:
+// returns that g (bit for bit the value the device recomputes per entity), else 0.
+double plain_gravity(Entity** es, size_t n) {
+    double g = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const Entity* e = es[i];
+        if (e->fixed) continue;
+        if (la_len(e->forces) != 1) return 0.0;
+        const rpc_force& f = e->forces[0];
+        if (f.local_coords || f.position.x != 0.0 || f.position.y != 0.0 || f.position.z != 0.0 || f.force.x != 0.0 ||
+            f.force.z != 0.0 || !(e->inverse_mass > 0.0))
+            return 0.0;
+        if (g == 0.0) g = -f.force.y * e->inverse_mass;
+        if (!(g != 0.0) || -g * 1.0 / e->inverse_mass != f.force.y) return 0.0;
+    }
+    return g;
+}
+
+// colliders_update (collider.cpp:409-446) of every entity at its final pose, computed on the device
+// (rp_transformed_hulls) and copied into the caller's transformed vertices and face normals. The
+// reference itself leaves them at the last substep's predicted pose, and only for the bodies of that
+// substep's live pairs (pbd.cpp:598-599); its step recomputes them before every use, and callers run
+// colliders_update on every entity before the next call (stack.cpp:88-91), so the final pose is what a
+// caller reads. RP_SHIM_COLLIDERS=none skips the refresh (such callers recompute them anyway).
+bool refresh_colliders(Entity** es, size_t n) {
+    const char* mode = std::getenv("RP_SHIM_COLLIDERS");
+    if (mode && std::strcmp(mode, "none") == 0) return true;
+    uint64_t nv = 0, nn = 0;
+    if (rp_transformed_hulls_size(g_world, &nv, &nn) != RP_OK) return false;
+    g_hull_v.resize(3 * nv + 3);
+    g_hull_n.resize(3 * nn + 3);
+    if (rp_transformed_hulls(g_world, g_hull_v.data(), g_hull_n.data()) != RP_OK) return false;
+    size_t iv = 0, in = 0;
+    for (size_t i = 0; i < n; ++i) {
+        Entity* e = es[i];
+        for (size_t c = 0; c < la_len(e->colliders); ++c) {
+            rpc_collider* col = &e->colliders[c];
+            if (col->type == 0) { col->sphere.center = e->world_position; continue; }
+            rpc_hull& h = col->convex_hull;
+            const size_t hv = la_len(h.vertices), hf = la_len(h.faces);
+            for (size_t k = 0; k < hv; ++k, ++iv)
+                h.transformed_vertices[k] = {g_hull_v[3 * iv], g_hull_v[3 * iv + 1], g_hull_v[3 * iv + 2]};
+            for (size_t f = 0; f < hf; ++f, ++in)
+                h.transformed_faces[f].normal = {g_hull_n[3 * in], g_hull_n[3 * in + 1], g_hull_n[3 * in + 2]};
         }
     }
+    return true;
 }
 
 }  // namespace
+
+extern "C" rp_world* rp_compat_world(void) { return g_world; }
 
 extern "C" void rp_compat_reset(void) {
     if (g_world) rp_world_destroy(g_world);
     g_world = nullptr;
     g_signature.clear();
     g_entity_of_id.clear();
+    g_written.clear();
+    g_gravity = 0.0;
 }
 
 void pbd_simulate_with_constraints(double dt, Entity** entities, Constraint* cons, uint32_t num_substeps, uint32_t num_pos_iters,
@@ -228,6 +249,8 @@ void pbd_simulate_with_constraints(double dt, Entity** entities, Constraint* con
     if (!g_world || sig != g_signature) {
         if (!build(entities, n, cons, nc)) { rp_compat_reset(); return; }
         g_signature = sig;
+        g_written.clear();
+        g_gravity = 0.0;
     }
     std::vector<double> st(n * RP_STATE_DOUBLES);
     for (size_t i = 0; i < n; ++i) {
@@ -244,16 +267,25 @@ void pbd_simulate_with_constraints(double dt, Entity** entities, Constraint* con
         o[26] = e->active ? 1.0 : 0.0;
         o[27] = e->deactivation_time;
     }
-    if (rp_state_set(g_world, st.data()) != RP_OK) { report("state"); return; }
-    rp_world_set_gravity(g_world, 0.0);
-    for (size_t i = 0; i < n; ++i) {
-        const Entity* e = entities[i];
-        int32_t id = g_entity_of_id[e->id];
-        for (size_t k = 0; k < la_len(e->forces); ++k) {
-            // entity_add_force already stored world-frame values (entity.cpp:176-191)
-            double p[3] = {e->forces[k].position.x, e->forces[k].position.y, e->forces[k].position.z};
-            double f[3] = {e->forces[k].force.x, e->forces[k].force.y, e->forces[k].force.z};
-            rp_entity_add_force(g_world, id, p, f, 0);
+    // the device already holds the state this call would upload when the caller left it as written
+    if (g_written.size() != st.size() || std::memcmp(g_written.data(), st.data(), st.size() * sizeof(double)) != 0) {
+        if (rp_state_set(g_world, st.data()) != RP_OK) { report("state"); return; }
+    }
+    const double g = plain_gravity(entities, n);
+    if (g != g_gravity) {
+        rp_world_set_gravity(g_world, g);
+        g_gravity = g;
+    }
+    if (g == 0.0) {
+        for (size_t i = 0; i < n; ++i) {
+            const Entity* e = entities[i];
+            int32_t id = g_entity_of_id[e->id];
+            for (size_t k = 0; k < la_len(e->forces); ++k) {
+                // entity_add_force already stored world-frame values (entity.cpp:176-191)
+                double p[3] = {e->forces[k].position.x, e->forces[k].position.y, e->forces[k].position.z};
+                double f[3] = {e->forces[k].force.x, e->forces[k].force.y, e->forces[k].force.z};
+                rp_entity_add_force(g_world, id, p, f, 0);
+            }
         }
     }
     if (rp_simulate(g_world, dt, num_substeps, num_pos_iters, enable_collisions, 1) != RP_OK) { report("simulate"); return; }
@@ -271,8 +303,9 @@ void pbd_simulate_with_constraints(double dt, Entity** entities, Constraint* con
         e->previous_angular_velocity = {o[23], o[24], o[25]};
         e->active = o[26] != 0.0;
         e->deactivation_time = o[27];
-        refresh_colliders(e);
     }
+    g_written.swap(st);
+    if (!refresh_colliders(entities, n)) report("colliders");
 }
 
 void pbd_simulate(double dt, Entity** entities, uint32_t num_substeps, uint32_t num_pos_iters, int32_t enable_collisions) {

@@ -75,6 +75,8 @@ SIGNATURES = {
     "rp_world_set_mode": (_i, [_W, _i]),
     "rp_world_set_wait_limit": (_i, [_W, _u64]),
     "rp_world_set_sweep_order": (_i, [_W, _i]),
+    "rp_transformed_hulls_size": (_i, [_W, _P(_u64), _P(_u64)]),
+    "rp_transformed_hulls": (_i, [_W, _P(_d), _P(_d)]),
     "rp_last_schedule": (_i, [_W, _i, _i, _P(_i), _P(_i), _u, _P(_u)]),
     "rp_degenerate_info": (_i, [_W, _P(C.c_int64)]),
     "rp_adjoint_profile": (_i, [_W, _P(_d)]),
@@ -431,6 +433,15 @@ class World:
                 "pair": (int(out[2]), int(out[3])), "substep": int(out[4])}
 
     SWEEP_ORDERS = {"reference": 0, "coloured": 1}
+
+    def transformed_hulls(self):
+        """(vertices (nv, 3), normals (nf, 3)) of every hull collider at the current poses, entity by
+        entity (rp_transformed_hulls: colliders_update computed on the device in FP64)."""
+        nv, nn = _u64(), _u64()
+        self._check(self.lib.rp_transformed_hulls_size(self.h, C.byref(nv), C.byref(nn)))
+        v, n = np.zeros((max(nv.value, 1), 3)), np.zeros((max(nn.value, 1), 3))
+        self._check(self.lib.rp_transformed_hulls(self.h, _dp(v), _dp(n)))
+        return v[: nv.value], n[: nn.value]
 
     def last_schedule(self, scene: int = 0, which: int = 0):
         """(levels (n,), bodies (n, 2)) of the last substep's position (which=0) or velocity (1)

@@ -302,6 +302,51 @@ def chain_scene(links: int = 8, joint: str = "spherical", seed: int = 0, collisi
     return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=collisions, steps=300)
 
 
+def spring_scene(seed: int = 0) -> Scene:
+    """Positional and mutual-orientation constraints, as the reference's spring example builds them
+    (src/examples/spring.cpp:45-66): a unit cube (half extent 1, mass 1, friction 0.8) hung from a
+    small fixed attachment by a positional constraint with compliance 0.001 and rest offset
+    (0, -3, 0), over a floor (half extents 50 x 1 x 50 at y = -2). Beside it, seeded: a rope of four
+    cubes joined by positional constraints (compliance 0, anchors at the faces, no offset), the top one
+    to a second attachment with offset (0, -1, 0); two cubes locked together by a mutual-orientation
+    constraint (compliance 0) and a second pair with compliance 0.01, which fall onto the floor and
+    onto each other; every dynamic cube starts with a seeded rotation and velocity."""
+    rng = np.random.default_rng(seed)
+    b = _Builder("springs")
+    b.hull_body("cube", (50.0, 1.0, 50.0), (0.0, -2.0, 0.0), fixed=True, mus=0.5, mud=0.5)
+    q33 = tuple(_axis_angle((1.0, 1.0, 1.0), 33.0))
+    att = b.hull_body("cube", (0.1, 0.1, 0.1), (0.0, 6.0, 0.0), rot=q33, fixed=True, mus=0.5, mud=0.5)
+    cube = b.hull_body("cube", (1.0, 1.0, 1.0), (0.0, 2.0, 0.0), rot=q33, mass=1.0, mus=0.8, mud=0.8)
+    b.scene.constraints.append(Constraint("positional", cube, att, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.001,
+                                          distance=(0.0, -3.0, 0.0)))
+    # a rope of cubes hanging from a second attachment
+    att2 = b.hull_body("cube", (0.1, 0.1, 0.1), (5.0, 8.0, 0.0), fixed=True)
+    prev, r_prev = att2, (0.0, -0.1, 0.0)
+    for i in range(4):
+        e = b.hull_body("cube", (0.3, 0.3, 0.3), (5.0 + 0.2 * rng.standard_normal(), 7.4 - 0.8 * i, 0.0),
+                        rot=tuple(random_quaternions(rng, 1)[0]), mass=0.5, v=tuple(rng.normal(0.0, 0.5, 3)))
+        dist = (0.0, -1.0, 0.0) if i == 0 else (0.0, 0.0, 0.0)
+        b.scene.constraints.append(Constraint("positional", e, prev, (0.0, 0.3, 0.0), r_prev, 0.0, distance=dist))
+        prev, r_prev = e, (0.0, -0.3, 0.0)
+    # locked pairs falling onto the floor and onto each other
+    for k, comp in enumerate((0.0, 0.01)):
+        x = -5.0 - 3.0 * k
+        e1 = b.hull_body("cube", (0.5, 0.5, 0.5), (x, 1.0 + k, 0.0), rot=tuple(random_quaternions(rng, 1)[0]),
+                         mass=1.0, v=tuple(rng.normal(0.0, 1.0, 3)), w=tuple(rng.normal(0.0, 1.0, 3)))
+        e2 = b.hull_body("cube", (0.4, 0.4, 0.4), (x + 0.3, 2.4 + k, 0.2), rot=tuple(random_quaternions(rng, 1)[0]),
+                         mass=2.0, v=tuple(rng.normal(0.0, 1.0, 3)))
+        b.scene.constraints.append(Constraint("mutual_orientation", e1, e2, compliance=comp))
+    return b.finish(dt=1.0 / 60.0, substeps=20, pos_iters=1, collisions=True, steps=300)
+
+
+def _axis_angle(axis, degrees) -> np.ndarray:
+    """quaternion_new (src/quaternion.cpp): rotation of `degrees` about the normalised axis, (x, y, z, w)."""
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    h = math.radians(degrees) / 2.0
+    return np.concatenate([a * math.sin(h), [math.cos(h)]])
+
+
 def _rot_matrix(q) -> np.ndarray:
     x, y, z, w = q
     return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],

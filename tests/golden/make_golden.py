@@ -42,6 +42,7 @@ SCENES = {
     "spheres6": (lambda: S.sphere_scene(6, seed=0), [0, 1, 10, 40, 60], 40),
     "tower12": (lambda: S.tower_scene(12, ratio=100.0, seed=0), [0, 1, 5, 20, 60], 20),
     "large1024": (lambda: S.large_scene(1024, seed=0), [0, 1], 0),
+    "springs": (lambda: S.spring_scene(seed=0), [0, 1, 10, 40, 100, 200], 40),
 }
 
 

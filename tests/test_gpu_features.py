@@ -156,150 +156,130 @@ def test_deep_overlap_and_status(ext_built):
 
 
 # ---------------------------------------------------------------------------------------------
-# The pbd_simulate drop-in, driven through the reference's own data layout
+# The pbd_simulate drop-in, driven through the reference's own data layout (rawphys.compat)
 
-class Vec3(C.Structure):
-    _pack_ = 1
-    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+def oracle_callers(o, scene):
+    """The scene as a reference caller holds it, with hull topology and mass properties taken from
+    the oracle (the reference's own set-up, independent of this library's)."""
+    from rawphys import compat
+    topo = lambda b, k: o.hull_topology(b, k)
 
-
-class Quat(C.Structure):
-    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("w", C.c_double)]
-
-
-class Mat3(C.Structure):
-    _pack_ = 1
-    _fields_ = [("data", C.c_double * 9)]
+    def mass(b):
+        I, Ii = o.inertia(b)
+        return o.inverse_mass(b), I, Ii, o.radius(b)
+    return compat.build_callers(scene, topology=topo, mass_properties=mass)
 
 
-class Force(C.Structure):
-    _fields_ = [("position", Vec3), ("force", Vec3), ("local_coords", C.c_int32)]
+def _rot(q):
+    x, y, z, w_ = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w_ * z), 2 * (x * z + w_ * y)],
+                     [2 * (x * y + w_ * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w_ * x)],
+                     [2 * (x * z - w_ * y), 2 * (y * z + w_ * x), 1 - 2 * (x * x + y * y)]])
 
 
-class HullFace(C.Structure):
-    _fields_ = [("elements", C.c_void_p), ("normal", Vec3)]
-
-
-class Hull(C.Structure):
-    _fields_ = [("vertices", C.c_void_p), ("transformed_vertices", C.c_void_p), ("faces", C.c_void_p),
-                ("transformed_faces", C.c_void_p), ("vertex_to_faces", C.c_void_p), ("vertex_to_neighbors", C.c_void_p),
-                ("face_to_neighbors", C.c_void_p)]
-
-
-class Collider(C.Structure):
-    _fields_ = [("type", C.c_int32), ("convex_hull", Hull)]
-
-
-class Entity(C.Structure):
-    _fields_ = [("id", C.c_uint64), ("mesh", C.c_uint32 * 4), ("world_position", Vec3), ("world_rotation", Quat),
-                ("world_scale", Vec3), ("color", C.c_double * 4), ("colliders", C.c_void_p),
-                ("bounding_sphere_radius", C.c_double), ("forces", C.c_void_p), ("inverse_mass", C.c_double),
-                ("inertia_tensor", Mat3), ("inverse_inertia_tensor", Mat3), ("angular_velocity", Vec3),
-                ("linear_velocity", Vec3), ("fixed", C.c_int32), ("active", C.c_int32), ("deactivation_time", C.c_double),
-                ("static_friction_coefficient", C.c_double), ("dynamic_friction_coefficient", C.c_double),
-                ("restitution_coefficient", C.c_double), ("previous_world_position", Vec3), ("previous_world_rotation", Quat),
-                ("previous_linear_velocity", Vec3), ("previous_angular_velocity", Vec3)]
-
-
-class LightArrays:
-    """Builds include/light_array.h arrays: {size_t capacity, size_t length} then the elements."""
-
-    def __init__(self):
-        self.keep = []
-
-    def make(self, ctype, values):
-        n = len(values)
-        buf = (C.c_ubyte * (16 + C.sizeof(ctype) * max(n, 1)))()
-        self.keep.append(buf)
-        hdr = (C.c_size_t * 2).from_buffer(buf)
-        hdr[0] = max(n, 1)
-        hdr[1] = n
-        arr = (ctype * max(n, 1)).from_buffer(buf, 16)
-        for i, v in enumerate(values):
-            arr[i] = v
-        return C.addressof(buf) + 16
-
-    def malloc_ptrs(self, ptrs):
-        a = (C.c_void_p * max(len(ptrs), 1))(*ptrs)
-        self.keep.append(a)
-        return C.addressof(a)
-
-
-def build_entities(o, scene, la):
-    ents = []
-    st = o.get_state()
-    for e in range(scene.num_bodies):
-        verts, normals, tables = o.hull_topology(e)
-        vtx = [Vec3(*v) for v in verts]
-        faces = []
-        fs, fd = tables[0]
-        for f in range(len(normals)):
-            faces.append(HullFace(la.make(C.c_uint32, list(fd[fs[f]:fs[f + 1]])), Vec3(*normals[f])))
-        rows = lambda t: la.malloc_ptrs([la.make(C.c_uint32, list(t[1][t[0][r]:t[0][r + 1]])) for r in range(len(t[0]) - 1)])
-        hull = Hull(la.make(Vec3, vtx), la.make(Vec3, vtx), la.make(HullFace, faces), la.make(HullFace, faces),
-                    rows(tables[1]), rows(tables[2]), rows(tables[3]))
-        col = la.make(Collider, [Collider(1, hull)])
-        I, Ii = o.inertia(e)
-        ent = Entity()
-        ent.id = 1000 + e
-        ent.world_position = Vec3(*st[e, 0:3])
-        ent.world_rotation = Quat(*st[e, 3:7])
-        ent.colliders = col
-        ent.bounding_sphere_radius = o.radius(e)
-        invm = o.inverse_mass(e)
-        ent.inverse_mass = invm
-        ent.inertia_tensor = Mat3((C.c_double * 9)(*I.reshape(9)))
-        ent.inverse_inertia_tensor = Mat3((C.c_double * 9)(*Ii.reshape(9)))
-        ent.linear_velocity = Vec3(*st[e, 7:10])
-        ent.angular_velocity = Vec3(*st[e, 10:13])
-        ent.fixed = int(scene.fixed[e])
-        ent.active = 1
-        ent.static_friction_coefficient = scene.mus[e]
-        ent.dynamic_friction_coefficient = scene.mud[e]
-        ent.restitution_coefficient = scene.rest[e]
-        g = 10.0
-        ent.forces = la.make(Force, [Force(Vec3(0, 0, 0), Vec3(0.0, -g * 1.0 / invm if invm else -np.inf, 0.0), 0)])
-        ents.append(ent)
-    arr = la.make(C.POINTER(Entity), [C.pointer(x) for x in ents])
-    return ents, arr
+def _check_transformed(ents):
+    """Every hull's transformed vertices and normals follow the entity's final pose."""
+    from rawphys import compat
+    for ent in ents:
+        col = compat.Collider.from_address(ent.colliders)
+        if col.type != 1:
+            continue
+        h = col.convex_hull
+        nv = C.c_size_t.from_address(h.vertices - 8).value
+        v = (compat.Vec3 * nv).from_address(h.vertices)
+        tv = (compat.Vec3 * nv).from_address(h.transformed_vertices)
+        R = _rot([ent.world_rotation.x, ent.world_rotation.y, ent.world_rotation.z, ent.world_rotation.w])
+        p = np.array([ent.world_position.x, ent.world_position.y, ent.world_position.z])
+        for i in range(nv):
+            assert np.allclose([tv[i].x, tv[i].y, tv[i].z], R @ np.array([v[i].x, v[i].y, v[i].z]) + p, atol=1e-12)
+        nf = C.c_size_t.from_address(h.faces - 8).value
+        fs = (compat.HullFace * nf).from_address(h.faces)
+        tf = (compat.HullFace * nf).from_address(h.transformed_faces)
+        for f in range(nf):
+            n = R @ np.array([fs[f].normal.x, fs[f].normal.y, fs[f].normal.z])
+            assert np.allclose([tf[f].normal.x, tf[f].normal.y, tf[f].normal.z], n / np.linalg.norm(n), atol=1e-12)
 
 
 def test_pbd_simulate_dropin(ext_built, oracle_built, monkeypatch):
     """A caller holding the reference's Entity / Collider / Physics_Force structs calls the mangled
-    pbd_simulate; with the FP64 kernels the result equals the oracle bit for bit."""
-    from rawphys import scenes as S
+    pbd_simulate, adding gravity before each frame and clearing it after, as the examples do; with
+    the FP64 kernels the result equals the oracle bit for bit, the transformed hulls follow the final
+    poses, and steady frames upload nothing (state unchanged, gravity kept on the device)."""
+    from rawphys import compat, scenes as S
     monkeypatch.setenv("RP_SHIM_PRECISION", "fp64")
     lib = C.CDLL(ext_built.LIB_PATH)
     lib.rp_compat_reset()
-    f = getattr(lib, "_Z12pbd_simulatedPP6Entityjji")
-    f.argtypes = [C.c_double, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int32]
-    f.restype = None
+    lib.rp_compat_world.restype = C.c_void_p
+    sim, _ = compat.dropin(lib)
     sc = S.stack_scene(5, seed=2)
     o = oracle_built("port").load(sc)
-    la = LightArrays()
-    ents, arr = build_entities(o, sc, la)
-    for frame in range(3):
-        f(sc.dt, arr, 20, 1, 1)
+    callers = oracle_callers(o, sc)
+    h2d = []
+    for frame in range(4):
+        callers.add_gravity(sc.gravity)
+        sim(sc.dt, callers.array, 20, 1, 1)
+        callers.clear_forces()
         o.step(1)
-        ref = o.get_state()
-        for e, ent in enumerate(ents):
-            got = [ent.world_position.x, ent.world_position.y, ent.world_position.z,
-                   ent.world_rotation.x, ent.world_rotation.y, ent.world_rotation.z, ent.world_rotation.w,
-                   ent.linear_velocity.x, ent.linear_velocity.y, ent.linear_velocity.z]
-            assert np.array_equal(np.array(got), ref[e, 0:10]), (frame, e)
-    # transformed collider vertices follow the final pose
-    ent = ents[1]
-    hull = Collider.from_address(ent.colliders).convex_hull
-    tv = (Vec3 * 8).from_address(hull.transformed_vertices)
-    v = (Vec3 * 8).from_address(hull.vertices)
-    q = np.array([ent.world_rotation.x, ent.world_rotation.y, ent.world_rotation.z, ent.world_rotation.w])
-    x, y, z, w_ = q
-    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w_ * z), 2 * (x * z + w_ * y)],
-                  [2 * (x * y + w_ * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w_ * x)],
-                  [2 * (x * z - w_ * y), 2 * (y * z + w_ * x), 1 - 2 * (x * x + y * y)]])
-    p = np.array([ent.world_position.x, ent.world_position.y, ent.world_position.z])
-    for i in range(8):
-        assert np.allclose([tv[i].x, tv[i].y, tv[i].z], R @ np.array([v[i].x, v[i].y, v[i].z]) + p, atol=1e-12)
+        assert np.array_equal(callers.state(), o.get_state()), frame
+        tb = (C.c_uint64 * 2)()
+        assert ext_built.load_library().rp_transfer_bytes(C.c_void_p(lib.rp_compat_world()), tb) == 0
+        h2d.append(tb[0])
+    assert h2d[3] == h2d[1], "steady frames must upload nothing: %s" % h2d
+    _check_transformed(callers.entities)
+    lib.rp_compat_reset()
+
+
+@pytest.mark.parametrize("name", ["springs", "chain8_hinge", "chain8_spherical"])
+def test_pbd_simulate_with_constraints_dropin(ext_built, oracle_built, monkeypatch, name):
+    """The mangled pbd_simulate_with_constraints over the reference's Constraint light array
+    (positional with rest offsets, mutual orientation, hinge and spherical joints with limits): FP64
+    bit-exact to the oracle over several frames, and the caller's constraints are never written."""
+    from rawphys import compat
+    from make_golden import SCENES
+    monkeypatch.setenv("RP_SHIM_PRECISION", "fp64")
+    lib = C.CDLL(ext_built.LIB_PATH)
+    lib.rp_compat_reset()
+    _, simc = compat.dropin(lib)
+    sc = SCENES[name][0]()
+    o = oracle_built("port").load(sc)
+    callers = oracle_callers(o, sc)
+    nc = len(sc.constraints)
+    before = bytes((C.c_ubyte * (144 * nc)).from_address(callers.constraints))
+    for frame in range(6):
+        callers.add_gravity(sc.gravity)
+        simc(sc.dt, callers.array, callers.constraints, sc.substeps, 1, int(sc.collisions))
+        callers.clear_forces()
+        o.step(1)
+        assert np.array_equal(callers.state(), o.get_state()), (name, frame)
+    assert bytes((C.c_ubyte * (144 * nc)).from_address(callers.constraints)) == before
+    lib.rp_compat_reset()
+
+
+def test_pbd_simulate_dropin_fp32_default(ext_built, oracle_built, monkeypatch):
+    """The drop-in in its default FP32 mode: per-frame position error from identical states against
+    the oracle within 1e-4 m at the median on a pile and the spring scene, transformed hulls exact at
+    the final pose (computed on the device in FP64 in either mode)."""
+    from rawphys import compat, scenes as S
+    from rawphys.precision import step_error
+    from make_golden import SCENES
+    monkeypatch.delenv("RP_SHIM_PRECISION", raising=False)
+    lib = C.CDLL(ext_built.LIB_PATH)
+    _, simc = compat.dropin(lib)
+    for sc in (S.random_pile_scene(12, seed=1), SCENES["springs"][0]()):
+        lib.rp_compat_reset()
+        o = oracle_built("port").load(sc)
+        callers = oracle_callers(o, sc)
+        o.step(30)
+        for frame in range(3):
+            st = o.get_state()
+            callers.set_state(st)
+            callers.add_gravity(sc.gravity)
+            simc(sc.dt, callers.array, callers.constraints or None, sc.substeps, 1, 1)
+            callers.clear_forces()
+            o.step(1)
+            err = step_error(callers.state(), o.get_state(), ~sc.fixed)
+            assert err["pos_m"]["median"] <= 1e-4, (sc.name, frame, err)
+        _check_transformed(callers.entities)
     lib.rp_compat_reset()
 
 

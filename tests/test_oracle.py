@@ -107,7 +107,7 @@ def test_port_matches_reference_live(oracle_built):
     from oracle.oracle import reference_available
     if not reference_available():
         pytest.skip("reference build not present (only where the reference checkout exists)")
-    for name in ("stack10", "chain8_hinge", "spheres6"):
+    for name in ("stack10", "chain8_hinge", "spheres6", "springs"):
         scene = SCENES[name][0]()
         a = oracle_built("port").load(scene)
         a.step(40)
