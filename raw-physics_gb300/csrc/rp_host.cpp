@@ -155,7 +155,7 @@ struct rp_world {
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
     HostBuf h_state;                               // pinned staging of the body state (rp_state_set / _get)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
-    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue;
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
@@ -493,6 +493,8 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(w->d_hit_list.ensure(std::max<size_t>(P, 1) * 4));
         RP_CUDA(w->d_work_simplex.ensure(std::max<size_t>(P, 1) * 16 * R));
         RP_CUDA(w->d_work_epa.ensure(std::max<size_t>(P, 1) * 4 * 8));
+        RP_CUDA(w->d_work_off.ensure(std::max<size_t>(P, 1) * 16));
+        RP_CUDA(w->d_work_face.ensure(std::max<size_t>(P, 1) * 12 * 4));
         std::vector<int32_t> order((size_t)S);
         for (int sc = 0; sc < S; ++sc) order[(size_t)sc] = sc;
         // largest estimated sweep cost first: bodies, plus joints weighted for their serial chains
@@ -634,6 +636,8 @@ WorldView<R> make_view(rp_world* w) {
     V.hit_list = w->d_hit_list.as<int32_t>();
     V.work_simplex = w->d_work_simplex.as<R>();
     V.work_epa = w->d_work_epa.as<double>();
+    V.work_off = w->d_work_off.as<float4>();
+    V.work_face = w->d_work_face.as<float>();
     V.queue = w->d_queue.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
     V.solo_nodes = w->solo_nodes;

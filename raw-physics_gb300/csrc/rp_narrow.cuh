@@ -105,7 +105,7 @@ struct ColView {
     const V3<R>* norms;      // transformed face normals (global)
     int nv, nf;
     const Shape* shape;
-    Qt<double> q64;          // the body's orientation (FP64), for decisions made in FP64
+    int body;                // the body's slot (its FP64 orientation is read only for decisions made in FP64)
 };
 
 // A face normal of a hull rotated by the body's FP64 orientation (collider_update's normal
@@ -113,7 +113,8 @@ struct ColView {
 template <typename R>
 __device__ __forceinline__ V3<double> face_normal64(const WorldView<R>& W, const ColView<R>& c, int f) {
     const double* n = W.face_normal + 3 * (c.shape->face_off + f);
-    return vnorm_fast(mmulv(qmat3(c.q64), v3<double>(n[0], n[1], n[2])));
+    const double4_32a q = W.rot[c.body];
+    return vnorm_fast(mmulv(qmat3(qt<double>(q.x, q.y, q.z, q.w)), v3<double>(n[0], n[1], n[2])));
 }
 
 template <typename R>
@@ -575,9 +576,13 @@ __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, u
     d_out = d;
 }
 
+// face_out (optional): when FP32 decides the termination, lane 0 writes the final face's three
+// points and its FP32 normal there (12 floats) and *deferred is set, leaving the FP64 normal and depth
+// to a thread-per-pair kernel (k_epa_finish) instead of the warp; otherwise they are computed here.
 template <typename R>
 __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView<R>& c2, const Simplex<R>& s,
-                         V3<double>& out_n, double& out_pen, int& iters, long long* support_cycles = nullptr) {
+                         V3<double>& out_n, double& out_pen, int& iters, long long* support_cycles = nullptr,
+                         float* face_out = nullptr, bool* deferred = nullptr) {
     static_assert(sizeof(EpaFastSmem<R>) <= sizeof(typename NarrowSmem<R>::U), "EPA scratch must fit the union");
     EpaFastSmem<R>& sm = *reinterpret_cast<EpaFastSmem<R>*>(&smr.u);
     const unsigned lane = lane_id();
@@ -624,6 +629,18 @@ __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView
             const float err = 1e-6f * (1.f + cond) * (vlen(sp) + vlen(a) + 1e-3f) + 1e-7f;
             if (cond < 1e6f && gap < 0.0001f - err) { done = true; need64 = false; }
             else if (cond < 1e6f && gap > 0.0001f + err) { need64 = false; }
+        }
+        if (done && !need64 && face_out) {
+            if (lane == 0) {
+                const uchar4 f = sm.f[mi];
+                const V3<float> pa = sm.poly[f.x], pb = sm.poly[f.y], pc = sm.poly[f.z];
+                const float v[12] = {pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, pc.x, pc.y, pc.z, min_n.x, min_n.y, min_n.z};
+                for (int i = 0; i < 12; ++i) face_out[i] = v[i];
+                if (st) atomicOr(&smr.status, st);
+            }
+            *deferred = true;
+            __syncwarp();
+            return true;
         }
         V3<double> n64 = v3<double>(0, 0, 0);
         double d64 = 0.0;
@@ -747,6 +764,15 @@ __device__ bool epa_fast(NarrowSmem<R>& smr, const ColView<R>& c1, const ColView
     return false;
 }
 
+// The FP64 normal and depth of EPA's final face from its three points and FP32 normal (epa.cpp:32-77
+// on the face EPA stopped at), as epa_fast computes them in the warp: one thread per pair.
+__device__ __forceinline__ void epa_face_finish(const float* f, V3<double>& n64, double& d64) {
+    const V3<double> a = v3<double>(f[0], f[1], f[2]), b = v3<double>(f[3], f[4], f[5]), c = v3<double>(f[6], f[7], f[8]);
+    n64 = vnorm_fast(vcross(vsub(b, a), vsub(c, a)));
+    if (vdot(n64, v3<double>(f[9], f[10], f[11])) < 0.0) n64 = vinv(n64);
+    d64 = vdot(n64, a);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Clipping (clipping.cpp)
 template <typename R>
@@ -759,7 +785,9 @@ template <typename R>
 __device__ __forceinline__ bool plane_edge(V3<R> pn, V3<R> pp, V3<R> start, V3<R> end, V3<R>& out) {
     V3<R> ab = vsub(end, start);
     float ab_p = vdot(pn, ab);
-    if ((double)fabsf(ab_p) > 0.000001) {
+    // (double)|ab_p| > 0.000001 (clipping.cpp:30): 1e-6f is the largest float below 1e-6 and no float
+    // lies between them, so the FP32 comparison decides exactly the same
+    if (fabsf(ab_p) > 1e-6f) {
         float distance = -vdot(pn, pp);
         V3<R> p_co = vscale((R)(-distance), pn);
         float fac = -vdot(pn, vsub(start, p_co)) / (R)ab_p;
@@ -923,7 +951,8 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         return;
     }
     bool ref1 = d1 > d2;
-    if (!EXACT && fabs((double)d1 - (double)d2) < 1e-5) {
+    // screen in FP32: |d1 - d2| below 1e-5 (within the float subtraction's rounding: 1.1e-5 covers it)
+    if (!EXACT && fabsf((float)d1 - (float)d2) < 1.1e-5f) {
         // The reference face is the better-aligned of the two candidates (clipping.cpp:284). For
         // nearly parallel faces d1 and d2 differ by ~1e-11, below FP32 resolution; decide it from
         // FP64 normals so the FP32 build picks the reference's face (and so its contact order).

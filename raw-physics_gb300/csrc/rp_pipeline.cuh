@@ -53,26 +53,32 @@ struct WarpTally {
 };
 
 // Views of a pair of single-hull bodies in the pair frame of pair_contacts (FP32 build: body a's
-// origin; exact build: world coordinates), staging both hulls' vertices in shared memory.
+// origin; exact build: world coordinates), staging both hulls' vertices in shared memory. The FP32
+// build reads the pair's FP32 offset (work_off, rounded from the FP64 poses by k_cull) and the FP32
+// orientations of the predict phase (pose_f), which equal the casts of the FP64 values: no FP64
+// arithmetic or conversion runs in the warp.
 template <typename R, bool EXACT>
-__device__ void single_views(const WorldView<R>& W, V3<R>* stage_a, V3<R>* stage_b, int a, int b, ColView<R>& va,
+__device__ void single_views(const WorldView<R>& W, V3<R>* stage_a, V3<R>* stage_b, int a, int b, int k, ColView<R>& va,
                              ColView<R>& vb, PairFrame<R, EXACT>& fr) {
-    double4_32a pa = W.pos[a], pb = W.pos[b], qa4 = W.rot[a], qb4 = W.rot[b];
     fr.raw = false;
     V3<R> offa = v3<R>(0, 0, 0), offb;
-    if (EXACT) {
+    if constexpr (EXACT) {
+        double4_32a pa = W.pos[a], pb = W.pos[b], qa4 = W.rot[a], qb4 = W.rot[b];
         offb = v3<R>(0, 0, 0);
         fr.x1 = v3<R>((R)pa.x, (R)pa.y, (R)pa.z);
         fr.x2 = v3<R>((R)pb.x, (R)pb.y, (R)pb.z);
+        fr.q1inv = qinverse(qt<R>((R)qa4.x, (R)qa4.y, (R)qa4.z, (R)qa4.w));
+        fr.q2inv = qinverse(qt<R>((R)qb4.x, (R)qb4.y, (R)qb4.z, (R)qb4.w));
     } else {
-        offb = v3<R>((R)(pb.x - pa.x), (R)(pb.y - pa.y), (R)(pb.z - pa.z));
+        const float4 o = W.work_off[k], qa = W.pose_f[2 * a + 1], qb = W.pose_f[2 * b + 1];
+        offb = v3<R>(o.x, o.y, o.z);
         fr.x1 = offa;
         fr.x2 = offb;
+        fr.q1inv = qinverse(qt<R>(qa.x, qa.y, qa.z, qa.w));
+        fr.q2inv = qinverse(qt<R>(qb.x, qb.y, qb.z, qb.w));
     }
-    fr.q1inv = qinverse(qt<R>((R)qa4.x, (R)qa4.y, (R)qa4.z, (R)qa4.w));
-    fr.q2inv = qinverse(qt<R>((R)qb4.x, (R)qb4.y, (R)qb4.z, (R)qb4.w));
-    va = make_view<R, EXACT>(W, W.col_start[a], EXACT ? fr.x1 : offa, offa, stage_a, qt<double>(qa4.x, qa4.y, qa4.z, qa4.w));
-    vb = make_view<R, EXACT>(W, W.col_start[b], EXACT ? fr.x2 : offb, offb, stage_b, qt<double>(qb4.x, qb4.y, qb4.z, qb4.w));
+    va = make_view<R, EXACT>(W, W.col_start[a], EXACT ? fr.x1 : offa, offa, stage_a, a);
+    vb = make_view<R, EXACT>(W, W.col_start[b], EXACT ? fr.x2 : offb, offb, stage_b, b);
 }
 
 // True when both bodies have exactly one collider, a hull whose vertices fit the staging area.
@@ -201,7 +207,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int nc
         if (col.type != COL_HULL) continue;
         const int b = W.col_body[ci];
         if (W.fixed[b] && !include_fixed) continue;
-        transform_collider<R, EXACT>(W, col, b, sub, group);
+        transform_collider<R, EXACT, !EXACT>(W, col, b, sub, group);
     }
 }
 
@@ -249,6 +255,11 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
                 else if (bounds_apart_f(W, a, b)) ++apart;
                 else gjk = true;
             }
+            if (gjk && !std::is_same<R, double>::value) {
+                // the pair frame's offset for the warp kernels: one FP64 difference per pair here
+                const double4_32a pa = W.pos[a], pb = W.pos[b];
+                W.work_off[k] = make_float4((float)(pb.x - pa.x), (float)(pb.y - pa.y), (float)(pb.z - pa.z), 0.f);
+            }
             W.work_state[k] = state;
             if (state == WS_NONE && !gjk) { W.pair_ccount[gp] = 0; W.pair_cstart[gp] = 0; }
         }
@@ -278,7 +289,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 3) k_gjk(WorldView<R> W) {
         const int a = pr.x, b = pr.y;
         ColView<R> va, vb;
         PairFrame<R, EXACT> fr;
-        single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+        single_views<R, EXACT>(W, sm.va, sm.vb, a, b, k, va, vb, fr);
         Simplex<R> sx;
         int gi = 0;
         long long tsup = 0;
@@ -343,7 +354,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             const long long tv = clock64();
             ColView<R> va, vb;
             PairFrame<R, EXACT> fr;
-            single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+            single_views<R, EXACT>(W, sm.va, sm.vb, a, b, k, va, vb, fr);
             const R* in = W.work_simplex + 16 * (size_t)k;
             Simplex<R> sx;
             sx.a = v3<R>(in[0], in[1], in[2]);
@@ -356,8 +367,10 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             int ei = 0;
             const long long t0 = clock64();
             long long tsup = 0;
+            bool deferred = false;
             const bool ok = (EXACT || !kEpaFast) ? epa(sm, va, vb, sx, nrm, pen, ei)
-                                                 : epa_fast(sm, va, vb, sx, nrm, pen, ei, &tsup);
+                                                 : epa_fast(sm, va, vb, sx, nrm, pen, ei, &tsup,
+                                                            W.work_face + 12 * (size_t)k, &deferred);
             t.v[0] += ei;
             t.v[1] += 1;
             t.v[2] += clock64() - t0;
@@ -371,9 +384,15 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
                     atomicOr(&W.status[s], (uint32_t)sm.status);
                     note_degenerate(W, (uint32_t)sm.status, s, a, b);
                 }
-                if (ok) {
+                if (ok && deferred) {
+                    W.work_state[k] = WS_EPA_FACE;
+                } else if (ok) {
                     double* o = W.work_epa + 4 * (size_t)k;
                     o[0] = nrm.x; o[1] = nrm.y; o[2] = nrm.z; o[3] = pen;
+                    if (!EXACT) {
+                        float* fo = W.work_face + 12 * (size_t)k;
+                        fo[0] = (float)nrm.x; fo[1] = (float)nrm.y; fo[2] = (float)nrm.z; fo[3] = (float)pen;
+                    }
                     W.work_state[k] = WS_EPA_OK;
                 } else {
                     W.work_state[k] = WS_NONE;
@@ -386,6 +405,27 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
     }
     const int slots[8] = {1, 2, 13, 7, 17, 18, -1, -1};
     t.flush(W.counters, slots);
+}
+
+// Thread per hit: the FP64 normal and depth of every EPA whose termination FP32 decided (WS_EPA_FACE),
+// 32 pairs per warp instruction instead of one pair's arithmetic repeated by all 32 lanes; the FP32
+// copies the manifold kernel works with are stored beside them.
+template <typename R>
+__global__ void __launch_bounds__(PIPE_BLOCK) k_epa_finish(WorldView<R> W) {
+    if (frame_abandoned(W.status)) return;
+    const int n = W.queue[3];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int k = W.hit_list[j];
+        if (W.work_state[k] != WS_EPA_FACE) continue;
+        float* f = W.work_face + 12 * (size_t)k;
+        V3<double> n64;
+        double d64;
+        epa_face_finish(f, n64, d64);
+        double* o = W.work_epa + 4 * (size_t)k;
+        o[0] = n64.x; o[1] = n64.y; o[2] = n64.z; o[3] = d64;
+        f[0] = (float)n64.x; f[1] = (float)n64.y; f[2] = (float)n64.z; f[3] = (float)d64;
+        W.work_state[k] = WS_EPA_OK;
+    }
 }
 
 template <typename R, bool EXACT>
@@ -415,11 +455,17 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
                 __syncwarp();
                 ColView<R> va, vb;
                 PairFrame<R, EXACT> fr;
-                single_views<R, EXACT>(W, sm.va, sm.vb, a, b, va, vb, fr);
+                single_views<R, EXACT>(W, sm.va, sm.vb, a, b, k, va, vb, fr);
                 const double* e = W.work_epa + 4 * (size_t)k;
                 const V3<double> n64 = v3<double>(e[0], e[1], e[2]);
                 t1 = clock64();
-                contact_manifold<R, EXACT>(sm, W, va, vb, v3cast<R>(n64), n64, (R)e[3], fr);
+                if constexpr (EXACT) {
+                    contact_manifold<R, EXACT>(sm, W, va, vb, v3cast<R>(n64), n64, (R)e[3], fr);
+                } else {
+                    // the FP32 normal and depth stored beside the FP64 ones (no conversion in the warp)
+                    const float* f = W.work_face + 12 * (size_t)k;
+                    contact_manifold<R, EXACT>(sm, W, va, vb, v3<R>(f[0], f[1], f[2]), n64, (R)f[3], fr);
+                }
             }
             const long long t2 = clock64();
             t.v[1] += t2 - t0;
@@ -572,7 +618,12 @@ struct PipeLauncher {
                 k_gjk<R, EXACT><<<c.gjk_blocks, PIPE_BLOCK, gjk_smem(), st>>>(W);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_GJK)) != cudaSuccess) return e;
                 k_epa<R, EXACT><<<c.epa_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
-                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_EPA)) != cudaSuccess) return e;
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if (!EXACT) {
+                    k_epa_finish<R><<<c.cull_blocks, PIPE_BLOCK, 0, st>>>(W);
+                    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                }
+                if ((e = mark(PH_EPA)) != cudaSuccess) return e;
                 k_manifold<R, EXACT><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_MANIFOLD)) != cudaSuccess) return e;
             }
@@ -595,7 +646,7 @@ struct PipeLauncher {
     }
 
     static int launches_per_frame(const StepParams& P) {
-        const int per_sub = 2 + (P.enable_collisions ? 5 : 1) + P.num_pos_iters + 1;
+        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 5 : 6) : 1) + P.num_pos_iters + 1;
         return 1 + P.num_substeps * per_sub;
     }
 };

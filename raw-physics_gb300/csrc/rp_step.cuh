@@ -869,13 +869,15 @@ __device__ void resched(const WorldView<R>& W, const G& g, int s) {
 // ---------------------------------------------------------------------------------------------
 // Hull transform (colliders_update, collider.cpp:409-446): one collider of body b by `nsub` threads
 // (index `lane` among them)
-template <typename R, bool EXACT>
+// POSE_F: take the FP32 build's orientation from the predict phase's FP32 copy (pose_f, the same
+// rounding of the FP64 quaternion) instead of converting it again in every lane.
+template <typename R, bool EXACT, bool POSE_F = false>
 __device__ void transform_collider(const WorldView<R>& W, const Collider& col, int b, int lane, int nsub = 32) {
     const Shape sh = W.shapes[col.shape];
-    double4_32a p4 = W.pos[b], q4 = W.rot[b];
     V3<R>* tv = (V3<R>*)(W.tverts) + col.tv_off;
     V3<R>* tn = (V3<R>*)(W.tnorms) + col.tn_off;
     if (EXACT) {
+        const double4_32a p4 = W.pos[b], q4 = W.rot[b];
         M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
         for (int i = lane; i < sh.nv; i += nsub) {
             const double* v = W.shape_verts + 3 * (sh.vert_off + i);
@@ -886,7 +888,15 @@ __device__ void transform_collider(const WorldView<R>& W, const Collider& col, i
             tn[i] = v3cast<R>(vnorm(m4_dir(M, v3<double>(nrm[0], nrm[1], nrm[2]))));
         }
     } else {
-        M3<R> Rm = qmat3(qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w));
+        Qt<R> q;
+        if (POSE_F) {
+            const float4 f = W.pose_f[2 * b + 1];
+            q = qt<R>(f.x, f.y, f.z, f.w);
+        } else {
+            const double4_32a q4 = W.rot[b];
+            q = qt<R>((R)q4.x, (R)q4.y, (R)q4.z, (R)q4.w);
+        }
+        M3<R> Rm = qmat3(q);
         for (int i = lane; i < sh.nv; i += nsub) {
             const float* v = W.shape_verts_f + 3 * (sh.vert_off + i);
             tv[i] = mmulv(Rm, v3<R>((R)v[0], (R)v[1], (R)v[2]));
@@ -917,9 +927,9 @@ __device__ void transform_hulls(const WorldView<R>& W, const G& g, int s, bool i
 // ---------------------------------------------------------------------------------------------
 // Narrowphase: one warp per broad-phase pair
 template <typename R, bool EXACT>
-__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged, Qt<double> q64) {
+__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged, int body) {
     ColView<R> v;
-    v.q64 = q64;
+    v.body = body;
     const Collider col = W.colliders[ci];
     v.type = col.type;
     v.radius = (R)col.radius;
@@ -973,9 +983,9 @@ __device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, i
     for (int ca = ca0; ca < ca1; ++ca) {
         // exact build: stored vertices are world coordinates, sphere centres the body positions;
         // FP32 build: stored vertices are rotated about the body origin, the frame origin is body a
-        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va, qt<double>(qa4.x, qa4.y, qa4.z, qa4.w));
+        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va, a);
         for (int cb = cb0; cb < cb1; ++cb) {
-            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb, qt<double>(qb4.x, qb4.y, qb4.z, qb4.w));
+            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb, b);
             collider_contacts<R, EXACT>(sm, W, va, vb, fr, W.counters);
             __syncwarp();
         }

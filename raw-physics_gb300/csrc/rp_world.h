@@ -60,7 +60,7 @@ struct Shape {               // one convex hull's topology (collider_convex_hull
 };
 
 // Per-pair state between the narrowphase kernels of the phase-major pipeline
-enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3 };
+enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3, WS_EPA_FACE = 4 };
 
 // Phases of the step timed per frame (rp_phase_times). The persistent kernel times the whole
 // narrowphase as PH_NARROW; the phase-major form splits it into the cull (PH_NARROW), GJK, EPA and
@@ -183,6 +183,10 @@ struct WorldView {
     int32_t* hit_list;           // [pair capacity] work items needing a manifold this substep (queue[3])
     R* work_simplex;             // [16 * pair capacity] GJK simplex of a hit (a, b, c, d)
     double* work_epa;            // [4 * pair capacity] EPA normal (FP64) and penetration of a hit
+    float4* work_off;            // [pair capacity] FP32 build: body b's origin relative to body a's (xyz; the
+                                 //     FP64 difference rounded once per pair and substep by k_cull)
+    float* work_face;            // [12 * pair capacity] FP32 build: EPA's final face (three Minkowski points)
+                                 //     and its FP32 normal, finished in FP64 by k_epa_finish
     int32_t* queue;              // [16] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
                                  //     [2] gjk_list length, [3] hit_list length, [4] substeps run since
                                  //     the world was built (phase-major form)

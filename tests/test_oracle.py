@@ -136,3 +136,28 @@ def test_port_forces_and_edge_cases(oracle_built):
         o.step(3, collisions=False)
         outs.append(o.get_state())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_port_speed_against_the_reference(oracle_built):
+    """The port is the CPU baseline on machines without the reference checkout (the GPU host), so
+    its speed relative to the reference's own build is recorded here: the same frames of the same
+    scenes, same flags, same results. Printed (pytest -s) as body-substeps/s of each and their ratio;
+    the assertion only keeps the comparison honest (equal results, both measured)."""
+    import time
+    from oracle.oracle import reference_available
+    if not reference_available():
+        pytest.skip("reference build not present (only where the reference checkout exists)")
+    for name, settle, frames in (("stack10", 20, 20), ("large1024", 2, 3)):
+        scene = SCENES[name][0]()
+        rates, states = {}, {}
+        for kind in ("port", "reference"):
+            o = oracle_built(kind).load(scene)
+            o.step(settle)
+            t = time.perf_counter()
+            o.step(frames)
+            dt = time.perf_counter() - t
+            rates[kind] = scene.num_dynamic * scene.substeps * frames / dt
+            states[kind] = o.get_state()
+        assert np.array_equal(states["port"], states["reference"]), name
+        print("%s: port %.3g, reference %.3g body-substeps/s, port / reference %.2f"
+              % (name, rates["port"], rates["reference"], rates["port"] / rates["reference"]))
