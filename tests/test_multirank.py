@@ -1,6 +1,8 @@
 """The multi-GPU path on CPU ranks (gloo, world_size 2): the batched form shards by scene with no
 exchange while stepping; every rank builds its shard of the batch, the shards partition the batch,
-and the bench's timing reduction (max over ranks) and throughput sum behave as on GPUs."""
+each rank steps its shard (with the oracle port, the CPU stand-in for its GPU) and the gathered
+states equal the unsharded batch's run, and the bench's timing reduction (max over ranks) and
+throughput sum behave as on GPUs."""
 from __future__ import annotations
 
 import os
@@ -35,6 +37,19 @@ def _rank_main(rank, world, port, out):
     first = w.load_batch(shard)
     n = w.num_entities()
     w.close()
+    # step the shard: every scene of it, 5 frames, with no exchange between ranks
+    from oracle.oracle import Oracle, build
+    build(ref=False)
+    states = []
+    for s in range(shard.num_scenes):
+        o = Oracle("port").load(S.batch_scene(shard, s))
+        o.step(5)
+        states.append(o.get_state())
+    mine = np.concatenate(states) if states else np.zeros((0, 28))
+    every = [None] * world
+    dist.all_gather_object(every, mine)
+    if rank == 0:
+        np.save(out + ".states.npy", np.concatenate(every))
     stats = torch.tensor([shard.num_scenes, shard.num_bodies, len(shard.constraints), first, n], dtype=torch.int64)
     gathered = [torch.zeros_like(stats) for _ in range(world)]
     dist.all_gather(gathered, stats)
@@ -60,3 +75,16 @@ def test_batched_form_shards_over_two_gloo_ranks(tmp_path):
     assert shards[:, 1].sum() == tail[2]                    # bodies partitioned
     assert shards[:, 2].sum() == tail[3]                    # joints stay with their scene
     assert np.all(shards[:, 0] > 0) and np.all(shards[:, 3] == 0) and np.all(shards[:, 4] == shards[:, 1])
+    # the sharded run equals the unsharded batch's, scene by scene
+    sys.path.insert(0, os.path.join(ROOT, "raw-physics_gb300"))
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle, build
+    from rawphys import scenes as S
+    build(ref=False)
+    batch = S.batched_scenes(24, seed=11, min_bodies=2, max_bodies=40, chain_fraction=0.25, chain_links=(8, 10))
+    whole = []
+    for s in range(batch.num_scenes):
+        o = Oracle("port").load(S.batch_scene(batch, s))
+        o.step(5)
+        whole.append(o.get_state())
+    assert np.array_equal(np.load(out + ".states.npy"), np.concatenate(whole))
