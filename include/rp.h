@@ -314,7 +314,9 @@ rp_status rp_last_contacts(rp_world* w, int32_t scene, int32_t* pairs_out, doubl
  * support mapping, [18] GJK runs ended early on a repeated state (they would have reached the
  * iteration cap and returned no collision), [19] EPA set-up cycles (hull staging, simplex load),
  * [20] EPA support-mapping cycles, [21] manifold set-up cycles, [22] contact write-out cycles,
- * [23] reserved (0). Cycle counters of the phase-major kernels are summed per warp. */
+ * [23] pairs the FP32 build redid in FP64 because FP32 rounding made their EPA polytope or edge
+ * contact degenerate (phase-major form). Cycle counters of the phase-major kernels are summed per
+ * warp. */
 /* The sweep schedules of the last substep of the last rp_simulate call for one scene: per solver
  * node (the scene's external constraints, then its broad-phase pairs, in constraint order) its level
  * (RP_SWEEP_REFERENCE) or colour (RP_SWEEP_COLOURED) in the position sweep (which = 0) or the

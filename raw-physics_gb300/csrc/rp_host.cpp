@@ -149,13 +149,14 @@ struct rp_world {
     HostBuf h_hull;              // and its pinned staging
     std::vector<int64_t> hull_v_off, hull_n_off;   // per entity: first vertex / normal in entity order
     int64_t hull_nv = 0, hull_nn = 0;              // totals (vertices, normals) over every hull collider
+    DevBuf d_node_bits;
     DevBuf d_node_vpred, d_node_vlevel, d_vlevel_count, d_vlevel_fill, d_vlevel_nodes, d_scene_vlevels, d_act_list, d_act_count;
 
     // phase-major pipeline
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
     HostBuf h_state;                               // pinned staging of the body state (rp_state_set / _get)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
-    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face;
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
@@ -471,6 +472,9 @@ rp_status build_device(rp_world* w) {
     RP_CUDA(w->d_scene_vlevels.ensure((size_t)S * 4));
     RP_CUDA(w->d_act_list.ensure(std::max<size_t>(2 * NN, 1) * 4));
     RP_CUDA(w->d_act_count.ensure((size_t)S * 8));
+    RP_CUDA(w->d_node_bits.ensure((NN / 32 + 1) * 4));
+    RP_CUDA(cudaMemsetAsync(w->d_node_bits.p, 0, (NN / 32 + 1) * 4, st));
+    w->dims.node_words = (int)(NN / 32 + 1);
     RP_CUDA(w->d_scene_nodes.ensure((size_t)S * 4));
     RP_CUDA(w->d_pair_cstart.ensure(std::max<size_t>(P, 1) * 4));
     RP_CUDA(w->d_pair_ccount.ensure(std::max<size_t>(P, 1) * 4));
@@ -494,6 +498,7 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(w->d_work_simplex.ensure(std::max<size_t>(P, 1) * 16 * R));
         RP_CUDA(w->d_work_epa.ensure(std::max<size_t>(P, 1) * 4 * 8));
         RP_CUDA(w->d_work_off.ensure(std::max<size_t>(P, 1) * 16));
+        RP_CUDA(w->d_fallback.ensure(std::max<size_t>(P, 1) * 4));
         RP_CUDA(w->d_work_face.ensure(std::max<size_t>(P, 1) * 12 * 4));
         std::vector<int32_t> order((size_t)S);
         for (int sc = 0; sc < S; ++sc) order[(size_t)sc] = sc;
@@ -623,6 +628,7 @@ WorldView<R> make_view(rp_world* w) {
     V.act_list = w->d_act_list.as<int32_t>();
     V.act_count = w->d_act_count.as<int32_t>();
     V.sweep_order = w->sweep_order;
+    V.node_bits = w->d_node_bits.as<uint32_t>();
     V.status = w->d_status.as<uint32_t>();
     V.barrier = w->d_barrier.as<unsigned int>();
     V.counters = w->d_counters.as<unsigned long long>();
@@ -637,6 +643,7 @@ WorldView<R> make_view(rp_world* w) {
     V.work_simplex = w->d_work_simplex.as<R>();
     V.work_epa = w->d_work_epa.as<double>();
     V.work_off = w->d_work_off.as<float4>();
+    V.fallback_list = w->d_fallback.as<int32_t>();
     V.work_face = w->d_work_face.as<float>();
     V.queue = w->d_queue.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
@@ -1622,6 +1629,7 @@ rp_status rp_counters(rp_world* w, uint64_t out[RP_NUM_COUNTERS]) {
         out[8] = c[4]; out[9] = c[7]; out[10] = c[8]; out[11] = c[9]; out[12] = c[10]; out[13] = c[11];
         out[14] = c[12]; out[15] = c[13]; out[16] = c[14]; out[17] = c[15]; out[18] = c[16];
         out[19] = c[17]; out[20] = c[18]; out[21] = c[19]; out[22] = c[20];
+        out[23] = c[23];
     }
     out[3] = w->steps;
     out[4] = w->substeps;

@@ -17,6 +17,7 @@ struct PipeConfig {
 };
 struct PipeDims {
     int nbodies = 0, ncolliders = 0, next = 0, num_scenes = 0;
+    int node_words = 0;  // words of the node bitmap (node capacity / 32 + 1)
     int grid_mode = 0;   // one large scene: cooperative setup and sweeps
 };
 // Optional events recorded after each phase (timing runs; never inside a captured graph).

@@ -112,6 +112,11 @@ __device__ void emit_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int s, i
         tally += (unsigned long long)nc;
         W.pair_cstart[gp] = start;
         W.pair_ccount[gp] = nc;
+        if (nc > 0) {
+            // the pair's solver node (after the scene's external constraints) acts this substep
+            const int node = W.scene_node_cap[s] + (W.scene_ext[s + 1] - W.scene_ext[s]) + (gp - W.scene_pair_cap[s]);
+            atomicOr(&W.node_bits[node >> 5], 1u << (node & 31));
+        }
     }
     start = __shfl_sync(0xffffffffu, start, 0);
     nc = __shfl_sync(0xffffffffu, nc, 0);
@@ -191,7 +196,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
         W.act_count[2 * s] = 0;
         W.act_count[2 * s + 1] = 0;
     }
-    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; }
+    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; W.queue[5] = 0; }
 }
 
 // `group` threads per collider (a power of two up to 32; 8 by default: the typical hull has 8-64
@@ -378,6 +383,16 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             t.v[4] += t0 - tv;
             t.v[5] += tsup;
             const int s = W.body_scene[a];
+            if (!EXACT && (sm.status & (ST_DEG_EPA_NORMAL | ST_DEG_EPA_COPLANAR))) {
+                // FP32 resolved this polytope to a degenerate one: the pair is redone in FP64 (k_fallback),
+                // which decides it as the reference would
+                if (lane == 0) {
+                    W.work_state[k] = WS_FALLBACK;
+                    W.fallback_list[atomicAdd(&W.queue[5], 1)] = k;
+                }
+                __syncwarp();
+                continue;
+            }
             if (lane == 0) {
                 if (!ok) atomicOr(&W.status[s], (uint32_t)ST_EPA_NOT_CONVERGED);
                 if (sm.status) {
@@ -470,12 +485,139 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
             const long long t2 = clock64();
             t.v[1] += t2 - t0;
             t.v[2] += t1 - t0;
+            if (!EXACT && st == WS_EPA_OK && (sm.status & ST_DEG_SKEW)) {
+                if (lane == 0) {
+                    W.work_state[k] = WS_FALLBACK;
+                    W.fallback_list[atomicAdd(&W.queue[5], 1)] = k;
+                }
+                __syncwarp();
+                continue;
+            }
             emit_contacts(W, sm, s, gp, t.v[0]);
             t.v[3] += clock64() - t2;
         }
     }
     const int slots[8] = {3, 14, 19, 20, -1, -1, -1, -1};
     t.flush(W.counters, slots);
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64 redo of the FP32 build's degenerate pairs. Where FP32 rounding makes EPA's polytope degenerate
+// (its points coplanar, a face normal that vanishes: typically two boxes resting face to face, as the
+// links of a joint chain do) or the edge-edge contact's lines parallel, the reference, in FP64,
+// usually is not: the pair's GJK, EPA and contact manifold run again in FP64 from the FP64 poses and
+// hull geometry (the exact build's code), and its contacts replace the FP32 ones. One warp per pair.
+constexpr int FALLBACK_MAXF = 128;   // face normals staged per hull
+
+template <typename R>
+__device__ WorldView<double> fp64_geometry(const WorldView<R>& W) {
+    WorldView<double> G;
+    memset(&G, 0, sizeof(G));
+    G.colliders = W.colliders;
+    G.shapes = W.shapes;
+    G.shape_verts = W.shape_verts;
+    G.face_normal = W.face_normal;
+    G.face_elem_start = W.face_elem_start;
+    G.face_elem = W.face_elem;
+    G.csr_start = W.csr_start;
+    G.csr_data = W.csr_data;
+    G.pos = W.pos;
+    G.rot = W.rot;
+    return G;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32) k_fallback(WorldView<R> W) {
+    if (frame_abandoned(W.status)) return;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    NarrowSmem<double>& sm = *reinterpret_cast<NarrowSmem<double>*>(dyn_smem);
+    V3<double>* norms = reinterpret_cast<V3<double>*>(dyn_smem + sizeof(NarrowSmem<double>));
+    const int lane = threadIdx.x & 31;
+    const int n = W.queue[5];
+    const WorldView<double> G = fp64_geometry(W);
+    for (int j = blockIdx.x; j < n; j += gridDim.x) {
+        const int k = W.fallback_list[j];
+        const int gp = W.work_list[k];
+        const int2 pr = W.pairs[gp];
+        const int s = W.body_scene[pr.x];
+        ColView<double> v[2];
+        const double4_32a pa = W.pos[pr.x], pb = W.pos[pr.y], qa = W.rot[pr.x], qb = W.rot[pr.y];
+        for (int side = 0; side < 2; ++side) {
+            const int body = side ? pr.y : pr.x;
+            const Collider col = W.colliders[W.col_start[body]];
+            const Shape* sh = W.shapes + col.shape;
+            const double4_32a p4 = side ? pb : pa, q4 = side ? qb : qa;
+            const M4<double> M = model_matrix(qt<double>(q4.x, q4.y, q4.z, q4.w), v3<double>(p4.x, p4.y, p4.z));
+            V3<double>* tv = side ? sm.vb : sm.va;
+            V3<double>* tn = norms + side * FALLBACK_MAXF;
+            for (int i = lane; i < sh->nv; i += 32) {
+                const double* x = W.shape_verts + 3 * (size_t)(sh->vert_off + i);
+                tv[i] = m4_point(M, v3<double>(x[0], x[1], x[2]));
+            }
+            for (int i = lane; i < sh->nf; i += 32) {
+                const double* x = W.face_normal + 3 * (size_t)(sh->face_off + i);
+                tn[i] = vnorm(m4_dir(M, v3<double>(x[0], x[1], x[2])));
+            }
+            ColView<double>& c = v[side];
+            c.type = COL_HULL;
+            c.radius = 0.0;
+            c.center = v3<double>(p4.x, p4.y, p4.z);
+            c.off = v3<double>(0, 0, 0);
+            c.verts = tv;
+            c.staged = true;
+            c.norms = tn;
+            c.nv = sh->nv;
+            c.nf = sh->nf;
+            c.shape = sh;
+            c.body = body;
+        }
+        PairFrame<double, true> fr;
+        fr.raw = false;
+        fr.x1 = v3<double>(pa.x, pa.y, pa.z);
+        fr.x2 = v3<double>(pb.x, pb.y, pb.z);
+        fr.q1inv = qinverse(qt<double>(qa.x, qa.y, qa.z, qa.w));
+        fr.q2inv = qinverse(qt<double>(qb.x, qb.y, qb.z, qb.w));
+        if (lane == 0) { sm.ncontacts = 0; sm.status = 0; }
+        __syncwarp();
+        collider_contacts<double, true>(sm, G, v[0], v[1], fr, nullptr);
+        __syncwarp();
+        // write the contacts as the FP32 build stores them (emit_contacts)
+        const int cbase = W.scene_contact_cap[s];
+        const int ccap = W.scene_contact_cap[s + 1] - cbase;
+        int nc = sm.ncontacts, start = 0;
+        if (lane == 0) {
+            start = nc ? atomicAdd(&W.contact_count[s], nc) : 0;
+            if (start + nc > ccap) {
+                atomicOr(&W.status[s], (uint32_t)ST_CONTACT_OVERFLOW);
+                nc = 0;
+            }
+            if (sm.status) {
+                atomicOr(&W.status[s], (uint32_t)sm.status);
+                note_degenerate(W, (uint32_t)sm.status, s, pr.x, pr.y);
+            }
+            W.pair_cstart[gp] = start;
+            W.pair_ccount[gp] = nc;
+            W.work_state[k] = nc ? WS_EPA_OK : WS_NONE;
+            if (nc > 0) {
+                const int node = W.scene_node_cap[s] + (W.scene_ext[s + 1] - W.scene_ext[s]) + (gp - W.scene_pair_cap[s]);
+                atomicOr(&W.node_bits[node >> 5], 1u << (node & 31));
+            }
+            if (W.counters) {
+                atomicAdd(&W.counters[3], (unsigned long long)nc);
+                atomicAdd(&W.counters[23], 1ull);
+            }
+        }
+        start = __shfl_sync(0xffffffffu, start, 0);
+        nc = __shfl_sync(0xffffffffu, nc, 0);
+        for (int c = lane; c < nc; c += 32) {
+            R* o = W.contacts + 12 * (size_t)(cbase + start + c);
+            const V3<double> r1 = sm.c_r1[c], r2 = sm.c_r2[c], nn = sm.c_n[c];
+            o[0] = (R)r1.x; o[1] = (R)r1.y; o[2] = (R)r1.z; o[3] = 0;
+            o[4] = (R)r2.x; o[5] = (R)r2.y; o[6] = (R)r2.z; o[7] = 0;
+            o[8] = (R)nn.x; o[9] = (R)nn.y; o[10] = (R)nn.z; o[11] = 0;
+        }
+        __syncwarp();
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -497,6 +639,90 @@ __global__ void __launch_bounds__(BLOCK) k_sweep_cta(WorldView<R> W, double h, i
 // sweep of a substep builds the substep's schedules first (resched).
 constexpr int SWEEP_WARP_BLOCK = 128;
 
+// Both per-substep schedules of scene s by one warp, in one ordered pass (the result resched would
+// give). The active nodes are gathered in constraint order (external constraints, then the pairs
+// whose bit the contact write-out set), then lane 0 walks them once: in reference order a node's level
+// is one more than the latest level on either of its bodies (the longest path, since a body's nodes
+// are visited in order); in coloured order it takes the smallest colour neither body has used yet
+// (first-fit, so a joint chain alternates two colours). One pass instead of one relaxation round per
+// dependent step (a 64-link chain would take 64). Scenes beyond the shared tables take resched.
+constexpr int SERIAL_MAX_BODIES = 512;
+constexpr int SERIAL_MAX_WORDS = 256;   // node bitmap words staged per warp (8192 nodes)
+struct SerialSmem {
+    uint64_t mask[SERIAL_MAX_BODIES];   // coloured: colours used per body (position sweep)
+    uint64_t vmask[SERIAL_MAX_BODIES];  // (velocity sweep)
+    uint32_t words[SERIAL_MAX_WORDS + 2];
+};
+
+template <typename R>
+__device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
+    const int lane = threadIdx.x & 31;
+    const int b0 = W.scene_body[s], nb = W.scene_body[s + 1] - b0;
+    const int ne = W.scene_ext[s + 1] - W.scene_ext[s];
+    const int nbase = W.scene_node_cap[s];
+    const int nn = W.scene_nodes[s];
+    const int w0 = (nbase + ne) >> 5, w1 = (nbase + nn + 31) >> 5;
+    if (nb > SERIAL_MAX_BODIES || w1 - w0 > SERIAL_MAX_WORDS) return false;
+    const int* nbody = W.node_body + 2 * nbase;
+    const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
+    const bool coloured = W.sweep_order == SWEEP_COLOURED;
+    // clear the level tables the previous substep used, and the per-body tables
+    const int used0 = min(*(volatile int*)v0.levels + 1, W.max_levels), used1 = min(*(volatile int*)v1.levels + 1, W.max_levels);
+    for (int l = lane; l <= used0; l += 32) { v0.count[l] = 0; v0.fill[l] = 0; }
+    for (int l = lane; l <= used1; l += 32) { v1.count[l] = 0; v1.fill[l] = 0; }
+    for (int b = lane; b < nb; b += 32) { sm.mask[b] = 0ull; sm.vmask[b] = 0ull; }
+    for (int w = lane; w < w1 - w0; w += 32) sm.words[w] = W.node_bits[w0 + w];
+    __syncwarp();
+    if (lane == 0) {
+        // per body: reference order keeps 1 + its latest level (0: none yet), coloured order the set
+        // of colours its nodes use
+        int n0 = 0, n1 = 0, extra = 0;
+        auto place = [&](int k, bool pair) {
+            const int a = nbody[2 * k], c = nbody[2 * k + 1];
+            const int ia = a >= 0 ? a - b0 : -1, ic = c >= 0 ? c - b0 : -1;
+            if (ia < 0 && ic < 0) return;                       // no dynamic body: a no-op node
+            for (int which = 0; which < (pair ? 2 : 1); ++which) {
+                uint64_t* m = which ? sm.vmask : sm.mask;
+                const uint64_t ma = ia >= 0 ? m[ia] : 0ull, mc = ic >= 0 ? m[ic] : 0ull;
+                int l;
+                if (coloured) {
+                    const uint64_t used = ma | mc;
+                    if (~used) {
+                        l = __ffsll((long long)~used) - 1;
+                        if (ia >= 0) m[ia] = ma | (1ull << l);
+                        if (ic >= 0) m[ic] = mc | (1ull << l);
+                    } else {
+                        l = 64 + extra++;                          // every small colour taken: a colour of its own
+                    }
+                } else {
+                    l = (int)(ma > mc ? ma : mc);
+                    if (ia >= 0) m[ia] = (uint64_t)l + 1ull;
+                    if (ic >= 0) m[ic] = (uint64_t)l + 1ull;
+                }
+                const SchedView<R>& v = which ? v1 : v0;
+                v.lev[k] = l;
+                v.list[which ? n1++ : n0++] = k;
+            }
+        };
+        for (int k = 0; k < ne; ++k) place(k, false);
+        for (int w = 0; w < w1 - w0; ++w) {
+            uint32_t bits = sm.words[w];
+            const int base = ((w0 + w) << 5) - nbase;
+            while (bits) {
+                const int k = base + __ffs(bits) - 1;
+                bits &= bits - 1u;
+                if (k >= ne && k < nn) place(k, true);
+            }
+        }
+        *v0.active = n0;
+        *v1.active = n1;
+        *v0.levels = 0;
+        *v1.levels = 0;
+    }
+    __syncwarp();
+    return true;
+}
+
 template <typename R, bool EXACT, bool VELOCITY>
 __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
@@ -508,7 +734,19 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= W.num_scenes) break;
         const int s = W.scene_order[i];
-        if (!VELOCITY && resched_first) resched(W, g, s);
+        if constexpr (!VELOCITY) {
+            __shared__ SerialSmem ssm[SWEEP_WARP_BLOCK / 32];
+            if (resched_first) {
+                if (resched_serial(W, s, ssm[threadIdx.x >> 5])) {
+                    SubWarp q;
+                    const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
+                    bucket_schedule(W, q, s, v0, *(volatile int*)v0.active, true);
+                    bucket_schedule(W, q, s, v1, *(volatile int*)v1.active, false);
+                } else {
+                    resched(W, g, s);
+                }
+            }
+        }
         sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
         __syncwarp();
     }
@@ -534,11 +772,14 @@ template <typename R, bool EXACT>
 struct PipeLauncher {
     static size_t gjk_smem() { return sizeof(GjkSmem<R>) * PIPE_WARPS; }
     static size_t narrow_smem() { return sizeof(NarrowSmem<R>) * PIPE_WARPS; }
+    static size_t fallback_smem() { return sizeof(NarrowSmem<double>) + 2 * FALLBACK_MAXF * sizeof(V3<double>); }
 
     static cudaError_t configure(PipeConfig& c, int sms) {
         cudaError_t e = cudaFuncSetAttribute(k_gjk<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gjk_smem());
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_epa<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_manifold<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
+        if (e == cudaSuccess && !EXACT)
+            e = cudaFuncSetAttribute(k_fallback<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fallback_smem());
         if (e != cudaSuccess) return e;
         int nb = 0;
         auto occ = [&](const void* f, int block, size_t smem) {
@@ -607,7 +848,9 @@ struct PipeLauncher {
         if (e != cudaSuccess || (e = mark(PH_BROAD)) != cudaSuccess) return e;
         for (int sub = 0; sub < P.num_substeps; ++sub) {
             k_predict<R, EXACT><<<body_blocks, PIPE_BLOCK, 0, st>>>(W, d.nbodies, d.next, h);
-            if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_PREDICT)) != cudaSuccess) return e;
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(W.node_bits, 0, (size_t)d.node_words * 4, st)) != cudaSuccess) return e;
+            if ((e = mark(PH_PREDICT)) != cudaSuccess) return e;
             if (P.enable_collisions) {
                 k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0, c.transform_group);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
@@ -625,7 +868,12 @@ struct PipeLauncher {
                 }
                 if ((e = mark(PH_EPA)) != cudaSuccess) return e;
                 k_manifold<R, EXACT><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
-                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_MANIFOLD)) != cudaSuccess) return e;
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if (!EXACT) {
+                    k_fallback<R><<<c.sms, 32, fallback_smem(), st>>>(W);
+                    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                }
+                if ((e = mark(PH_MANIFOLD)) != cudaSuccess) return e;
             }
             for (int it = 0; it < P.num_pos_iters; ++it) {
                 const int first = it == 0 ? 1 : 0;   // the substep's schedules are built by its first sweep
@@ -646,7 +894,7 @@ struct PipeLauncher {
     }
 
     static int launches_per_frame(const StepParams& P) {
-        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 5 : 6) : 1) + P.num_pos_iters + 1;
+        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 5 : 7) : 1) + P.num_pos_iters + 1;
         return 1 + P.num_substeps * per_sub;
     }
 };

@@ -60,7 +60,7 @@ struct Shape {               // one convex hull's topology (collider_convex_hull
 };
 
 // Per-pair state between the narrowphase kernels of the phase-major pipeline
-enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3, WS_EPA_FACE = 4 };
+enum : int32_t { WS_NONE = 0, WS_HIT = 1, WS_GENERAL = 2, WS_EPA_OK = 3, WS_EPA_FACE = 4, WS_FALLBACK = 5 };
 
 // Phases of the step timed per frame (rp_phase_times). The persistent kernel times the whole
 // narrowphase as PH_NARROW; the phase-major form splits it into the cull (PH_NARROW), GJK, EPA and
@@ -164,6 +164,8 @@ struct WorldView {
     int32_t* act_list;       // [2 * nodes] active nodes of each schedule (position, then velocity)
     int32_t* act_count;      // [2 * S] their counts (zeroed by the substep's predict phase)
     int32_t sweep_order;     // SWEEP_REFERENCE (the reference's serial order) or SWEEP_COLOURED
+    uint32_t* node_bits;     // [nodes / 32 + 1] phase-major form: bit (scene node base + k) set when pair node
+                             //     k has contacts this substep (cleared before every substep's narrowphase)
     int32_t* scene_nodes;    // [S] number of live nodes (ext + pairs)
     int32_t* pair_cstart;    // [pairs] first contact of each pair
     int32_t* pair_ccount;    // [pairs]
@@ -185,11 +187,13 @@ struct WorldView {
     double* work_epa;            // [4 * pair capacity] EPA normal (FP64) and penetration of a hit
     float4* work_off;            // [pair capacity] FP32 build: body b's origin relative to body a's (xyz; the
                                  //     FP64 difference rounded once per pair and substep by k_cull)
+    int32_t* fallback_list;      // [pair capacity] FP32 build: work items whose FP32 EPA or edge contact met a
+                                 //     degenerate configuration, redone in FP64 (queue[5] of them)
     float* work_face;            // [12 * pair capacity] FP32 build: EPA's final face (three Minkowski points)
                                  //     and its FP32 normal, finished in FP64 by k_epa_finish
     int32_t* queue;              // [16] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
                                  //     [2] gjk_list length, [3] hit_list length, [4] substeps run since
-                                 //     the world was built (phase-major form)
+                                 //     the world was built (phase-major form), [5] fallback_list length
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
     int32_t max_colliders_per_body;
     int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
