@@ -2134,12 +2134,28 @@ rp_status rp_last_schedule(rp_world* w, int32_t scene, int32_t which, int32_t* l
     const int32_t nbase = w->scene_node_cap[(size_t)scene];
     const uint32_t m = std::min<uint32_t>((uint32_t)nn, cap);
     if (m == 0) return RP_OK;
-    std::vector<int32_t> lev(m), bod(2 * (size_t)m);
-    const DevBuf& L = which ? w->d_node_vlevel : w->d_node_level;
-    RP_CUDA(cudaMemcpyAsync(lev.data(), L.as<int32_t>() + nbase, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    // the schedule is what the sweeps read: the level table and the nodes bucketed by level
+    const DevBuf& Lv = which ? w->d_scene_vlevels : w->d_scene_levels;
+    const DevBuf& Lc = which ? w->d_vlevel_count : w->d_level_count;
+    const DevBuf& Ln = which ? w->d_vlevel_nodes : w->d_level_nodes;
+    int32_t L = 0;
+    RP_CUDA(cudaMemcpyAsync(&L, Lv.as<int32_t>() + scene, 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    L = std::max(0, std::min(L, w->max_levels));
+    std::vector<int32_t> start((size_t)L + 1);
+    RP_CUDA(cudaMemcpyAsync(start.data(), Lc.as<int32_t>() + (size_t)scene * (size_t)(w->max_levels + 1),
+                            ((size_t)L + 1) * 4, cudaMemcpyDeviceToHost, w->stream));
+    RP_CUDA(cudaStreamSynchronize(w->stream));
+    const int32_t total = std::max(0, std::min(start[(size_t)L], nn));
+    std::vector<int32_t> nodes((size_t)std::max(total, 1)), bod(2 * (size_t)m);
+    if (total) RP_CUDA(cudaMemcpyAsync(nodes.data(), Ln.as<int32_t>() + nbase, (size_t)total * 4, cudaMemcpyDeviceToHost, w->stream));
     RP_CUDA(cudaMemcpyAsync(bod.data(), w->d_node_body.as<int32_t>() + 2 * (size_t)nbase, 2 * (size_t)m * 4,
                             cudaMemcpyDeviceToHost, w->stream));
     RP_CUDA(cudaStreamSynchronize(w->stream));
+    std::vector<int32_t> lev(m, -1);
+    for (int32_t l = 0; l < L; ++l)
+        for (int32_t i = start[(size_t)l]; i < start[(size_t)l + 1] && i < total; ++i)
+            if (nodes[(size_t)i] >= 0 && (uint32_t)nodes[(size_t)i] < m) lev[(size_t)nodes[(size_t)i]] = l;
     for (uint32_t k = 0; k < m; ++k) {
         if (level_out) level_out[k] = lev[k];
         if (bodies_out)
