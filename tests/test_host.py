@@ -338,3 +338,6 @@ def test_bench_sample_and_step_error():
     b[1, 1] = 2e-4
     e = step_error(b, a, np.array([True, True, False]))
     assert e["bodies"] == 2 and abs(e["pos_m"]["max"] - 2e-4) < 1e-15 and e["within_1e-4"] == 0.5
+    # the second body's 2e-4 m is within three times a reference that itself moves 1e-4 m under noise
+    e = bench.with_spread(e, b, a, np.array([True, True, False]), np.array([0.0, 1e-4, 0.0]))
+    assert e["within_1e-4_or_3x_spread"] == 1.0 and e["reference_spread_m"]["max"] == 1e-4
