@@ -149,7 +149,7 @@ struct rp_world {
     HostBuf h_hull;              // and its pinned staging
     std::vector<int64_t> hull_v_off, hull_n_off;   // per entity: first vertex / normal in entity order
     int64_t hull_nv = 0, hull_nn = 0;              // totals (vertices, normals) over every hull collider
-    DevBuf d_node_bits;
+    DevBuf d_node_bits, d_sdx, d_sdq, d_pred_d, d_prev_qf;
     DevBuf d_node_vpred, d_node_vlevel, d_vlevel_count, d_vlevel_fill, d_vlevel_nodes, d_scene_vlevels, d_act_list, d_act_count;
 
     // phase-major pipeline
@@ -491,6 +491,10 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(upload(w->d_body_scene, body_scene, st));
         RP_CUDA(upload(w->d_col_body, col_body, st));
         RP_CUDA(w->d_pose_f.ensure(std::max<size_t>(N, 1) * 32));
+        for (DevBuf* b : {&w->d_sdx, &w->d_sdq, &w->d_pred_d, &w->d_prev_qf}) {
+            RP_CUDA(b->ensure(std::max<size_t>(N, 1) * 16));
+            RP_CUDA(cudaMemsetAsync(b->p, 0, std::max<size_t>(N, 1) * 16, st));
+        }
         RP_CUDA(w->d_work_list.ensure(std::max<size_t>(P, 1) * 4));
         RP_CUDA(w->d_work_state.ensure(std::max<size_t>(P, 1) * 4));
         RP_CUDA(w->d_gjk_list.ensure(std::max<size_t>(P, 1) * 4));
@@ -635,6 +639,10 @@ WorldView<R> make_view(rp_world* w) {
     V.phase_ns = w->d_phase.as<unsigned long long>();
     V.body_scene = w->d_body_scene.as<int32_t>();
     V.pose_f = w->d_pose_f.as<float4>();
+    V.sdx = w->d_sdx.as<float4>();
+    V.sdq = w->d_sdq.as<float4>();
+    V.pred_d = w->d_pred_d.as<float4>();
+    V.prev_qf = w->d_prev_qf.as<float4>();
     V.col_body = w->d_col_body.as<int32_t>();
     V.work_list = w->d_work_list.as<int32_t>();
     V.work_state = w->d_work_state.as<int32_t>();

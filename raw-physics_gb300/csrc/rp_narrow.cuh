@@ -957,8 +957,13 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         // nearly parallel faces d1 and d2 differ by ~1e-11, below FP32 resolution; decide it from
         // FP64 normals so the FP32 build picks the reference's face (and so its contact order).
         // Outside 1e-5 (FP32 error of these unit-vector dot products: ~3e-7) FP32 decides the same.
-        V3<double> m1 = face_normal64(W, h1, f1), m2 = face_normal64(W, h2, f2);
-        ref1 = vdot(m1, normal64) > vdot(m2, vinv(normal64));
+        // one lane evaluates it (FP64 on GB300 issues at 1/64 of the FP32 rate) and broadcasts it
+        int r = 0;
+        if (lane == 0) {
+            const V3<double> m1 = face_normal64(W, h1, f1), m2 = face_normal64(W, h2, f2);
+            r = vdot(m1, normal64) > vdot(m2, vinv(normal64)) ? 1 : 0;
+        }
+        ref1 = __shfl_sync(0xffffffffu, r, 0) != 0;
     }
     const ColView<R>& rh = ref1 ? h1 : h2;
     const ColView<R>& ih = ref1 ? h2 : h1;

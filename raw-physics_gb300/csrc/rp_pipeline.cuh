@@ -185,9 +185,13 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
     const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
     for (int b = t; b < nbodies; b += n) {
         predict_body<R, EXACT>(W, b, h);
-        const double4_32a p = W.pos[b], q = W.rot[b];
-        W.pose_f[2 * b] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
-        W.pose_f[2 * b + 1] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+        if constexpr (EXACT) {
+            const double4_32a p = W.pos[b], q = W.rot[b];
+            W.pose_f[2 * b] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+            W.pose_f[2 * b + 1] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+        } else {
+            stage_body(W, b);
+        }
     }
     for (int e = t; e < next; e += n)
         for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
@@ -220,7 +224,10 @@ template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_velocity(WorldView<R> W, int nbodies, double h) {
     if (frame_abandoned(W.status)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
-    for (int b = t; b < nbodies; b += n) velocity_body<R, EXACT>(W, b, h);
+    for (int b = t; b < nbodies; b += n) {
+        if constexpr (!EXACT) fold_body(W, b);   // the position sweep's corrections into the FP64 pose
+        velocity_body<R, EXACT>(W, b, h);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -388,9 +388,12 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
 // with u = dq + increment and e = |q0 + u|^2 - 1 = 2 q0.u + u.u, the normalised quaternion is
 // q0 + q0 (r - 1) + u r with r - 1 = -e / (s (1 + s)), s = sqrt(1 + e), all of which are small,
 // well-conditioned FP32 quantities. Per contact the solve then needs no FP64 arithmetic at all.
+// FP32 build: a body during the substep's position sweep. Its FP64 pose stays at the predicted pose
+// (pos / rot); the sweep's corrections accumulate per body in FP32 deltas (sdx, sdq), and the pose is
+// folded into FP64 once per substep (fold_body), so FP64 carries the pose across substeps while the
+// solve itself runs in FP32. A node loads the body's FP32 orientation (pose_f) and deltas and stores
+// the deltas back.
 struct FBody {
-    V3<double> x0;
-    Qt<double> q0;
     V3<float> dx;
     Qt<float> q0f, dq;
     float invm;
@@ -402,12 +405,10 @@ struct FBody {
 
 __device__ __forceinline__ FBody load_fbody(const WorldView<float>& W, int b) {
     FBody B;
-    double4_32a p = W.pos[b], q = W.rot[b];
-    B.x0 = v3<double>(p.x, p.y, p.z);
-    B.q0 = qt<double>(q.x, q.y, q.z, q.w);
-    B.q0f = qcast<float>(B.q0);
-    B.dx = v3<float>(0.f, 0.f, 0.f);
-    B.dq = qt<float>(0.f, 0.f, 0.f, 0.f);
+    const float4 qf = W.pose_f[2 * b + 1], d = W.sdx[b], q = W.sdq[b];
+    B.q0f = qt<float>(qf.x, qf.y, qf.z, qf.w);
+    B.dx = v3<float>(d.x, d.y, d.z);
+    B.dq = qt<float>(q.x, q.y, q.z, q.w);
     B.invm = W.inv_mass[b];
     float s[6];
 #pragma unroll
@@ -420,11 +421,27 @@ __device__ __forceinline__ FBody load_fbody(const WorldView<float>& W, int b) {
 
 __device__ __forceinline__ void store_fbody(const WorldView<float>& W, const FBody& B) {
     if (B.fixed) return;
-    V3<double> x = vadd(B.x0, v3cast<double>(B.dx));
-    Qt<double> q = qnormalize_fast(qt<double>(B.q0.x + (double)B.dq.x, B.q0.y + (double)B.dq.y, B.q0.z + (double)B.dq.z,
-                                              B.q0.w + (double)B.dq.w));
-    W.pos[B.idx] = make_double4_32a(x.x, x.y, x.z, 0.0);
-    W.rot[B.idx] = make_double4_32a(q.x, q.y, q.z, q.w);
+    W.sdx[B.idx] = make_float4(B.dx.x, B.dx.y, B.dx.z, 0.f);
+    W.sdq[B.idx] = make_float4(B.dq.x, B.dq.y, B.dq.z, B.dq.w);
+}
+
+// (float)(x_a - x_b) of the two bodies' predicted positions: the FP32 offset a node solves around
+__device__ __forceinline__ V3<float> fbase(const WorldView<float>& W, int a, int b) {
+    const double4_32a pa = W.pos[a], pb = W.pos[b];
+    return v3<float>((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z));
+}
+
+// The position sweep's corrections into the FP64 pose (x += dx, q = normalize(q + dq)), and the
+// FP32 orientation copy the velocity sweep reads; bodies the sweep did not touch keep their pose.
+__device__ __forceinline__ void fold_body(const WorldView<float>& W, int b) {
+    const float4 d = W.sdx[b], q = W.sdq[b];
+    if (d.x == 0.f && d.y == 0.f && d.z == 0.f && q.x == 0.f && q.y == 0.f && q.z == 0.f && q.w == 0.f) return;
+    const double4_32a p4 = W.pos[b], q4 = W.rot[b];
+    const Qt<double> nq = qnormalize_fast(qt<double>(q4.x + (double)q.x, q4.y + (double)q.y, q4.z + (double)q.z,
+                                                     q4.w + (double)q.w));
+    W.pos[b] = make_double4_32a(p4.x + (double)d.x, p4.y + (double)d.y, p4.z + (double)d.z, 0.0);
+    W.rot[b] = make_double4_32a(nq.x, nq.y, nq.z, nq.w);
+    W.pose_f[2 * b + 1] = make_float4((float)nq.x, (float)nq.y, (float)nq.z, (float)nq.w);
 }
 
 // q <- normalize(q + inc), in delta form
@@ -488,10 +505,12 @@ static __device__ void fcollision_solve(const WorldView<float>& W, FBody& a, FBo
         dl = fpos_dlambda(a, b, p, 0.f, dx);
         float lt = lambda_t + dl;
         if (lt > mus * lambda_n) {
-            double4_32a pa = W.prev_pos[a.idx], qa = W.prev_rot[a.idx], pb = W.prev_pos[b.idx], qb = W.prev_rot[b.idx];
-            Qt<float> qa_prev = qcast<float>(qt<double>(qa.x, qa.y, qa.z, qa.w)), qb_prev = qcast<float>(qt<double>(qb.x, qb.y, qb.z, qb.w));
-            V3<float> da = vadd(vadd(v3cast<float>(vsub(a.x0, v3<double>(pa.x, pa.y, pa.z))), a.dx), vsub(p.r1, qrotate(qa_prev, r1)));
-            V3<float> db = vadd(vadd(v3cast<float>(vsub(b.x0, v3<double>(pb.x, pb.y, pb.z))), b.dx), vsub(p.r2, qrotate(qb_prev, r2)));
+            // displacement since the substep began: the predict step's (pred_d, FP32 from the FP64 poses)
+            // plus the sweep's; the previous orientations' FP32 copies (prev_qf)
+            const float4 pda = W.pred_d[a.idx], pdb = W.pred_d[b.idx], qa = W.prev_qf[a.idx], qb = W.prev_qf[b.idx];
+            Qt<float> qa_prev = qt<float>(qa.x, qa.y, qa.z, qa.w), qb_prev = qt<float>(qb.x, qb.y, qb.z, qb.w);
+            V3<float> da = vadd(vadd(v3<float>(pda.x, pda.y, pda.z), a.dx), vsub(p.r1, qrotate(qa_prev, r1)));
+            V3<float> db = vadd(vadd(v3<float>(pdb.x, pdb.y, pdb.z), b.dx), vsub(p.r2, qrotate(qb_prev, r2)));
             V3<float> dp = vsub(da, db);
             V3<float> dpt = vsub(dp, vscale(vdot(dp, n), n));
             fpos_apply(a, b, p, dl, dpt);
@@ -540,9 +559,10 @@ __device__ __forceinline__ void fang_apply(FBody& a, FBody& b, const Acpd<float>
     if (!b.fixed) frot_update(b, qt<float>(-0.5f * q2.x, -0.5f * q2.y, -0.5f * q2.z, -0.5f * q2.w));
 }
 
-// the FP64 orientation of a body in delta form
-__device__ __forceinline__ Qt<double> fq64(const FBody& B) {
-    return qt<double>(B.q0.x + (double)B.dq.x, B.q0.y + (double)B.dq.y, B.q0.z + (double)B.dq.z, B.q0.w + (double)B.dq.w);
+// the FP64 orientation of a body in delta form (the predicted FP64 orientation plus the sweep's delta)
+__device__ __forceinline__ Qt<double> fq64(const WorldView<float>& W, const FBody& B) {
+    const double4_32a q = W.rot[B.idx];
+    return qt<double>(q.x + (double)B.dq.x, q.y + (double)B.dq.y, q.z + (double)B.dq.z, q.w + (double)B.dq.w);
 }
 
 // angular correction of one joint limit (limit_angle's dq, FP64) on the deltas
@@ -561,11 +581,13 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
     FBody a = load_fbody(W, C.e1), b = load_fbody(W, C.e2);
     const V3<float> r1 = v3<float>((float)C.r1[0], (float)C.r1[1], (float)C.r1[2]);
     const V3<float> r2 = v3<float>((float)C.r2[0], (float)C.r2[1], (float)C.r2[2]);
-    const V3<float> base_ab = v3cast<float>(vsub(a.x0, b.x0));
+    const V3<float> base_ab = fbase(W, C.e1, C.e2);
     auto anchor = [&](const Pcpd<float>& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
     switch (C.type) {
     case CON_POSITIONAL: {  // pbd.cpp:81-97
-        const V3<float> base = v3cast<float>(vsub(vsub(a.x0, b.x0), v3<double>(C.distance[0], C.distance[1], C.distance[2])));
+        const double4_32a pa = W.pos[C.e1], pb = W.pos[C.e2];
+        const V3<float> base = v3<float>((float)((pa.x - pb.x) - C.distance[0]), (float)((pa.y - pb.y) - C.distance[1]),
+                                         (float)((pa.z - pb.z) - C.distance[2]));
         const V3<float> dx = vadd(base, vsub(a.dx, b.dx));
         const Pcpd<float> p = fpcpd(a, b, r1, r2);
         const float dl = fpos_dlambda_c(a, b, p, h, (float)C.compliance, (float)lam[0], dx);
@@ -592,7 +614,7 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
         fpos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
         if (C.limited && limit_may_act(qaxis(a.q(), C.a1), qaxis(a.q(), C.l1), qaxis(b.q(), C.l2), C.lo, C.hi)) {
-            const Qt<double> qa = fq64(a), qb = fq64(b);
+            const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
             V3<double> dq64;
             if (limit_angle<double>(qaxis(qa, C.a1), qaxis(qa, C.l1), qaxis(qb, C.l2), C.lo, C.hi, dq64))
                 flimit_apply(a, b, dq64, h, &lam[2]);
@@ -609,7 +631,7 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
             const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2), fn = vcross(f1, f2);
             const float fl = vlen(fn);
             if (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi)) {
-                const Qt<double> qa = fq64(a), qb = fq64(b);
+                const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
                 const V3<double> n1 = qaxis(qa, C.a1), n2 = qaxis(qb, C.a2);
                 V3<double> n = vcross(n1, n2);
                 const double nl = vlen(n);
@@ -635,7 +657,7 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
                                                  : limit_may_act(gn, vscale(1.f / l1, h1), vscale(1.f / l2, h2), C.lo2, C.hi2);
             }
             if (act) {
-                const Qt<double> qa = fq64(a), qb = fq64(b);
+                const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
                 const V3<double> a1 = qaxis(qa, C.a1), b1 = qaxis(qa, C.l1), a2 = qaxis(qb, C.a2), b2 = qaxis(qb, C.l2);
                 V3<double> n = vadd(a1, a2);
                 const double nl = vlen(n);
@@ -656,6 +678,18 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
     }
     store_fbody(W, a);
     store_fbody(W, b);
+}
+
+// FP32 build: after predict, the FP32 copies the substep's sweeps work from (the pose, the predict
+// step's displacement and the previous orientation) and zero sweep deltas.
+__device__ __forceinline__ void stage_body(const WorldView<float>& W, int b) {
+    const double4_32a p = W.pos[b], q = W.rot[b], pp = W.prev_pos[b], pq = W.prev_rot[b];
+    W.pose_f[2 * b] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+    W.pose_f[2 * b + 1] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+    W.sdx[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+    W.sdq[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+    W.pred_d[b] = make_float4((float)(p.x - pp.x), (float)(p.y - pp.y), (float)(p.z - pp.z), 0.f);
+    W.prev_qf[b] = make_float4((float)pq.x, (float)pq.y, (float)pq.z, (float)pq.w);
 }
 
 // --------------------------------------------------------------------------------------------

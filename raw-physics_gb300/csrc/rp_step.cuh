@@ -1153,7 +1153,7 @@ __device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
         store_pose(W, b);
     } else {
         FBody a = load_fbody(W, pr.x), b = load_fbody(W, pr.y);
-        const V3<float> base_ab = v3cast<float>(vsub(a.x0, b.x0));
+        const V3<float> base_ab = fbase(W, pr.x, pr.y);
         for (int i = 0; i < nc; ++i) fcollision_solve(W, a, b, base_ab, c + 12 * i, mus);
         store_fbody(W, a);
         store_fbody(W, b);
@@ -1174,9 +1174,15 @@ __device__ void vsolve_node(const WorldView<R>& W, int s, int k, R h) {
     M3<R> Ia, Ib;
     VelBody<R> a, b;
     {
-        double4_32a q4a = W.rot[ia], q4b = W.rot[ib];
-        qa = qcast<R>(qt<double>(q4a.x, q4a.y, q4a.z, q4a.w));
-        qb = qcast<R>(qt<double>(q4b.x, q4b.y, q4b.z, q4b.w));
+        if constexpr (EXACT) {
+            double4_32a q4a = W.rot[ia], q4b = W.rot[ib];
+            qa = qcast<R>(qt<double>(q4a.x, q4a.y, q4a.z, q4a.w));
+            qb = qcast<R>(qt<double>(q4b.x, q4b.y, q4b.z, q4b.w));
+        } else {   // the FP32 copies the fold wrote: the same casts of the FP64 orientations
+            const float4 fa = W.pose_f[2 * ia + 1], fb = W.pose_f[2 * ib + 1];
+            qa = qt<R>(fa.x, fa.y, fa.z, fa.w);
+            qb = qt<R>(fb.x, fb.y, fb.z, fb.w);
+        }
         R sa[6], sb[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) { sa[i] = W.inv_inertia[6 * ia + i]; sb[i] = W.inv_inertia[6 * ib + i]; }
@@ -1283,7 +1289,10 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
     mark(PH_SCHEDULE);
     const int e0 = W.scene_ext[s], e1 = W.scene_ext[s + 1];
     for (int sub = 0; sub < P.num_substeps; ++sub) {
-        for (int b = b0 + g.rank(); b < b1; b += g.size()) predict_body<R, EXACT>(W, b, h);
+        for (int b = b0 + g.rank(); b < b1; b += g.size()) {
+            predict_body<R, EXACT>(W, b, h);
+            if constexpr (!EXACT) stage_body(W, b);
+        }
         for (int e = e0 + g.rank(); e < e1; e += g.size())
             for (int k = 0; k < 4; ++k) W.ext_lambda[4 * (size_t)e + k] = 0.0;
         if (g.rank() == 0) {
@@ -1310,7 +1319,10 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
         mark(PH_SCHEDULE);
         for (int it = 0; it < P.num_pos_iters; ++it) sweep_levels<R, EXACT, false>(W, g, s, hR);
         mark(PH_SOLVE);
-        for (int b = b0 + g.rank(); b < b1; b += g.size()) velocity_body<R, EXACT>(W, b, h);
+        for (int b = b0 + g.rank(); b < b1; b += g.size()) {
+            if constexpr (!EXACT) fold_body(W, b);
+            velocity_body<R, EXACT>(W, b, h);
+        }
         g.sync();
         mark(PH_VELOCITY);
         sweep_levels<R, EXACT, true>(W, g, s, hR);

@@ -177,7 +177,11 @@ struct WorldView {
     // ---- phase-major pipeline (one kernel per phase over every scene of the batch) ----------
     const int32_t* body_scene;   // [N] scene of each body
     float4* pose_f;              // [2N] FP32 copy of the predicted pose (xyz, 0), (quaternion), written
-                                 // by the predict kernel for the narrowphase's bounds test
+                                 // by the predict phase (the orientation refreshed by the fold)
+    float4* sdx;                 // [N] FP32 build: the position sweep's accumulated position correction
+    float4* sdq;                 // [N]                 and orientation correction (delta form)
+    float4* pred_d;              // [N] FP32 build: (float)(predicted position - previous position)
+    float4* prev_qf;             // [N]             (float) previous orientation
     const int32_t* col_body;     // [colliders] body of each collider
     int32_t* work_list;          // [pair capacity] global pair slots narrowphased this frame
     int32_t* work_state;         // [pair capacity] per work item: WS_* below
