@@ -384,14 +384,15 @@ def e2e_frames(w, stream, flush, start_state, frames):
     b0 = w.transfer_bytes()
     torch.cuda.synchronize()
     wall = 0.0
+    buf = np.array(st, dtype=np.float64, order="C")    # the caller's state array, reused every frame
     for k in range(frames):
         with torch.cuda.stream(stream):
             flush.fill_(k & 0xff)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        w.set_state(st)
+        w.set_state(buf)
         w.step(1)
-        st = w.get_state()
+        w.get_state(out=buf)
         wall += time.perf_counter() - t
     b1 = w.transfer_bytes()
     return wall, (b1[0] - b0[0]) // frames, (b1[1] - b0[1]) // frames

@@ -135,9 +135,11 @@ rp_status rp_world_set_wait_limit(rp_world* w, uint64_t microseconds);
 /* Autotuner (no counterpart in the reference): times `frames` frames of the world's current scenes
  * from their current state under each candidate launch configuration — launch mode, threads per
  * collider in the hull transform (4/8/16/32), and the sweep layout (levels swept by one CTA below
- * 128..2048 nodes for one large scene; one warp or one CTA per scene for a batch) — keeps the
- * fastest, and restores the state. Every configuration gives identical results. Call it with no
- * forces pending. choice receives {mode, transform threads, CTA-per-scene sweeps, solo level size}. */
+ * 128..2048 nodes for one large scene; for a batch, which scenes a warp and which a whole CTA sweeps) —
+ * keeps the fastest, and restores the state. Every configuration gives identical results. Call it with
+ * no forces pending. choice receives {mode, transform threads, batch sweep assignment (0: a warp per
+ * scene, 1: a CTA per scene, n >= 2: a CTA for scenes of n or more bodies plus 8 per joint, a warp for
+ * the rest), solo level size}. */
 rp_status rp_autotune(rp_world* w, double dt, uint32_t num_substeps, uint32_t num_pos_iters, int32_t enable_collisions,
                       uint32_t frames, int32_t choice[4]);
 const char* rp_last_error(void);

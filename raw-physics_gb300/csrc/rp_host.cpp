@@ -14,8 +14,10 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <memory>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -155,10 +157,16 @@ struct rp_world {
     // phase-major pipeline
     DevBuf d_adj_scenes, d_adj_data, d_adj_ext;   // adjoint scratch
     HostBuf h_state;                               // pinned staging of the body state (rp_state_set / _get)
+    HostBuf h_rec;                                 // pinned staging of the state records (device-side packing)
+    DevBuf d_rec, d_slot_entity;                   // the records on the device; entity of each body slot
+    cudaEvent_t ev_rec = nullptr;                  // the last record upload (h_rec is refilled after it)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
+    int cta_from = 256;               // tunable: batched sweeps give a whole CTA to scenes of this cost or more
+    std::vector<int64_t> order_cost;  // sweep cost of the scenes in scene_order (decreasing)
+    int cta_scenes = 0;               // how many leading scenes of scene_order that is
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
     int sweep_order = RP_SWEEP_REFERENCE;   // Gauss–Seidel order of the sweeps (rp_world_set_sweep_order)
     bool pipe_ready = false;
@@ -219,6 +227,39 @@ std::vector<unsigned char> as_working(const std::vector<double>& v, size_t rsize
 }
 
 rp_status sync_state_to_host(rp_world* w);
+
+// Copies n doubles in parallel chunks (state records of a large batch are hundreds of MB: one core's
+// memcpy would dominate a frame); with `check`, also returns false if any is not finite.
+bool copy_records(double* dst, const double* src, size_t n, bool check) {
+    const size_t chunk_min = (size_t)1 << 18;
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const size_t chunks = std::max<size_t>(1, std::min<size_t>(hw, (n + chunk_min - 1) / chunk_min));
+    std::atomic<bool> ok(true);
+    auto work = [&](size_t c) {
+        const size_t lo = n * c / chunks, hi = n * (c + 1) / chunks;
+        bool good = true;
+        if (check)
+            for (size_t i = lo; i < hi; ++i) good = good && std::isfinite(src[i]);
+        if (!good) ok = false;
+        std::memcpy(dst + lo, src + lo, (hi - lo) * sizeof(double));
+    };
+    if (chunks == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (size_t c = 1; c < chunks; ++c) th.emplace_back(work, c);
+        work(0);
+        for (std::thread& t : th) t.join();
+    }
+    return ok;
+}
+
+// Scenes whose sweep cost (bodies + 8 per joint) reaches cta_from get a whole CTA in the warp sweeps.
+void set_cta_scenes(rp_world* w) {
+    int n = 0;
+    while (n < (int)w->order_cost.size() && w->cta_from > 0 && w->order_cost[(size_t)n] >= (int64_t)w->cta_from) ++n;
+    w->cta_scenes = n;
+}
 
 // (Re)build the device layout: bodies grouped by scene, shapes, colliders, constraints, scratch.
 rp_status build_device(rp_world* w) {
@@ -489,6 +530,7 @@ rp_status build_device(rp_world* w) {
         for (size_t slot = 0; slot < N; ++slot)
             for (int32_t c = col_start[slot]; c < col_start[slot + 1]; ++c) col_body[(size_t)c] = (int32_t)slot;
         RP_CUDA(upload(w->d_body_scene, body_scene, st));
+        RP_CUDA(upload(w->d_slot_entity, w->slot_to_entity, st));
         RP_CUDA(upload(w->d_col_body, col_body, st));
         RP_CUDA(w->d_pose_f.ensure(std::max<size_t>(N, 1) * 32));
         for (DevBuf* b : {&w->d_sdx, &w->d_sdq, &w->d_pred_d, &w->d_prev_qf}) {
@@ -513,6 +555,9 @@ rp_status build_device(rp_world* w) {
         };
         std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
         RP_CUDA(upload(w->d_scene_order, order, st));
+        w->order_cost.assign((size_t)S, 0);
+        for (int sc = 0; sc < S; ++sc) w->order_cost[(size_t)sc] = cost(order[(size_t)sc]);
+        set_cta_scenes(w);
         RP_CUDA(w->d_queue.ensure(64));
         RP_CUDA(cudaMemsetAsync(w->d_queue.p, 0, 64, st));
         w->dims.nbodies = (int)N;
@@ -656,6 +701,7 @@ WorldView<R> make_view(rp_world* w) {
     V.queue = w->d_queue.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
     V.solo_nodes = w->solo_nodes;
+    V.cta_scenes = w->cta_scenes;
     V.wait_ns = w->wait_ns;
     V.deg_first = w->d_deg.as<int32_t>();
     return V;
@@ -988,6 +1034,7 @@ void rp_world_destroy(rp_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     if (w->ev0) cudaEventDestroy(w->ev0);
     if (w->ev1) cudaEventDestroy(w->ev1);
+    if (w->ev_rec) cudaEventDestroy(w->ev_rec);
     if (w->graph) cudaGraphExecDestroy(w->graph);
     for (cudaEvent_t ev : w->marks) cudaEventDestroy(ev);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
@@ -1444,6 +1491,25 @@ rp_status rp_last_status(rp_world* w, uint32_t* bits) {
 
 rp_status rp_state_get(rp_world* w, double* out) {
     if (check_world(w) || (!out && !w->bodies.empty())) return fail(RP_ERR_INVALID, "null argument");
+    const size_t n = w->bodies.size();
+    if (w->device_state_valid && !w->static_dirty && n && w->d_slot_entity.p) {
+        // the device holds the state: pack the records there, one copy back, a parallel host copy
+        const size_t bytes = n * RP_STATE_DOUBLES * sizeof(double);
+        RP_CUDA(cudaSetDevice(w->device));
+        if (w->ev_rec) RP_CUDA(cudaEventSynchronize(w->ev_rec));
+        RP_CUDA(w->d_rec.ensure(bytes));
+        RP_CUDA(w->h_rec.ensure(bytes));
+        if (w->precision == RP_PRECISION_FP64)
+            RP_CUDA(state_io_f64(make_view<double>(w), w->d_rec.as<double>(), w->d_slot_entity.as<int32_t>(), (int)n, true, w->stream));
+        else
+            RP_CUDA(state_io_f32(make_view<float>(w), w->d_rec.as<double>(), w->d_slot_entity.as<int32_t>(), (int)n, true, w->stream));
+        w->launches++;
+        RP_CUDA(cudaMemcpyAsync(w->h_rec.p, w->d_rec.p, bytes, cudaMemcpyDeviceToHost, w->stream));
+        RP_CUDA(cudaStreamSynchronize(w->stream));
+        w->d2h_bytes += bytes;
+        copy_records(out, (const double*)w->h_rec.p, n * RP_STATE_DOUBLES, false);
+        return RP_OK;
+    }
     if (w->device_state_valid) {
         rp_status s = sync_state_to_host(w);
         if (s != RP_OK) return s;
@@ -1461,6 +1527,29 @@ rp_status rp_state_get(rp_world* w, double* out) {
 
 rp_status rp_state_set(rp_world* w, const double* in) {
     if (check_world(w) || (!in && !w->bodies.empty())) return fail(RP_ERR_INVALID, "null argument");
+    const size_t n = w->bodies.size();
+    if (w->device >= 0 && !w->static_dirty && n && w->d_slot_entity.p && w->d_pos.p) {
+        // a built world: the records go to the device as they are and are unpacked there; the
+        // device then holds the state (the host mirror is refreshed from it when needed)
+        const size_t bytes = n * RP_STATE_DOUBLES * sizeof(double);
+        RP_CUDA(cudaSetDevice(w->device));
+        if (w->ev_rec) RP_CUDA(cudaEventSynchronize(w->ev_rec));
+        RP_CUDA(w->h_rec.ensure(bytes));
+        RP_CUDA(w->d_rec.ensure(bytes));
+        if (!copy_records((double*)w->h_rec.p, in, n * RP_STATE_DOUBLES, true))
+            return fail(RP_ERR_INVALID, "state is not finite");
+        RP_CUDA(cudaMemcpyAsync(w->d_rec.p, w->h_rec.p, bytes, cudaMemcpyHostToDevice, w->stream));
+        if (!w->ev_rec) RP_CUDA(cudaEventCreateWithFlags(&w->ev_rec, cudaEventDisableTiming));
+        RP_CUDA(cudaEventRecord(w->ev_rec, w->stream));
+        if (w->precision == RP_PRECISION_FP64)
+            RP_CUDA(state_io_f64(make_view<double>(w), w->d_rec.as<double>(), w->d_slot_entity.as<int32_t>(), (int)n, false, w->stream));
+        else
+            RP_CUDA(state_io_f32(make_view<float>(w), w->d_rec.as<double>(), w->d_slot_entity.as<int32_t>(), (int)n, false, w->stream));
+        w->launches++;
+        w->h2d_bytes += bytes;
+        w->device_state_valid = true;
+        return RP_OK;
+    }
     for (size_t e = 0; e < w->bodies.size(); ++e) {
         const double* o = in + e * RP_STATE_DOUBLES;
         for (int k = 0; k < RP_STATE_DOUBLES; ++k)
@@ -1701,14 +1790,19 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
             return fail(RP_ERR_CUDA, "event timing");
         return RP_OK;
     };
+    // cta: how a batch's sweeps assign scenes: 1 = one CTA per scene (k_sweep_cta); 0 = one warp per
+    // scene; n >= 2 = scenes of sweep cost n or more get a whole CTA, the rest a warp each
     auto set_tune = [&](int mode, int group, int cta, int solo) {
         w->mode = mode;
         w->pipe.transform_group = group;
-        w->pipe.sweep_cta = cta;
+        w->pipe.sweep_cta = cta == 1 ? 1 : 0;
+        w->cta_from = cta == 1 ? 0 : cta;
+        set_cta_scenes(w);
         w->solo_nodes = solo;
         w->layout_gen++;   // recapture the frame graph with the new launch shapes
     };
-    int best[4] = {RP_MODE_PHASED, 8, 0, 512};
+    const int cta0 = w->pipe.sweep_cta ? 1 : w->cta_from;
+    int best[4] = {RP_MODE_PHASED, 8, cta0, 512};
     float best_ms = 0.f;
     auto consider = [&](int mode, int group, int cta, int solo) -> rp_status {
         set_tune(mode, group, cta, solo);
@@ -1722,17 +1816,19 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
         return RP_OK;
     };
     // coordinate search: launch mode, then the hull-transform group, then the sweep layout
-    s = consider(RP_MODE_PHASED, 8, 0, 512);
-    if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, 0, 512);
+    s = consider(RP_MODE_PHASED, 8, cta0, 512);
+    if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, cta0, 512);
     if (s == RP_OK && best[0] == RP_MODE_PHASED) {
         for (int g : {4, 16, 32})
-            if (s == RP_OK) s = consider(RP_MODE_PHASED, g, 0, 512);
+            if (s == RP_OK) s = consider(RP_MODE_PHASED, g, cta0, 512);
         const int g = best[1];
         if (w->grid_mode) {
             for (int solo : {128, 256, 1024, 2048})
-                if (s == RP_OK) s = consider(RP_MODE_PHASED, g, 0, solo);
-        } else if (s == RP_OK) {
-            s = consider(RP_MODE_PHASED, g, 1, 512);
+                if (s == RP_OK) s = consider(RP_MODE_PHASED, g, cta0, solo);
+        } else {
+            // the sweeps' scene assignment: every scene a warp, every scene a CTA, or the largest a CTA
+            for (int cta : {0, 1, 96, 160, 256, 384})
+                if (s == RP_OK && cta != cta0) s = consider(RP_MODE_PHASED, g, cta, 512);
         }
     } else if (s == RP_OK && w->grid_mode) {
         for (int solo : {128, 256, 1024, 2048})

@@ -4,6 +4,7 @@
 #pragma once
 #include "rp_step.cuh"
 #include "rp_launch.h"
+#include <algorithm>
 
 namespace rp {
 
@@ -60,6 +61,47 @@ __global__ void __launch_bounds__(32) contacts_kernel(WorldView<R> W, int a, int
     }
 }
 
+// rp_state_set / rp_state_get on the device: the entity-ordered 28-double records (include/rp.h,
+// RP_STATE_DOUBLES) to and from the body-slot SoA state, thread per body.
+template <typename R>
+__global__ void __launch_bounds__(256) state_unpack_kernel(WorldView<R> W, const double* rec, const int32_t* slot_entity, int n) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        const double* o = rec + 28 * (size_t)slot_entity[b];
+        W.pos[b] = make_double4_32a(o[0], o[1], o[2], 0.0);
+        W.rot[b] = make_double4_32a(o[3], o[4], o[5], o[6]);
+        W.prev_pos[b] = make_double4_32a(o[13], o[14], o[15], 0.0);
+        W.prev_rot[b] = make_double4_32a(o[16], o[17], o[18], o[19]);
+        for (int k = 0; k < 3; ++k) {
+            W.vel[3 * b + k] = (R)o[7 + k];
+            W.omega[3 * b + k] = (R)o[10 + k];
+            W.prev_vel[3 * b + k] = (R)o[20 + k];
+            W.prev_omega[3 * b + k] = (R)o[23 + k];
+        }
+        W.active[b] = o[26] != 0.0 ? 1 : 0;
+        W.deact[b] = o[27];
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) state_pack_kernel(WorldView<R> W, double* rec, const int32_t* slot_entity, int n) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        double* o = rec + 28 * (size_t)slot_entity[b];
+        const double4_32a p = W.pos[b], q = W.rot[b], pp = W.prev_pos[b], pq = W.prev_rot[b];
+        o[0] = p.x; o[1] = p.y; o[2] = p.z;
+        o[3] = q.x; o[4] = q.y; o[5] = q.z; o[6] = q.w;
+        for (int k = 0; k < 3; ++k) {
+            o[7 + k] = (double)W.vel[3 * b + k];
+            o[10 + k] = (double)W.omega[3 * b + k];
+            o[20 + k] = (double)W.prev_vel[3 * b + k];
+            o[23 + k] = (double)W.prev_omega[3 * b + k];
+        }
+        o[13] = pp.x; o[14] = pp.y; o[15] = pp.z;
+        o[16] = pq.x; o[17] = pq.y; o[18] = pq.z; o[19] = pq.w;
+        o[26] = W.active[b] ? 1.0 : 0.0;
+        o[27] = W.deact[b];
+    }
+}
+
 template <typename R, bool EXACT>
 struct Launcher {
     static size_t smem_bytes() { return sizeof(NarrowSmem<R>) * WARPS_PER_BLOCK; }
@@ -98,6 +140,15 @@ struct Launcher {
             return cudaLaunchCooperativeKernel((const void*)broad_grid_kernel<R>, dim3(grid_blocks), dim3(BLOCK), args, 0, st);
         }
         broad_kernel<R><<<1, BLOCK, 0, st>>>(W, s);
+        return cudaGetLastError();
+    }
+
+    static cudaError_t state_io(const WorldView<R>& W, double* rec, const int32_t* slot_entity, int n, bool pack,
+                                cudaStream_t st) {
+        if (n <= 0) return cudaSuccess;
+        const int blocks = std::min((n + 255) / 256, 4096);
+        if (pack) state_pack_kernel<R><<<blocks, 256, 0, st>>>(W, rec, slot_entity, n);
+        else state_unpack_kernel<R><<<blocks, 256, 0, st>>>(W, rec, slot_entity, n);
         return cudaGetLastError();
     }
 

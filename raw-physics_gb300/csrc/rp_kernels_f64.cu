@@ -11,6 +11,9 @@ cudaError_t step_f64(const WorldView<double>& W, const StepParams& P, bool grid,
 cudaError_t broad_f64(const WorldView<double>& W, int scene, int grid_blocks, cudaStream_t st) {
     return Launcher<double, true>::broad(W, scene, grid_blocks, st);
 }
+cudaError_t state_io_f64(const WorldView<double>& W, double* rec, const int32_t* slot_entity, int n, bool pack, cudaStream_t st) {
+    return Launcher<double, true>::state_io(W, rec, slot_entity, n, pack, st);
+}
 cudaError_t contacts_f64(const WorldView<double>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st) {
     return Launcher<double, true>::contacts(W, a, b, out, cap, count, st);
 }

@@ -34,6 +34,7 @@ struct PipeMarks {
     cudaError_t step_##SUF(const WorldView<R>& W, const StepParams& P, bool grid, int blocks, cudaStream_t st); \
     cudaError_t broad_##SUF(const WorldView<R>& W, int scene, int grid_blocks, cudaStream_t st);              \
     cudaError_t contacts_##SUF(const WorldView<R>& W, int a, int b, double* out, int cap, int* count, cudaStream_t st); \
+    cudaError_t state_io_##SUF(const WorldView<R>& W, double* rec, const int32_t* slot_entity, int n, bool pack, cudaStream_t st); \
     cudaError_t pipe_configure_##SUF(PipeConfig& c, int sms);                                                 \
     cudaError_t pipe_frame_##SUF(const WorldView<R>& W, const StepParams& P, const PipeConfig& c, const PipeDims& d, \
                                  cudaStream_t st, PipeMarks* marks);                                          \

@@ -733,25 +733,52 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
 template <typename R, bool EXACT, bool VELOCITY>
 __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
-    WarpGroup g;
-    const int lane = threadIdx.x & 31;
+    __shared__ SerialSmem ssm[VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32];
+    __shared__ int s_next, s_ok;
+    // the W.cta_scenes largest scenes first, each swept by a whole CTA (queue[6] hands them out), so
+    // the biggest scenes do not leave one warp finishing alone; then one warp per scene (queue[1])
     for (;;) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(&W.queue[1], 1);
-        i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= W.num_scenes) break;
+        if (threadIdx.x == 0) s_next = atomicAdd(&W.queue[6], 1);
+        __syncthreads();
+        const int i = s_next;
+        __syncthreads();
+        if (i >= W.cta_scenes) break;
         const int s = W.scene_order[i];
-        if constexpr (!VELOCITY) {
-            __shared__ SerialSmem ssm[SWEEP_WARP_BLOCK / 32];
-            if (resched_first) {
-                if (resched_serial(W, s, ssm[threadIdx.x >> 5])) {
+        CtaGroup cg;
+        if (!VELOCITY && resched_first) {
+            if (threadIdx.x < 32) {
+                const bool ok = resched_serial(W, s, ssm[0]);
+                if (ok) {
                     SubWarp q;
                     const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
                     bucket_schedule(W, q, s, v0, *(volatile int*)v0.active, true);
                     bucket_schedule(W, q, s, v1, *(volatile int*)v1.active, false);
-                } else {
-                    resched(W, g, s);
                 }
+                if (threadIdx.x == 0) s_ok = ok ? 1 : 0;
+            }
+            __syncthreads();
+            if (!s_ok) resched(W, cg, s);
+            __syncthreads();
+        }
+        sweep_levels<R, EXACT, VELOCITY>(W, cg, s, (R)h);
+        __syncthreads();
+    }
+    WarpGroup g;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = W.cta_scenes + atomicAdd(&W.queue[1], 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= W.num_scenes) break;
+        const int s = W.scene_order[i];
+        if (!VELOCITY && resched_first) {
+            if (resched_serial(W, s, ssm[(threadIdx.x >> 5) % (VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32)])) {
+                SubWarp q;
+                const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
+                bucket_schedule(W, q, s, v0, *(volatile int*)v0.active, true);
+                bucket_schedule(W, q, s, v1, *(volatile int*)v1.active, false);
+            } else {
+                resched(W, g, s);
             }
         }
         sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
@@ -829,6 +856,7 @@ struct PipeLauncher {
     template <bool VELOCITY>
     static cudaError_t sweep_warp(const WorldView<R>& W, const PipeConfig& c, cudaStream_t st, double h, int first) {
         cudaError_t e = cudaMemsetAsync(W.queue + 1, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(W.queue + 6, 0, sizeof(int32_t), st);
         if (e != cudaSuccess) return e;
         k_sweep_warp<R, EXACT, VELOCITY><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h, first);
         return cudaGetLastError();

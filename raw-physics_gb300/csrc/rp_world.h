@@ -197,8 +197,10 @@ struct WorldView {
                                  //     and its FP32 normal, finished in FP64 by k_epa_finish
     int32_t* queue;              // [16] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
                                  //     [2] gjk_list length, [3] hit_list length, [4] substeps run since
-                                 //     the world was built (phase-major form), [5] fallback_list length
+                                 //     the world was built (phase-major form), [5] fallback_list length,
+                                 //     [6] next of the CTA-swept scenes
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
+    int32_t cta_scenes;          // the first cta_scenes of scene_order are swept by a whole CTA each
     int32_t max_colliders_per_body;
     int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
     // ---- control ----------------------------------------------------------------------------

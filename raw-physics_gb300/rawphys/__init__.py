@@ -335,8 +335,11 @@ class World:
     def num_entities(self) -> int:
         return int(self.lib.rp_num_entities(self.h))
 
-    def get_state(self) -> np.ndarray:
-        out = np.zeros((self.num_entities(), STATE_DOUBLES))
+    def get_state(self, out: np.ndarray = None) -> np.ndarray:
+        """The state records (RP_STATE_DOUBLES per entity); into `out` when given (no allocation)."""
+        if out is None:
+            out = np.empty((self.num_entities(), STATE_DOUBLES))
+        assert out.shape == (self.num_entities(), STATE_DOUBLES) and out.dtype == np.float64 and out.flags.c_contiguous
         self._check(self.lib.rp_state_get(self.h, _dp(out)))
         return out
 
@@ -472,7 +475,8 @@ class World:
         self._check(self.lib.rp_autotune(self.h, float(s.dt), int(s.substeps), int(s.pos_iters), int(bool(s.collisions)),
                                          int(frames), out))
         modes = {v: k for k, v in self.MODES.items()}
-        return {"mode": modes.get(out[0], out[0]), "transform_threads": out[1], "cta_per_scene_sweeps": bool(out[2]),
+        return {"mode": modes.get(out[0], out[0]), "transform_threads": out[1],
+                "batch_sweep_assignment": {0: "warp per scene", 1: "CTA per scene"}.get(out[2], "CTA for scenes of cost >= %d" % out[2]),
                 "solo_level_nodes": out[3]}
 
     def counters(self):
