@@ -9,7 +9,7 @@ namespace rp {
 // Launch shapes of the phase-major pipeline, chosen once per device (occupancy) and per world.
 struct PipeConfig {
     int sms = 0;
-    int cull_blocks = 0, gjk_blocks = 0, epa_blocks = 0, manifold_blocks = 0;
+    int cull_blocks = 0, gjk_blocks = 0, epa_blocks = 0, manifold_blocks = 0, general_blocks = 0;
     int setup_grid_blocks = 0, sweep_grid_blocks = 0, vsweep_grid_blocks = 0, sweep_warp_blocks = 0;
     // tunable (rp_autotune): results do not depend on them
     int transform_group = 8;     // threads per collider in the hull transform

@@ -11,6 +11,7 @@
 // References (raw-physics): support.cpp:5-39, gjk.cpp:7-379, epa.cpp:8-237, clipping.cpp:12-370,
 // collider.cpp:523-571.
 #pragma once
+#include <type_traits>
 #include <float.h>
 #include "rp_math.cuh"
 #include "rp_world.h"
@@ -27,21 +28,47 @@ constexpr int CMAX = 64;         // contacts of one body pair
 
 // Precision policy. R: working type of geometry and solver. EPA face normals, distances and the
 // termination test are always FP64.
+// EPA of the FP32 build. 1 (default): polytope faces and the closest-face search in FP32, the
+// termination test and the returned normal and depth in FP64 (the closest face re-evaluated from its
+// three Minkowski points every iteration). 0: every face normal and distance in FP64, which on GB300
+// (FP64 at 1/64 of the FP32 rate) made EPA the most expensive part of the batched narrowphase.
+#ifndef RP_EPA_FAST
+#define RP_EPA_FAST 1
+#endif
+constexpr bool kEpaFast = RP_EPA_FAST != 0;
+
 template <bool EXACT> struct Prec;
 template <> struct Prec<false> { typedef float R; static constexpr bool exact = false; };
 template <> struct Prec<true> { typedef double R; static constexpr bool exact = true; };
+
+// The FP32 build's EPA polytope (epa_fast): FP32 points, face normals and distances; the closest
+// face is re-evaluated in FP64 before it is returned.
+template <typename R>
+struct EpaFastSmem {
+    V3<float> poly[EPA_MAXV];
+    V3<float> fn[EPA_MAXF];
+    float fd[EPA_MAXF];
+    uchar4 f[EPA_MAXF];
+    uchar2 edge[3 * WARP];   // edges of this iteration's visible faces
+    uchar2 hz[3 * WARP];     // the horizon
+};
+
+// The exact build's EPA polytope (epa): FP64 face normals and distances.
+template <typename R>
+struct EpaExactSmem {
+    V3<R> poly[EPA_MAXV];
+    V3<double> fn[EPA_MAXF];
+    double fd[EPA_MAXF];
+    uchar4 f[EPA_MAXF];      // x, y, z polytope indices, w = visibility
+};
 
 template <typename R>
 struct NarrowSmem {
     V3<R> va[STAGE_V];
     V3<R> vb[STAGE_V];
     union U {
-        struct {
-            V3<R> poly[EPA_MAXV];
-            V3<double> fn[EPA_MAXF];
-            double fd[EPA_MAXF];
-            uchar4 f[EPA_MAXF];      // x, y, z polytope indices, w = visibility
-        } epa;
+        // the FP32 build runs epa_fast only, so its scratch holds the FP32 polytope
+        typename std::conditional<std::is_same<R, float>::value && (RP_EPA_FAST != 0), EpaFastSmem<R>, EpaExactSmem<R>>::type epa;
         struct {
             V3<R> buf[2][CLIP_MAX];
             V3<R> pn[CLIP_MAX];      // clip planes: normal
@@ -530,16 +557,6 @@ __device__ bool epa(NarrowSmem<R>& sm, const ColView<R>& c1, const ColView<R>& c
 // toggling add_edge leaves; surviving faces keep their relative order and new faces follow in
 // horizon order, so only exact ties in the closest-face search can resolve differently. The
 // closest face is re-evaluated in FP64 before it is returned.
-template <typename R>
-struct EpaFastSmem {
-    V3<float> poly[EPA_MAXV];
-    V3<float> fn[EPA_MAXF];
-    float fd[EPA_MAXF];
-    uchar4 f[EPA_MAXF];
-    uchar2 edge[3 * WARP];   // edges of this iteration's visible faces
-    uchar2 hz[3 * WARP];     // the horizon
-};
-
 __device__ __forceinline__ void epa_face_f32(const V3<float>* poly, int npoly, uchar4 f, V3<float>& n_out, float& d_out, int& status) {
     V3<float> a = poly[f.x], b = poly[f.y], c = poly[f.z];
     const V3<float> e1 = vsub(b, a), e2 = vsub(c, a), cr = vcross(e1, e2);
@@ -1039,14 +1056,7 @@ __device__ void contact_manifold(NarrowSmem<R>& sm, const WorldView<R>& W, const
     }
 }
 
-// EPA of the FP32 build. 1 (default): polytope faces and the closest-face search in FP32, the
-// termination test and the returned normal and depth in FP64 (the closest face re-evaluated from its
-// three Minkowski points every iteration). 0: every face normal and distance in FP64, which on GB300
-// (FP64 at 1/64 of the FP32 rate) made EPA the most expensive part of the batched narrowphase.
-#ifndef RP_EPA_FAST
-#define RP_EPA_FAST 1
-#endif
-constexpr bool kEpaFast = RP_EPA_FAST != 0;
+
 
 // collider_get_contacts (collider.cpp:523-558)
 template <typename R, bool EXACT>
@@ -1080,7 +1090,9 @@ __device__ void collider_contacts(NarrowSmem<R>& sm, const WorldView<R>& W, cons
     if (!hit) return;
     V3<double> n;
     double pen;
-    bool ok = (EXACT || !kEpaFast) ? epa(sm, c1, c2, s, n, pen, ei) : epa_fast(sm, c1, c2, s, n, pen, ei);
+    bool ok;
+    if constexpr (EXACT || !kEpaFast) ok = epa(sm, c1, c2, s, n, pen, ei);
+    else ok = epa_fast(sm, c1, c2, s, n, pen, ei);
     const long long t2 = clock64();
     if (counters && lane_id() == 0) {
         atomicAdd(&counters[1], (unsigned long long)ei);

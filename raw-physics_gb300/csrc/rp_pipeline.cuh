@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 3) k_gjk(WorldView<R> W) {
 }
 
 template <typename R, bool EXACT>
-__global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
+__global__ void __launch_bounds__(PIPE_BLOCK, EXACT ? 2 : 3) k_epa(WorldView<R> W) {
     if (frame_abandoned(W.status)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
@@ -380,9 +380,9 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_epa(WorldView<R> W) {
             const long long t0 = clock64();
             long long tsup = 0;
             bool deferred = false;
-            const bool ok = (EXACT || !kEpaFast) ? epa(sm, va, vb, sx, nrm, pen, ei)
-                                                 : epa_fast(sm, va, vb, sx, nrm, pen, ei, &tsup,
-                                                            W.work_face + 12 * (size_t)k, &deferred);
+            bool ok;
+            if constexpr (EXACT || !kEpaFast) ok = epa(sm, va, vb, sx, nrm, pen, ei);
+            else ok = epa_fast(sm, va, vb, sx, nrm, pen, ei, &tsup, W.work_face + 12 * (size_t)k, &deferred);
             t.v[0] += ei;
             t.v[1] += 1;
             t.v[2] += clock64() - t0;
@@ -450,8 +450,11 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_epa_finish(WorldView<R> W) {
     }
 }
 
-template <typename R, bool EXACT>
-__global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
+// GENERAL: the pairs of the general path (compound bodies, sphere colliders: the whole
+// colliders_get_contacts per pair); otherwise the contact manifolds of the EPA hits. Two instantiations
+// keep the common kernel's code and registers free of the general path.
+template <typename R, bool EXACT, bool GENERAL>
+__global__ void __launch_bounds__(PIPE_BLOCK, (GENERAL || EXACT) ? 2 : 3) k_manifold(WorldView<R> W) {
     if (frame_abandoned(W.status)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     NarrowSmem<R>& sm = reinterpret_cast<NarrowSmem<R>*>(dyn_smem)[threadIdx.x >> 5];
@@ -462,7 +465,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
     for (int j = gw; j < n; j += nw) {
         const int k = W.hit_list[j];
         const int st = W.work_state[k];
-        if (st != WS_EPA_OK && st != WS_GENERAL) continue;
+        if (st != (GENERAL ? WS_GENERAL : WS_EPA_OK)) continue;
         {
             const int gp = W.work_list[k];
             const int2 pr = W.pairs[gp];
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
             const int s = W.body_scene[a];
             const long long t0 = clock64();
             long long t1 = t0;
-            if (st == WS_GENERAL) {
+            if constexpr (GENERAL) {
                 pair_contacts<R, EXACT>(W, sm, a, b, false);
             } else {
                 if (lane == 0) { sm.ncontacts = 0; sm.status = 0; }
@@ -492,7 +495,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, 2) k_manifold(WorldView<R> W) {
             const long long t2 = clock64();
             t.v[1] += t2 - t0;
             t.v[2] += t1 - t0;
-            if (!EXACT && st == WS_EPA_OK && (sm.status & ST_DEG_SKEW)) {
+            if (!EXACT && !GENERAL && (sm.status & ST_DEG_SKEW)) {
                 if (lane == 0) {
                     W.work_state[k] = WS_FALLBACK;
                     W.fallback_list[atomicAdd(&W.queue[5], 1)] = k;
@@ -811,7 +814,8 @@ struct PipeLauncher {
     static cudaError_t configure(PipeConfig& c, int sms) {
         cudaError_t e = cudaFuncSetAttribute(k_gjk<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gjk_smem());
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_epa<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_manifold<R, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_manifold<R, EXACT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_manifold<R, EXACT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem());
         if (e == cudaSuccess && !EXACT)
             e = cudaFuncSetAttribute(k_fallback<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fallback_smem());
         if (e != cudaSuccess) return e;
@@ -825,8 +829,10 @@ struct PipeLauncher {
         c.gjk_blocks = nb * sms;
         nb = occ((const void*)k_epa<R, EXACT>, PIPE_BLOCK, narrow_smem());
         c.epa_blocks = nb * sms;
-        nb = occ((const void*)k_manifold<R, EXACT>, PIPE_BLOCK, narrow_smem());
+        nb = occ((const void*)k_manifold<R, EXACT, false>, PIPE_BLOCK, narrow_smem());
         c.manifold_blocks = nb * sms;
+        nb = occ((const void*)k_manifold<R, EXACT, true>, PIPE_BLOCK, narrow_smem());
+        c.general_blocks = nb * sms;
         c.sweep_warp_blocks = occ((const void*)k_sweep_warp<R, EXACT, false>, SWEEP_WARP_BLOCK, 0) * sms;
         c.cull_blocks = occ((const void*)k_cull<R>, PIPE_BLOCK, 0) * sms;
         // cooperative kernels: one CTA per SM keeps the grid barrier's arrival count low
@@ -902,7 +908,9 @@ struct PipeLauncher {
                     if ((e = cudaGetLastError()) != cudaSuccess) return e;
                 }
                 if ((e = mark(PH_EPA)) != cudaSuccess) return e;
-                k_manifold<R, EXACT><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
+                k_manifold<R, EXACT, false><<<c.manifold_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                k_manifold<R, EXACT, true><<<c.general_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
                 if (!EXACT) {
                     k_fallback<R><<<c.sms, 32, fallback_smem(), st>>>(W);
@@ -929,7 +937,7 @@ struct PipeLauncher {
     }
 
     static int launches_per_frame(const StepParams& P) {
-        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 5 : 7) : 1) + P.num_pos_iters + 1;
+        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 6 : 8) : 1) + P.num_pos_iters + 1;
         return 1 + P.num_substeps * per_sub;
     }
 };
