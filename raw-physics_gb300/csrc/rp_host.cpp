@@ -167,7 +167,6 @@ struct rp_world {
     int cta_from = 256;               // tunable: batched sweeps give a whole CTA to scenes of this cost or more
     std::vector<int64_t> order_cost;  // sweep cost of the scenes in scene_order (decreasing)
     int cta_scenes = 0;               // how many leading scenes of scene_order that is
-    int max_hull_verts = 0;           // largest hull of the world (on-the-fly transforms need it staged)
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
     int sweep_order = RP_SWEEP_REFERENCE;   // Gauss–Seidel order of the sweeps (rp_world_set_sweep_order)
     bool pipe_ready = false;
@@ -358,8 +357,6 @@ rp_status build_device(rp_world* w) {
         shapes.push_back(sh);
     }
     fstart.push_back((int32_t)felem.size());
-    w->max_hull_verts = 0;
-    for (const Shape& sh : shapes) w->max_hull_verts = std::max(w->max_hull_verts, (int)sh.nv);
     // colliders, transformed-geometry offsets
     std::vector<Collider> cols;
     std::vector<int32_t> col_start(N + 1, 0);
@@ -705,7 +702,6 @@ WorldView<R> make_view(rp_world* w) {
     V.scene_order = w->d_scene_order.as<int32_t>();
     V.solo_nodes = w->solo_nodes;
     V.cta_scenes = w->cta_scenes;
-    V.hull_onfly = (w->precision == RP_PRECISION_FP32 && w->max_hull_verts <= NARROW_STAGE_V) ? 1 : 0;
     V.wait_ns = w->wait_ns;
     V.deg_first = w->d_deg.as<int32_t>();
     return V;

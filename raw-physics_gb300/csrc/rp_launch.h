@@ -137,9 +137,6 @@ struct WorldHullsArgs {
 };
 cudaError_t world_hulls(const WorldHullsArgs& a, cudaStream_t st);
 
-// Hull vertices the narrowphase stages per body in shared memory (rp_narrow.cuh STAGE_V).
-constexpr int NARROW_STAGE_V = 64;
-
 // No-allocation contact query: contacts per call held by its static device scratch (rp_noalloc.cu).
 constexpr int NOALLOC_MAX_CONTACTS = 64;
 cudaError_t noalloc_scratch(int device, double** contacts, int** count);

@@ -19,7 +19,7 @@
 namespace rp {
 
 constexpr int WARP = 32;
-constexpr int STAGE_V = 64;      // hull vertices staged per body in shared memory (NARROW_STAGE_V)
+constexpr int STAGE_V = 64;      // hull vertices staged per body in shared memory
 constexpr int EPA_MAXV = 104;    // 4 simplex points + at most 100 EPA iterations
 constexpr int EPA_MAXF = 192;    // faces of the EPA polytope
 constexpr int EPA_MAXE = 64;     // horizon edges of one EPA iteration (two register slots per lane)
@@ -133,23 +133,7 @@ struct ColView {
     int nv, nf;
     const Shape* shape;
     int body;                // the body's slot (its FP64 orientation is read only for decisions made in FP64)
-    // FP32 build, phase-major form: the hull is transformed where it is used instead of by a transform
-    // pass (the same arithmetic: the orientation's FP32 matrix times the FP32 local geometry); the
-    // staged vertices already hold it and face normals are transformed on access
-    bool onfly;
-    M3<R> rot;
-    const float* lnorm;      // local face normals (FP32 copy)
 };
-
-// Face normal f of a hull in the view's frame (the transform pass's normal, collider.cpp:425-429)
-template <typename R>
-__device__ __forceinline__ V3<R> cv_norm(const ColView<R>& c, int f) {
-    if (c.onfly) {
-        const float* n = c.lnorm + 3 * f;
-        return vnorm(mmulv(c.rot, v3<R>((R)n[0], (R)n[1], (R)n[2])));
-    }
-    return c.norms[f];
-}
 
 // A face normal of a hull rotated by the body's FP64 orientation (collider_update's normal
 // transform, collider.cpp:425-429), for the FP32 build's FP64 reference-face decision.
@@ -920,19 +904,19 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
     int f1 = 0x7fffffff, f2 = 0x7fffffff;
     for (int k = (int)lane; k < csr_len<R>(cs, v2f1); k += WARP) {
         int fi = cd[cs[v2f1] + k];
-        R p = vdot(cv_norm(h1, fi), normal);
+        R p = vdot(h1.norms[fi], normal);
         if (p > best1) { best1 = p; f1 = k; }
     }
     for (int k = (int)lane; k < csr_len<R>(cs, v2f2); k += WARP) {
         int fi = cd[cs[v2f2] + k];
-        R p = vdot(cv_norm(h2, fi), inv_n);
+        R p = vdot(h2.norms[fi], inv_n);
         if (p > best2) { best2 = p; f2 = k; }
     }
     warp_argmax_first(best1, f1);
     warp_argmax_first(best2, f2);
     f1 = cd[cs[v2f1] + (f1 == 0x7fffffff ? 0 : f1)];
     f2 = cd[cs[v2f2] + (f2 == 0x7fffffff ? 0 : f2)];
-    V3<R> n1 = cv_norm(h1, f1), n2 = cv_norm(h2, f2);
+    V3<R> n1 = h1.norms[f1], n2 = h2.norms[f2];
     // get_edge_with_most_fitting_normal: candidates in (i, j, normal / inverted) order
     int v2n1 = h1.shape->v2n_off + s1, v2n2 = h2.shape->v2n_off + s2;
     int nn1 = csr_len<R>(cs, v2n1), nn2 = csr_len<R>(cs, v2n2);
@@ -1014,7 +998,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
     for (int k = (int)lane; k < npl; k += WARP) {
         int nf = cd[cs[f2n_row] + k];
         sm.u.clip.pp[k] = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + nf]]);
-        sm.u.clip.pn[k] = vinv(cv_norm(rh, nf));
+        sm.u.clip.pn[k] = vinv(rh.norms[nf]);
     }
     __syncwarp();
     int st = 0;
@@ -1024,7 +1008,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         const int m = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], sm.u.clip.pn[p], sm.u.clip.pp[p], false, st);
         if (m >= 0) { n = m; cur ^= 1; }
     }
-    V3<R> ref_n = vinv(cv_norm(rh, rf));
+    V3<R> ref_n = vinv(rh.norms[rf]);
     V3<R> ref_p = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + rf]]);
     if (n > 0) {
         const int m = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], ref_n, ref_p, true, st);

@@ -28,8 +28,6 @@
 
 namespace rp {
 
-static_assert(STAGE_V == NARROW_STAGE_V, "the host's staging bound must match the narrowphase's");
-
 constexpr int PIPE_BLOCK = 256;
 constexpr int PIPE_WARPS = PIPE_BLOCK / 32;
 
@@ -79,8 +77,8 @@ __device__ void single_views(const WorldView<R>& W, V3<R>* stage_a, V3<R>* stage
         fr.q1inv = qinverse(qt<R>(qa.x, qa.y, qa.z, qa.w));
         fr.q2inv = qinverse(qt<R>(qb.x, qb.y, qb.z, qb.w));
     }
-    va = make_view<R, EXACT>(W, W.col_start[a], EXACT ? fr.x1 : offa, offa, stage_a, a, W.hull_onfly != 0);
-    vb = make_view<R, EXACT>(W, W.col_start[b], EXACT ? fr.x2 : offb, offb, stage_b, b, W.hull_onfly != 0);
+    va = make_view<R, EXACT>(W, W.col_start[a], EXACT ? fr.x1 : offa, offa, stage_a, a);
+    vb = make_view<R, EXACT>(W, W.col_start[b], EXACT ? fr.x2 : offb, offb, stage_b, b);
 }
 
 // True when both bodies have exactly one collider, a hull whose vertices fit the staging area.
@@ -476,7 +474,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK, (GENERAL || EXACT) ? 2 : 3) k_mani
             const long long t0 = clock64();
             long long t1 = t0;
             if constexpr (GENERAL) {
-                pair_contacts<R, EXACT>(W, sm, a, b, false, W.hull_onfly != 0);
+                pair_contacts<R, EXACT>(W, sm, a, b, false);
             } else {
                 if (lane == 0) { sm.ncontacts = 0; sm.status = 0; }
                 __syncwarp();
@@ -582,8 +580,6 @@ __global__ void __launch_bounds__(32) k_fallback(WorldView<R> W) {
             c.nf = sh->nf;
             c.shape = sh;
             c.body = body;
-            c.onfly = false;
-            c.lnorm = nullptr;
         }
         PairFrame<double, true> fr;
         fr.raw = false;
@@ -896,7 +892,7 @@ struct PipeLauncher {
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(W.node_bits, 0, (size_t)d.node_words * 4, st)) != cudaSuccess) return e;
             if ((e = mark(PH_PREDICT)) != cudaSuccess) return e;
-            if (P.enable_collisions && !W.hull_onfly) {
+            if (P.enable_collisions) {
                 k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0, c.transform_group);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
             }
@@ -941,7 +937,7 @@ struct PipeLauncher {
     }
 
     static int launches_per_frame(const StepParams& P) {
-        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 6 : 7) : 1) + P.num_pos_iters + 1;
+        const int per_sub = 2 + (P.enable_collisions ? (EXACT ? 6 : 8) : 1) + P.num_pos_iters + 1;
         return 1 + P.num_substeps * per_sub;
     }
 };

@@ -927,12 +927,9 @@ __device__ void transform_hulls(const WorldView<R>& W, const G& g, int s, bool i
 // ---------------------------------------------------------------------------------------------
 // Narrowphase: one warp per broad-phase pair
 template <typename R, bool EXACT>
-__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged, int body,
-                                bool onfly = false) {
+__device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<R> off, const V3<R>* staged, int body) {
     ColView<R> v;
     v.body = body;
-    v.onfly = false;
-    v.lnorm = nullptr;
     const Collider col = W.colliders[ci];
     v.type = col.type;
     v.radius = (R)col.radius;
@@ -950,19 +947,7 @@ __device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<
         v.nf = v.shape->nf;
         v.verts = (const V3<R>*)(W.tverts) + col.tv_off;
         v.norms = (const V3<R>*)(W.tnorms) + col.tn_off;
-        if (!EXACT && onfly && staged && v.nv <= STAGE_V) {
-            // transform here (the FP32 build's transform pass, k_transform, is then not run)
-            const float4 q = W.pose_f[2 * body + 1];
-            v.rot = qmat3(qt<R>((R)q.x, (R)q.y, (R)q.z, (R)q.w));
-            v.lnorm = W.face_normal_f + 3 * v.shape->face_off;
-            v.onfly = true;
-            const float* lv = W.shape_verts_f + 3 * v.shape->vert_off;
-            for (int i = (int)lane_id(); i < v.nv; i += 32)
-                ((V3<R>*)staged)[i] = vadd(mmulv(v.rot, v3<R>((R)lv[3 * i], (R)lv[3 * i + 1], (R)lv[3 * i + 2])), off);
-            __syncwarp();
-            v.verts = staged;
-            v.staged = true;
-        } else if (staged && v.nv <= STAGE_V) {
+        if (staged && v.nv <= STAGE_V) {
             for (int i = (int)lane_id(); i < v.nv; i += 32) ((V3<R>*)staged)[i] = vadd(v.verts[i], off);
             __syncwarp();
             v.verts = staged;
@@ -974,7 +959,7 @@ __device__ ColView<R> make_view(const WorldView<R>& W, int ci, V3<R> center, V3<
 
 // colliders_get_contacts for one body pair (collider.cpp:560-571); contacts land in sm.
 template <typename R, bool EXACT>
-__device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, int b, bool raw, bool onfly = false) {
+__device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, int b, bool raw) {
     if (lane_id() == 0) { sm.ncontacts = 0; sm.status = 0; }
     __syncwarp();
     double4_32a pa = W.pos[a], pb = W.pos[b], qa4 = W.rot[a], qb4 = W.rot[b];
@@ -998,9 +983,9 @@ __device__ void pair_contacts(const WorldView<R>& W, NarrowSmem<R>& sm, int a, i
     for (int ca = ca0; ca < ca1; ++ca) {
         // exact build: stored vertices are world coordinates, sphere centres the body positions;
         // FP32 build: stored vertices are rotated about the body origin, the frame origin is body a
-        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va, a, onfly);
+        ColView<R> va = make_view<R, EXACT>(W, ca, EXACT ? fr.x1 : offa, offa, sm.va, a);
         for (int cb = cb0; cb < cb1; ++cb) {
-            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb, b, onfly);
+            ColView<R> vb = make_view<R, EXACT>(W, cb, EXACT ? fr.x2 : offb, offb, sm.vb, b);
             collider_contacts<R, EXACT>(sm, W, va, vb, fr, W.counters);
             __syncwarp();
         }

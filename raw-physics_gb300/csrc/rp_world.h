@@ -201,8 +201,6 @@ struct WorldView {
                                  //     [6] next of the CTA-swept scenes
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
     int32_t cta_scenes;          // the first cta_scenes of scene_order are swept by a whole CTA each
-    int32_t hull_onfly;          // FP32 build, phase-major form: hulls are transformed where the narrowphase
-                                 //     stages them (every hull fits the staging), no transform pass
     int32_t max_colliders_per_body;
     int32_t solo_nodes;          // grid sweeps: levels of at most this many nodes run on CTA 0 alone
     // ---- control ----------------------------------------------------------------------------
