@@ -132,15 +132,15 @@ def measured_peak_hbm():
 def profile_traffic(summary, kernel):
     """DRAM bytes per launch of `kernel` from a committed ncu summary (a line
     `traffic_bytes_per_launch[<kernel>]: <bytes>`), or None with the reason."""
-    path = os.path.join(ROOT, "profiles", summary)
+    rel = "profiles/" + summary
     key = "traffic_bytes_per_launch[%s]:" % kernel
     try:
-        for line in open(path):
+        for line in open(os.path.join(ROOT, rel)):
             if line.startswith(key):
-                return float(line.split(":", 1)[1]), path
+                return float(line.split(":", 1)[1]), rel
     except OSError:
-        return None, "missing " + path
-    return None, "no %s line in %s" % (key, path)
+        return None, "missing " + rel
+    return None, "no %s line in %s" % (key, rel)
 
 
 # ---------------------------------------------------------------------------------------------

@@ -658,10 +658,13 @@ constexpr int SWEEP_WARP_BLOCK = 128;
 // dependent step (a 64-link chain would take 64). Scenes beyond the shared tables take resched.
 constexpr int SERIAL_MAX_BODIES = 512;
 constexpr int SERIAL_MAX_WORDS = 256;   // node bitmap words staged per warp (8192 nodes)
+constexpr int SERIAL_MAX_LEVELS = 256;  // levels (colours) counted in shared memory
 struct SerialSmem {
-    uint64_t mask[SERIAL_MAX_BODIES];   // coloured: colours used per body (position sweep)
+    uint64_t mask[SERIAL_MAX_BODIES];   // per body: 1 + latest level, or the colours used (position sweep)
     uint64_t vmask[SERIAL_MAX_BODIES];  // (velocity sweep)
     uint32_t words[SERIAL_MAX_WORDS + 2];
+    int cnt[2][SERIAL_MAX_LEVELS];      // nodes per level, then the fill cursors
+    int n[2], L[2], overflow;
 };
 
 template <typename R>
@@ -682,6 +685,7 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
     for (int l = lane; l <= used1; l += 32) { v1.count[l] = 0; v1.fill[l] = 0; }
     for (int b = lane; b < nb; b += 32) { sm.mask[b] = 0ull; sm.vmask[b] = 0ull; }
     for (int w = lane; w < w1 - w0; w += 32) sm.words[w] = W.node_bits[w0 + w];
+    for (int l = lane; l < SERIAL_MAX_LEVELS; l += 32) { sm.cnt[0][l] = 0; sm.cnt[1][l] = 0; }
     __syncwarp();
     if (lane == 0) {
         // per body: reference order keeps 1 + its latest level (0: none yet), coloured order the set
@@ -712,8 +716,16 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
                 const SchedView<R>& v = which ? v1 : v0;
                 v.lev[k] = l;
                 v.list[which ? n1++ : n0++] = k;
+                if (l < SERIAL_MAX_LEVELS) {
+                    sm.cnt[which][l]++;
+                    sm.L[which] = max(sm.L[which], l + 1);
+                } else {
+                    sm.overflow = 1;
+                }
             }
         };
+        sm.L[0] = sm.L[1] = 0;
+        sm.overflow = 0;
         for (int k = 0; k < ne; ++k) place(k, false);
         for (int w = 0; w < w1 - w0; ++w) {
             uint32_t bits = sm.words[w];
@@ -724,12 +736,44 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
                 if (k >= ne && k < nn) place(k, true);
             }
         }
+        sm.n[0] = n0;
+        sm.n[1] = n1;
         *v0.active = n0;
         *v1.active = n1;
         *v0.levels = 0;
         *v1.levels = 0;
     }
     __syncwarp();
+    if (sm.overflow) return false;
+    // bucket by level from the shared counts: prefix (the level table the sweep reads), then every
+    // lane places list entries at its level's cursor (shared-memory atomics)
+    for (int which = 0; which < 2; ++which) {
+        const SchedView<R>& v = which ? v1 : v0;
+        const int L = sm.L[which], n = sm.n[which];
+        int carry = 0;
+        for (int base = 0; base < L; base += 32) {
+            const int l = base + lane;
+            const int c = l < L ? sm.cnt[which][l] : 0;
+            const int incl = warp_incl_scan(c);
+            if (l < L) {
+                v.count[l] = carry + incl - c;
+                sm.cnt[which][l] = carry + incl - c;
+            }
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) {
+            v.count[L] = carry;
+            *v.levels = L;
+            if (which == 0) atomicAdd(&W.counters[6], (unsigned long long)L);
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            const int k = v.list[i];
+            const int l = v.lev[k];
+            v.nodes[atomicAdd(&sm.cnt[which][l], 1)] = k;
+        }
+        __syncwarp();
+    }
     return true;
 }
 
@@ -751,12 +795,6 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
         if (!VELOCITY && resched_first) {
             if (threadIdx.x < 32) {
                 const bool ok = resched_serial(W, s, ssm[0]);
-                if (ok) {
-                    SubWarp q;
-                    const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
-                    bucket_schedule(W, q, s, v0, *(volatile int*)v0.active, true);
-                    bucket_schedule(W, q, s, v1, *(volatile int*)v1.active, false);
-                }
                 if (threadIdx.x == 0) s_ok = ok ? 1 : 0;
             }
             __syncthreads();
@@ -775,14 +813,7 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
         if (i >= W.num_scenes) break;
         const int s = W.scene_order[i];
         if (!VELOCITY && resched_first) {
-            if (resched_serial(W, s, ssm[(threadIdx.x >> 5) % (VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32)])) {
-                SubWarp q;
-                const SchedView<R> v0 = sched_view(W, s, 0), v1 = sched_view(W, s, 1);
-                bucket_schedule(W, q, s, v0, *(volatile int*)v0.active, true);
-                bucket_schedule(W, q, s, v1, *(volatile int*)v1.active, false);
-            } else {
-                resched(W, g, s);
-            }
+            if (!resched_serial(W, s, ssm[(threadIdx.x >> 5) % (VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32)])) resched(W, g, s);
         }
         sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
         __syncwarp();
