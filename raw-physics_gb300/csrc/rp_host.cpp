@@ -161,7 +161,7 @@ struct rp_world {
     DevBuf d_rec, d_slot_entity;                   // the records on the device; entity of each body slot
     cudaEvent_t ev_rec = nullptr;                  // the last record upload (h_rec is refilled after it)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
-    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback;
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     int cta_from = 256;               // tunable: batched sweeps give a whole CTA to scenes of this cost or more
@@ -292,6 +292,8 @@ rp_status build_device(rp_world* w) {
             ExtConstraint c = x.c;
             c.e1 = w->bodies[(size_t)c.e1].slot;
             c.e2 = w->bodies[(size_t)c.e2].slot;
+            for (int k = 0; k < 3; ++k) { c.r1f[k] = (float)c.r1[k]; c.r2f[k] = (float)c.r2[k]; }
+            c.compliance_f = (float)c.compliance;
             ext[(size_t)ef[(size_t)x.scene]++] = c;
         }
     }
@@ -560,6 +562,10 @@ rp_status build_device(rp_world* w) {
         set_cta_scenes(w);
         RP_CUDA(w->d_queue.ensure(64));
         RP_CUDA(cudaMemsetAsync(w->d_queue.p, 0, 64, st));
+        // transform-list stamps restart with the substep counter
+        RP_CUDA(w->d_tstamp.ensure(std::max<size_t>(N, 1) * 4));
+        RP_CUDA(cudaMemsetAsync(w->d_tstamp.p, 0, std::max<size_t>(N, 1) * 4, st));
+        RP_CUDA(w->d_tlist.ensure(std::max<size_t>(N, 1) * 4));
         w->dims.nbodies = (int)N;
         w->dims.ncolliders = (int)cols.size();
         w->dims.next = (int)E;
@@ -699,6 +705,8 @@ WorldView<R> make_view(rp_world* w) {
     V.fallback_list = w->d_fallback.as<int32_t>();
     V.work_face = w->d_work_face.as<float>();
     V.queue = w->d_queue.as<int32_t>();
+    V.tstamp = w->d_tstamp.as<int32_t>();
+    V.tlist = w->d_tlist.as<int32_t>();
     V.scene_order = w->d_scene_order.as<int32_t>();
     V.solo_nodes = w->solo_nodes;
     V.cta_scenes = w->cta_scenes;
@@ -1906,6 +1914,8 @@ rp_status rp_adjoint_trajectory(rp_world* w, double dt, uint32_t substeps, uint3
             ExtConstraint c = x.c;
             c.e1 = w->bodies[(size_t)c.e1].slot;
             c.e2 = w->bodies[(size_t)c.e2].slot;
+            for (int k = 0; k < 3; ++k) { c.r1f[k] = (float)c.r1[k]; c.r2f[k] = (float)c.r2[k]; }
+            c.compliance_f = (float)c.compliance;
             ext.push_back(c);
         }
     }

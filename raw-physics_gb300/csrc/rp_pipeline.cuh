@@ -200,23 +200,26 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
         W.act_count[2 * s] = 0;
         W.act_count[2 * s + 1] = 0;
     }
-    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; W.queue[5] = 0; }
+    if (t == 0) { W.queue[2] = 0; W.queue[3] = 0; W.queue[4] += 1; W.queue[5] = 0; W.queue[7] = 0; }
 }
 
-// `group` threads per collider (a power of two up to 32; 8 by default: the typical hull has 8-64
-// vertices, so a whole warp per collider would leave most lanes idle).
+// The hulls of the bodies k_cull listed for this substep (tlist: bodies of the pairs that go on to
+// GJK or the general path; the narrowphase reads no other transformed hull), `group` threads per
+// collider (a power of two up to 32; 8 by default: the typical hull has 8-64 vertices, so a whole
+// warp per collider would leave most lanes idle).
 template <typename R, bool EXACT>
-__global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int ncolliders, int include_fixed, int group) {
+__global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int group) {
     if (frame_abandoned(W.status)) return;
     const int sub = threadIdx.x % group;
     const int gi = (blockIdx.x * blockDim.x + threadIdx.x) / group;
     const int ng = (gridDim.x * blockDim.x) / group;
-    for (int ci = gi; ci < ncolliders; ci += ng) {
-        const Collider col = W.colliders[ci];
-        if (col.type != COL_HULL) continue;
-        const int b = W.col_body[ci];
-        if (W.fixed[b] && !include_fixed) continue;
-        transform_collider<R, EXACT, !EXACT>(W, col, b, sub, group);
+    const int n = W.queue[7];
+    for (int i = gi; i < n; i += ng) {
+        const int b = W.tlist[i];
+        for (int ci = W.col_start[b]; ci < W.col_start[b + 1]; ++ci) {
+            const Collider col = W.colliders[ci];
+            if (col.type == COL_HULL) transform_collider<R, EXACT, !EXACT>(W, col, b, sub, group);
+        }
     }
 }
 
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
         const int k = base + (int)threadIdx.x;
         int state = WS_NONE;
         bool gjk = false;
+        int ta = -1, tb = -1;
         if (k < n) {
             const int gp = W.work_list[k];
             const int2 pr = W.pairs[gp];
@@ -274,6 +278,26 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
             }
             W.work_state[k] = state;
             if (state == WS_NONE && !gjk) { W.pair_ccount[gp] = 0; W.pair_cstart[gp] = 0; }
+            if (gjk || state == WS_GENERAL) {   // both hulls are read this substep: list each body once
+                const int stamp = W.queue[4];
+                ta = atomicExch(&W.tstamp[a], stamp) != stamp ? a : -1;
+                tb = atomicExch(&W.tstamp[b], stamp) != stamp ? b : -1;
+            }
+        }
+        {   // warp-aggregated append of the newly listed bodies
+            const int lane = threadIdx.x & 31;
+            const int c = (ta >= 0) + (tb >= 0);
+            int incl = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int base = 0;
+            if (lane == 31 && total) base = atomicAdd(&W.queue[7], total);
+            base = __shfl_sync(0xffffffffu, base, 31) + incl - c;
+            if (ta >= 0) W.tlist[base++] = ta;
+            if (tb >= 0) W.tlist[base] = tb;
         }
         block_append(W.gjk_list, &W.queue[2], gjk, k, scan_smem, &base_smem);
         block_append(W.hit_list, &W.queue[3], state == WS_GENERAL, k, scan_smem, &base_smem);
@@ -923,13 +947,11 @@ struct PipeLauncher {
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(W.node_bits, 0, (size_t)d.node_words * 4, st)) != cudaSuccess) return e;
             if ((e = mark(PH_PREDICT)) != cudaSuccess) return e;
-            if (P.enable_collisions) {
-                k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, d.ncolliders, sub == 0 ? 1 : 0, c.transform_group);
-                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
-            }
             k_cull<R><<<c.cull_blocks, PIPE_BLOCK, 0, st>>>(W, P.enable_collisions);
             if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_NARROW)) != cudaSuccess) return e;
             if (P.enable_collisions) {
+                k_transform<R, EXACT><<<col_blocks, PIPE_BLOCK, 0, st>>>(W, c.transform_group);
+                if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_TRANSFORM)) != cudaSuccess) return e;
                 k_gjk<R, EXACT><<<c.gjk_blocks, PIPE_BLOCK, gjk_smem(), st>>>(W);
                 if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(PH_GJK)) != cudaSuccess) return e;
                 k_epa<R, EXACT><<<c.epa_blocks, PIPE_BLOCK, narrow_smem(), st>>>(W);

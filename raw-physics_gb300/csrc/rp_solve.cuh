@@ -317,7 +317,8 @@ __device__ void ext_solve(const WorldView<R>& W, const ExtConstraint& C, double*
             const Qt<float> qa = qcast<float>(a.q), qb = qcast<float>(b.q);
             V3<float> f1 = qaxis(qa, C.a1), f2 = qaxis(qb, C.a2), fn = vcross(f1, f2);
             const float fl = vlen(fn);
-            swing = fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi);
+            // limits at or beyond +-pi never act, however parallel the swing axes are
+            swing = !(C.lo <= -PI_REF && C.hi >= PI_REF) && (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi));
         }
         V3<double> n1 = qaxis(a.q, C.a1), n2 = qaxis(b.q, C.a2);
         V3<double> n = vcross(n1, n2);
@@ -448,10 +449,27 @@ __device__ __forceinline__ void fold_body(const WorldView<float>& W, int b) {
 __device__ __forceinline__ void frot_update(FBody& B, Qt<float> inc) {
     Qt<float> u = qt<float>(B.dq.x + inc.x, B.dq.y + inc.y, B.dq.z + inc.z, B.dq.w + inc.w);
     float e = 2.f * (B.q0f.x * u.x + B.q0f.y * u.y + B.q0f.z * u.z + B.q0f.w * u.w) + (u.x * u.x + u.y * u.y + u.z * u.z + u.w * u.w);
-    float s = sqrtf(1.f + e);
-    float rm1 = -e / (s * (1.f + s));
+    const float u1 = 1.f + e;   // |q0 + u|^2, close to 1
+    float s = u1 * rsqrtf(u1);
+    float rm1 = __fdividef(-e, s * (1.f + s));
     float r = 1.f + rm1;
     B.dq = qt<float>(B.q0f.x * rm1 + u.x * r, B.q0f.y * rm1 + u.y * r, B.q0f.z * rm1 + u.z * r, B.q0f.w * rm1 + u.w * r);
+}
+
+// FP32 delta-form arithmetic: unit vectors from the reciprocal square root of the special-function
+// unit and divisions by __fdividef (each within 2 ulp), shorter dependent chains than IEEE sqrtf and
+// division in the serial Gauss-Seidel chains; squared lengths at or below 1e-36 take the IEEE path
+// (rsqrtf flushes subnormal inputs).
+__device__ __forceinline__ float funit(V3<float> v, V3<float>& n) {
+    const float c2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (c2 > 1e-36f) {
+        const float r = rsqrtf(c2);
+        n = v3<float>(v.x * r, v.y * r, v.z * r);
+        return c2 * r;
+    }
+    const float c = vlen(v);
+    if (c > 0.f) n = v3<float>(v.x / c, v.y / c, v.z / c);
+    return c;
 }
 
 __device__ __forceinline__ Pcpd<float> fpcpd(const FBody& a, const FBody& b, V3<float> r1_lc, V3<float> r2_lc) {
@@ -466,18 +484,18 @@ __device__ __forceinline__ Pcpd<float> fpcpd(const FBody& a, const FBody& b, V3<
 
 __device__ __forceinline__ float fpos_dlambda(const FBody& a, const FBody& b, const Pcpd<float>& p, float lambda_til_free, V3<float> dx) {
     (void)lambda_til_free;
-    float c = vlen(dx);
+    V3<float> n;
+    const float c = funit(dx, n);
     if (c <= 0.f) return 0.f;
-    V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
     float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
     float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
-    return -c / (w1 + w2);   // contacts carry zero compliance (pbd.cpp:123,133)
+    return __fdividef(-c, w1 + w2);   // contacts carry zero compliance (pbd.cpp:123,133)
 }
 
 __device__ __forceinline__ void fpos_apply(FBody& a, FBody& b, const Pcpd<float>& p, float dl, V3<float> dx) {
-    float c = vlen(dx);
+    V3<float> n;
+    const float c = funit(dx, n);
     if (c <= 0.f) return;
-    V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
     V3<float> imp = vscale(dl, n);
     if (!a.fixed) a.dx = vadd(a.dx, vscale(a.invm, imp));
     if (!b.fixed) b.dx = vadd(b.dx, vscale(-b.invm, imp));
@@ -526,15 +544,15 @@ static __device__ void fcollision_solve(const WorldView<float>& W, FBody& a, FBo
 // same order of corrections as ext_solve, each applied to the FP32 deltas; joint-limit angles are
 // screened in FP32 and evaluated in FP64 (from the FP64 orientation q0 + dq) where they may act.
 __device__ __forceinline__ float fdlambda(float c, float w1, float w2, float h, float compliance, float lambda) {
-    const float til = compliance / (h * h);
-    return (-c - til * lambda) / (w1 + w2 + til);
+    const float til = __fdividef(compliance, h * h);
+    return __fdividef(-c - til * lambda, w1 + w2 + til);
 }
 
 __device__ __forceinline__ float fpos_dlambda_c(const FBody& a, const FBody& b, const Pcpd<float>& p, float h,
                                                 float compliance, float lambda, V3<float> dx) {
-    const float c = vlen(dx);
+    V3<float> n;
+    const float c = funit(dx, n);
     if (c <= 0.f) return 0.f;
-    const V3<float> n = v3<float>(dx.x / c, dx.y / c, dx.z / c);
     const float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
     const float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
     return fdlambda(c, w1, w2, h, compliance, lambda);
@@ -547,10 +565,18 @@ __device__ __forceinline__ Acpd<float> facpd(const FBody& a, const FBody& b) {
     return r;
 }
 
+// ang_dlambda on the FP32 path
+__device__ __forceinline__ float fang_dlambda(const Acpd<float>& A, float h, float compliance, float lambda, V3<float> dq) {
+    V3<float> n;
+    const float th = funit(dq, n);
+    if (th <= 0.f) return 0.f;
+    return fdlambda(th, vdot(n, mmulv(A.I1, n)), vdot(n, mmulv(A.I2, n)), h, compliance, lambda);
+}
+
 __device__ __forceinline__ void fang_apply(FBody& a, FBody& b, const Acpd<float>& A, float dl, V3<float> dq) {
-    const float th = vlen(dq);
+    V3<float> n;
+    const float th = funit(dq, n);
     if (th <= 0.f) return;
-    const V3<float> n = v3<float>(dq.x / th, dq.y / th, dq.z / th);
     const V3<float> imp = vscale(-dl, n);
     const V3<float> a1 = mmulv(A.I1, imp), a2 = mmulv(A.I2, imp);
     const Qt<float> q1 = qmul(qt<float>(a1.x, a1.y, a1.z, 0.f), a.q());
@@ -569,9 +595,9 @@ __device__ __forceinline__ Qt<double> fq64(const WorldView<float>& W, const FBod
 __device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64, float h, double* lam) {
     const V3<float> dq = v3cast<float>(dq64);
     const Acpd<float> B = facpd(a, b);
-    const float th = vlen(dq);
+    V3<float> n;
+    const float th = funit(dq, n);
     if (th <= 0.f) return;
-    const V3<float> n = v3<float>(dq.x / th, dq.y / th, dq.z / th);
     const float dl = fdlambda(th, vdot(n, mmulv(B.I1, n)), vdot(n, mmulv(B.I2, n)), h, 0.f, (float)*lam);
     fang_apply(a, b, B, dl, dq);
     *lam += (double)dl;
@@ -579,8 +605,8 @@ __device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64
 
 static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint& C, double* lam, float h) {
     FBody a = load_fbody(W, C.e1), b = load_fbody(W, C.e2);
-    const V3<float> r1 = v3<float>((float)C.r1[0], (float)C.r1[1], (float)C.r1[2]);
-    const V3<float> r2 = v3<float>((float)C.r2[0], (float)C.r2[1], (float)C.r2[2]);
+    const V3<float> r1 = v3<float>(C.r1f[0], C.r1f[1], C.r1f[2]);
+    const V3<float> r2 = v3<float>(C.r2f[0], C.r2f[1], C.r2f[2]);
     const V3<float> base_ab = fbase(W, C.e1, C.e2);
     auto anchor = [&](const Pcpd<float>& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
     switch (C.type) {
@@ -590,7 +616,7 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
                                          (float)((pa.z - pb.z) - C.distance[2]));
         const V3<float> dx = vadd(base, vsub(a.dx, b.dx));
         const Pcpd<float> p = fpcpd(a, b, r1, r2);
-        const float dl = fpos_dlambda_c(a, b, p, h, (float)C.compliance, (float)lam[0], dx);
+        const float dl = fpos_dlambda_c(a, b, p, h, C.compliance_f, (float)lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
     } break;
@@ -598,14 +624,14 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
         const Acpd<float> A = facpd(a, b);
         const Qt<float> aux = qmul(a.q(), qinverse(b.q()));
         const V3<float> dq = v3<float>(2.f * aux.x, 2.f * aux.y, 2.f * aux.z);
-        const float dl = ang_dlambda(A, h, (float)C.compliance, (float)lam[0], dq);
+        const float dl = fang_dlambda(A, h, C.compliance_f, (float)lam[0], dq);
         fang_apply(a, b, A, dl, dq);
         lam[0] += (double)dl;
     } break;
     case CON_HINGE: {  // pbd.cpp:245-299
         const Acpd<float> A = facpd(a, b);
         const V3<float> dq = vcross(qaxis(a.q(), C.a1), qaxis(b.q(), C.a2));
-        float dl = ang_dlambda(A, h, (float)C.compliance, (float)lam[1], dq);
+        float dl = fang_dlambda(A, h, C.compliance_f, (float)lam[1], dq);
         fang_apply(a, b, A, dl, dq);
         lam[1] += (double)dl;
         const Pcpd<float> p = fpcpd(a, b, r1, r2);
@@ -630,7 +656,8 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
         {   // swing
             const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2), fn = vcross(f1, f2);
             const float fl = vlen(fn);
-            if (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi)) {
+            const bool never = C.lo <= -PI_REF && C.hi >= PI_REF;   // limits at or beyond +-pi never act
+            if (!never && (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi))) {
                 const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
                 const V3<double> n1 = qaxis(qa, C.a1), n2 = qaxis(qb, C.a2);
                 V3<double> n = vcross(n1, n2);

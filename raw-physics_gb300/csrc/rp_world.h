@@ -47,6 +47,8 @@ struct ExtConstraint {
     double distance[3];
     double lo, hi;           // hinge limits | spherical swing limits
     double lo2, hi2;         // spherical twist limits
+    float r1f[3], r2f[3];    // FP32 roundings of r1, r2 and compliance (the FP32 build's operands)
+    float compliance_f;
 };
 
 struct Shape {               // one convex hull's topology (collider_convex_hull_create output)
@@ -195,10 +197,12 @@ struct WorldView {
                                  //     degenerate configuration, redone in FP64 (queue[5] of them)
     float* work_face;            // [12 * pair capacity] FP32 build: EPA's final face (three Minkowski points)
                                  //     and its FP32 normal, finished in FP64 by k_epa_finish
+    int32_t* tstamp;             // [bodies] the substep (queue[4]) whose hull transform list took the body last
+    int32_t* tlist;              // [bodies] bodies whose hulls this substep transforms (queue[7] of them)
     int32_t* queue;              // [16] [0] work items this frame, [1] next scene of a warp-per-scene sweep,
                                  //     [2] gjk_list length, [3] hit_list length, [4] substeps run since
                                  //     the world was built (phase-major form), [5] fallback_list length,
-                                 //     [6] next of the CTA-swept scenes
+                                 //     [6] next of the CTA-swept scenes, [7] tlist length
     const int32_t* scene_order;  // [S] scenes by decreasing size (the order warps take them in)
     int32_t cta_scenes;          // the first cta_scenes of scene_order are swept by a whole CTA each
     int32_t max_colliders_per_body;
