@@ -801,14 +801,16 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
     return true;
 }
 
-template <typename R, bool EXACT, bool VELOCITY>
+// CTA: the instantiation with the CTA phase (W.cta_scenes > 0); without it the kernel's code holds
+// only the warp path.
+template <typename R, bool EXACT, bool VELOCITY, bool CTA>
 __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R> W, double h, int resched_first) {
     if (frame_abandoned(W.status)) return;
     __shared__ SerialSmem ssm[VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32];
     __shared__ int s_next, s_ok;
     // the W.cta_scenes largest scenes first, each swept by a whole CTA (queue[6] hands them out), so
     // the biggest scenes do not leave one warp finishing alone; then one warp per scene (queue[1])
-    for (;;) {
+    for (; CTA;) {
         if (threadIdx.x == 0) s_next = atomicAdd(&W.queue[6], 1);
         __syncthreads();
         const int i = s_next;
@@ -888,7 +890,7 @@ struct PipeLauncher {
         c.manifold_blocks = nb * sms;
         nb = occ((const void*)k_manifold<R, EXACT, true>, PIPE_BLOCK, narrow_smem());
         c.general_blocks = nb * sms;
-        c.sweep_warp_blocks = occ((const void*)k_sweep_warp<R, EXACT, false>, SWEEP_WARP_BLOCK, 0) * sms;
+        c.sweep_warp_blocks = occ((const void*)k_sweep_warp<R, EXACT, false, true>, SWEEP_WARP_BLOCK, 0) * sms;
         c.cull_blocks = occ((const void*)k_cull<R>, PIPE_BLOCK, 0) * sms;
         // cooperative kernels: one CTA per SM keeps the grid barrier's arrival count low
         (void)occ((const void*)k_setup_grid<R>, BLOCK, 0);
@@ -919,7 +921,8 @@ struct PipeLauncher {
         cudaError_t e = cudaMemsetAsync(W.queue + 1, 0, sizeof(int32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(W.queue + 6, 0, sizeof(int32_t), st);
         if (e != cudaSuccess) return e;
-        k_sweep_warp<R, EXACT, VELOCITY><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h, first);
+        if (W.cta_scenes > 0) k_sweep_warp<R, EXACT, VELOCITY, true><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h, first);
+        else k_sweep_warp<R, EXACT, VELOCITY, false><<<c.sweep_warp_blocks, SWEEP_WARP_BLOCK, 0, st>>>(W, h, first);
         return cudaGetLastError();
     }
 
