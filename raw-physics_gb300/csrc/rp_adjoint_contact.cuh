@@ -488,8 +488,8 @@ __device__ __noinline__ void g_manifold(const AdjointScene& sc, const AdjGeom& G
     GClip<S>& C = *X.clip;
     bool overflow = false;
     // incident polygon and boundary planes (build_boundary_planes, clipping.cpp:121-134)
-    const int fs_i = fes[ih.sh.face_off + inf];
-    int ninc = fes[ih.sh.face_off + inf + 1] - fs_i;
+    const int fs_i = fes[ih.sh.elem_off + inf];
+    int ninc = fes[ih.sh.elem_off + inf + 1] - fs_i;
     if (ninc > CLIP_MAX) { overflow = true; ninc = CLIP_MAX; }
     for (int k = 0; k < ninc; ++k) C.buf[0][k] = ih.tv[G.face_elem[fs_i + k]];
     const int f2n_row = rh.sh.f2n_off + rf;
@@ -497,7 +497,7 @@ __device__ __noinline__ void g_manifold(const AdjointScene& sc, const AdjGeom& G
     if (npl > CLIP_MAX) { overflow = true; npl = CLIP_MAX; }
     for (int k = 0; k < npl; ++k) {
         const int nf = cd[cs[f2n_row] + k];
-        C.pp[k] = rh.tv[G.face_elem[fes[rh.sh.face_off + nf]]];
+        C.pp[k] = rh.tv[G.face_elem[fes[rh.sh.elem_off + nf]]];
         C.pn[k] = vinv(rh.tn[nf]);
     }
     int n = ninc, cur = 0;
@@ -507,7 +507,7 @@ __device__ __noinline__ void g_manifold(const AdjointScene& sc, const AdjGeom& G
         if (m >= 0) { n = m; cur ^= 1; }
     }
     const V3<S> ref_n = vinv(rh.tn[rf]);
-    const V3<S> ref_p = rh.tv[G.face_elem[fes[rh.sh.face_off + rf]]];
+    const V3<S> ref_p = rh.tv[G.face_elem[fes[rh.sh.elem_off + rf]]];
     if (n > 0) {
         const int m = g_sh_pass(C.buf[cur], n, C.buf[cur ^ 1], ref_n, ref_p, true, overflow);
         if (m >= 0) { n = m; cur ^= 1; }

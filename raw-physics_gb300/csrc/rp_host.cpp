@@ -324,37 +324,60 @@ rp_status build_device(rp_world* w) {
     std::vector<double> sverts, snorm;
     std::vector<int32_t> fstart, felem, cstart, cdata;
     std::vector<int> shape_of_hull(w->hulls.size(), -1);
+    // topology tables once per distinct topology: scaled copies of one mesh share them, which keeps
+    // the contact manifold's lookups in a few kilobytes
+    std::map<std::vector<int32_t>, Shape> topo;
     for (size_t h = 0; h < w->hulls.size(); ++h) {
         const Hull& H = *w->hulls[h];
         Shape sh;
         sh.nv = H.nv();
         sh.nf = H.nf();
         sh.vert_off = (int32_t)(sverts.size() / 3);
-        sh.face_off = (int32_t)fstart.size();
-        sh.max_face_valence = 0;
-        sh.max_face_neighbours = 0;
+        sh.face_off = (int32_t)(snorm.size() / 3);
         sverts.insert(sverts.end(), H.verts.begin(), H.verts.end());
         snorm.insert(snorm.end(), H.normals.begin(), H.normals.end());
-        // face element CSR over one global face numbering (face_off = the shape's first face);
-        // a single sentinel after the last shape closes the final face
-        for (int f = 0; f < sh.nf; ++f) {
-            fstart.push_back((int32_t)felem.size());
-            felem.insert(felem.end(), H.faces[(size_t)f].begin(), H.faces[(size_t)f].end());
-            sh.max_face_valence = std::max(sh.max_face_valence, (int32_t)H.faces[(size_t)f].size());
-            sh.max_face_neighbours = std::max(sh.max_face_neighbours, (int32_t)H.f2n[(size_t)f].size());
-        }
-        auto add_csr = [&](const std::vector<std::vector<int>>& rows) {
-            int32_t off = (int32_t)cstart.size();
-            for (const auto& r : rows) {
-                cstart.push_back((int32_t)cdata.size());
-                cdata.insert(cdata.end(), r.begin(), r.end());
+        std::vector<int32_t> key{sh.nv};
+        for (const auto* rows : {&H.faces, &H.v2f, &H.v2n, &H.f2n}) {
+            key.push_back((int32_t)rows->size());
+            for (const auto& r : *rows) {
+                key.push_back((int32_t)r.size());
+                key.insert(key.end(), r.begin(), r.end());
             }
-            cstart.push_back((int32_t)cdata.size());
-            return off;
-        };
-        sh.v2f_off = add_csr(H.v2f);
-        sh.v2n_off = add_csr(H.v2n);
-        sh.f2n_off = add_csr(H.f2n);
+        }
+        auto it = topo.find(key);
+        if (it == topo.end()) {
+            Shape t;
+            t.max_face_valence = 0;
+            t.max_face_neighbours = 0;
+            // face element CSR over one global face numbering (elem_off = the topology's first face);
+            // a single sentinel after the last topology closes the final face
+            t.elem_off = (int32_t)fstart.size();
+            for (int f = 0; f < sh.nf; ++f) {
+                fstart.push_back((int32_t)felem.size());
+                felem.insert(felem.end(), H.faces[(size_t)f].begin(), H.faces[(size_t)f].end());
+                t.max_face_valence = std::max(t.max_face_valence, (int32_t)H.faces[(size_t)f].size());
+                t.max_face_neighbours = std::max(t.max_face_neighbours, (int32_t)H.f2n[(size_t)f].size());
+            }
+            auto add_csr = [&](const std::vector<std::vector<int>>& rows) {
+                int32_t off = (int32_t)cstart.size();
+                for (const auto& r : rows) {
+                    cstart.push_back((int32_t)cdata.size());
+                    cdata.insert(cdata.end(), r.begin(), r.end());
+                }
+                cstart.push_back((int32_t)cdata.size());
+                return off;
+            };
+            t.v2f_off = add_csr(H.v2f);
+            t.v2n_off = add_csr(H.v2n);
+            t.f2n_off = add_csr(H.f2n);
+            it = topo.emplace(std::move(key), t).first;
+        }
+        sh.elem_off = it->second.elem_off;
+        sh.v2f_off = it->second.v2f_off;
+        sh.v2n_off = it->second.v2n_off;
+        sh.f2n_off = it->second.f2n_off;
+        sh.max_face_valence = it->second.max_face_valence;
+        sh.max_face_neighbours = it->second.max_face_neighbours;
         shape_of_hull[h] = (int)shapes.size();
         shapes.push_back(sh);
     }
@@ -1812,12 +1835,16 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
     const int cta0 = w->pipe.sweep_cta ? 1 : w->cta_from;
     int best[4] = {RP_MODE_PHASED, 8, cta0, 512};
     float best_ms = 0.f;
+    // each candidate timed twice (the faster run counts); a later candidate replaces the best only
+    // when it is at least 3 % faster, so timing noise does not move the choice off the default
     auto consider = [&](int mode, int group, int cta, int solo) -> rp_status {
         set_tune(mode, group, cta, solo);
-        float ms = 0.f;
+        float ms = 0.f, ms2 = 0.f;
         rp_status r = trial(ms);
+        if (r == RP_OK) r = trial(ms2);
         if (r != RP_OK) return r;
-        if (best_ms == 0.f || ms < best_ms) {
+        ms = std::min(ms, ms2);
+        if (best_ms == 0.f || ms < 0.97f * best_ms) {
             best_ms = ms;
             best[0] = mode; best[1] = group; best[2] = cta; best[3] = solo;
         }

@@ -987,8 +987,8 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
     int rf = ref1 ? f1 : f2, inf = ref1 ? f2 : f1;
     const int32_t* fes = W.face_elem_start;
     // incident polygon and boundary planes (build_boundary_planes, clipping.cpp:121-134)
-    int fs_i = fes[ih.shape->face_off + inf];
-    int fe_i = fes[ih.shape->face_off + inf + 1];
+    int fs_i = fes[ih.shape->elem_off + inf];
+    int fe_i = fes[ih.shape->elem_off + inf + 1];
     int ninc = fe_i - fs_i;
     if (ninc > CLIP_MAX) { if (lane == 0) atomicOr(&sm.status, (int)ST_CLIP_OVERFLOW); ninc = CLIP_MAX; }
     for (int k = (int)lane; k < ninc; k += WARP) sm.u.clip.buf[0][k] = cv_vertex(ih, W.face_elem[fs_i + k]);
@@ -997,7 +997,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
     if (npl > CLIP_MAX) { if (lane == 0) atomicOr(&sm.status, (int)ST_CLIP_OVERFLOW); npl = CLIP_MAX; }
     for (int k = (int)lane; k < npl; k += WARP) {
         int nf = cd[cs[f2n_row] + k];
-        sm.u.clip.pp[k] = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + nf]]);
+        sm.u.clip.pp[k] = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->elem_off + nf]]);
         sm.u.clip.pn[k] = vinv(rh.norms[nf]);
     }
     __syncwarp();
@@ -1009,7 +1009,7 @@ __device__ void convex_convex_manifold(NarrowSmem<R>& sm, const WorldView<R>& W,
         if (m >= 0) { n = m; cur ^= 1; }
     }
     V3<R> ref_n = vinv(rh.norms[rf]);
-    V3<R> ref_p = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->face_off + rf]]);
+    V3<R> ref_p = cv_vertex(rh, W.face_elem[W.face_elem_start[rh.shape->elem_off + rf]]);
     if (n > 0) {
         const int m = sh_pass(sm.u.clip.buf[cur], n, sm.u.clip.buf[cur ^ 1], ref_n, ref_p, true, st);
         if (m >= 0) { n = m; cur ^= 1; }

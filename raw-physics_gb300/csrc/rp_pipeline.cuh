@@ -801,6 +801,14 @@ __device__ bool resched_serial(const WorldView<R>& W, int s, SerialSmem& sm) {
     return true;
 }
 
+// The relaxation schedule by one warp, for scenes beyond resched_serial's shared tables (rare): out of
+// line, so that the sweep's own path keeps its registers.
+template <typename R>
+__device__ __noinline__ void resched_warp_cold(const WorldView<R>& W, int s) {
+    WarpGroup g;
+    resched(W, g, s);
+}
+
 // CTA: the instantiation with the CTA phase (W.cta_scenes > 0); without it the kernel's code holds
 // only the warp path.
 template <typename R, bool EXACT, bool VELOCITY, bool CTA>
@@ -839,7 +847,7 @@ __global__ void __launch_bounds__(SWEEP_WARP_BLOCK, 4) k_sweep_warp(WorldView<R>
         if (i >= W.num_scenes) break;
         const int s = W.scene_order[i];
         if (!VELOCITY && resched_first) {
-            if (!resched_serial(W, s, ssm[(threadIdx.x >> 5) % (VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32)])) resched(W, g, s);
+            if (!resched_serial(W, s, ssm[(threadIdx.x >> 5) % (VELOCITY ? 1 : SWEEP_WARP_BLOCK / 32)])) resched_warp_cold(W, s);
         }
         sweep_levels<R, EXACT, VELOCITY>(W, g, s, (R)h);
         __syncwarp();

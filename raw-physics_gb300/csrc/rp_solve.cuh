@@ -398,7 +398,7 @@ struct FBody {
     V3<float> dx;
     Qt<float> q0f, dq;
     float invm;
-    M3<float> Iinv;
+    float S[6];   // local inverse inertia, symmetric storage (xx yy zz xy xz yz)
     bool fixed;
     int idx;
     __device__ __forceinline__ Qt<float> q() const { return qt<float>(q0f.x + dq.x, q0f.y + dq.y, q0f.z + dq.z, q0f.w + dq.w); }
@@ -411,10 +411,8 @@ __device__ __forceinline__ FBody load_fbody(const WorldView<float>& W, int b) {
     B.dx = v3<float>(d.x, d.y, d.z);
     B.dq = qt<float>(q.x, q.y, q.z, q.w);
     B.invm = W.inv_mass[b];
-    float s[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) s[i] = W.inv_inertia[6 * b + i];
-    B.Iinv = msym(s);
+    for (int i = 0; i < 6; ++i) B.S[i] = W.inv_inertia[6 * b + i];
     B.fixed = W.fixed[b] != 0;
     B.idx = b;
     return B;
@@ -472,35 +470,49 @@ __device__ __forceinline__ float funit(V3<float> v, V3<float>& n) {
     return c;
 }
 
-__device__ __forceinline__ Pcpd<float> fpcpd(const FBody& a, const FBody& b, V3<float> r1_lc, V3<float> r2_lc) {
-    Pcpd<float> p;
-    Qt<float> qa = a.q(), qb = b.q();
-    p.r1 = qrotate(qa, r1_lc);
-    p.r2 = qrotate(qb, r2_lc);
-    p.I1 = world_tensor(qa, a.Iinv);
-    p.I2 = world_tensor(qb, b.Iinv);
+// The world inverse inertia applied to v at the body's current orientation, R (S (R^T v)): the
+// products the reference forms with the world tensor R S R^T (physics_util.cpp:26-63), without
+// keeping the tensor itself live through the solve (the FP32 path's register budget).
+__device__ __forceinline__ V3<float> fIinv(const FBody& B, V3<float> v) {
+    const M3<float> R = qmat3(B.q());
+    const V3<float> l = v3<float>(R.d[0][0] * v.x + R.d[1][0] * v.y + R.d[2][0] * v.z,
+                                  R.d[0][1] * v.x + R.d[1][1] * v.y + R.d[2][1] * v.z,
+                                  R.d[0][2] * v.x + R.d[1][2] * v.y + R.d[2][2] * v.z);
+    const V3<float> t = v3<float>(B.S[0] * l.x + B.S[3] * l.y + B.S[4] * l.z, B.S[3] * l.x + B.S[1] * l.y + B.S[5] * l.z,
+                                  B.S[4] * l.x + B.S[5] * l.y + B.S[2] * l.z);
+    return mmulv(R, t);
+}
+
+// calculate_positional_constraint_preprocessed_data on the FP32 path: the anchors in world axes (the
+// inertia products are taken by fIinv at the same orientations, before the correction moves them)
+struct FPcpd { V3<float> r1, r2; };
+__device__ __forceinline__ FPcpd fpcpd(const FBody& a, const FBody& b, V3<float> r1_lc, V3<float> r2_lc) {
+    FPcpd p;
+    p.r1 = qrotate(a.q(), r1_lc);
+    p.r2 = qrotate(b.q(), r2_lc);
     return p;
 }
 
-__device__ __forceinline__ float fpos_dlambda(const FBody& a, const FBody& b, const Pcpd<float>& p, float lambda_til_free, V3<float> dx) {
+__device__ __forceinline__ float fpos_dlambda(const FBody& a, const FBody& b, const FPcpd& p, float lambda_til_free, V3<float> dx) {
     (void)lambda_til_free;
     V3<float> n;
     const float c = funit(dx, n);
     if (c <= 0.f) return 0.f;
-    float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
-    float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    const V3<float> c1 = vcross(p.r1, n), c2 = vcross(p.r2, n);
+    float w1 = a.invm + vdot(c1, fIinv(a, c1));
+    float w2 = b.invm + vdot(c2, fIinv(b, c2));
     return __fdividef(-c, w1 + w2);   // contacts carry zero compliance (pbd.cpp:123,133)
 }
 
-__device__ __forceinline__ void fpos_apply(FBody& a, FBody& b, const Pcpd<float>& p, float dl, V3<float> dx) {
+__device__ __forceinline__ void fpos_apply(FBody& a, FBody& b, const FPcpd& p, float dl, V3<float> dx) {
     V3<float> n;
     const float c = funit(dx, n);
     if (c <= 0.f) return;
     V3<float> imp = vscale(dl, n);
     if (!a.fixed) a.dx = vadd(a.dx, vscale(a.invm, imp));
     if (!b.fixed) b.dx = vadd(b.dx, vscale(-b.invm, imp));
-    V3<float> a1 = mmulv(p.I1, vcross(p.r1, imp));
-    V3<float> a2 = mmulv(p.I2, vcross(p.r2, imp));
+    V3<float> a1 = fIinv(a, vcross(p.r1, imp));
+    V3<float> a2 = fIinv(b, vcross(p.r2, imp));
     Qt<float> q1 = qmul(qt<float>(a1.x, a1.y, a1.z, 0.f), a.q());
     Qt<float> q2 = qmul(qt<float>(a2.x, a2.y, a2.z, 0.f), b.q());
     if (!a.fixed) frot_update(a, qt<float>(0.5f * q1.x, 0.5f * q1.y, 0.5f * q1.z, 0.5f * q1.w));
@@ -511,7 +523,7 @@ __device__ __forceinline__ void fpos_apply(FBody& a, FBody& b, const Pcpd<float>
 static __device__ void fcollision_solve(const WorldView<float>& W, FBody& a, FBody& b, V3<float> base_ab, float* c, float mus) {
     V3<float> r1 = v3<float>(c[0], c[1], c[2]), r2 = v3<float>(c[4], c[5], c[6]), n = v3<float>(c[8], c[9], c[10]);
     float lambda_n = c[3], lambda_t = c[7];
-    Pcpd<float> p = fpcpd(a, b, r1, r2);
+    FPcpd p = fpcpd(a, b, r1, r2);
     V3<float> d12 = vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2));
     float d = vdot(d12, n);
     if (d > 0.f) {
@@ -548,37 +560,31 @@ __device__ __forceinline__ float fdlambda(float c, float w1, float w2, float h, 
     return __fdividef(-c - til * lambda, w1 + w2 + til);
 }
 
-__device__ __forceinline__ float fpos_dlambda_c(const FBody& a, const FBody& b, const Pcpd<float>& p, float h,
+__device__ __forceinline__ float fpos_dlambda_c(const FBody& a, const FBody& b, const FPcpd& p, float h,
                                                 float compliance, float lambda, V3<float> dx) {
     V3<float> n;
     const float c = funit(dx, n);
     if (c <= 0.f) return 0.f;
-    const float w1 = a.invm + vdot(vcross(p.r1, n), mmulv(p.I1, vcross(p.r1, n)));
-    const float w2 = b.invm + vdot(vcross(p.r2, n), mmulv(p.I2, vcross(p.r2, n)));
+    const V3<float> c1 = vcross(p.r1, n), c2 = vcross(p.r2, n);
+    const float w1 = a.invm + vdot(c1, fIinv(a, c1));
+    const float w2 = b.invm + vdot(c2, fIinv(b, c2));
     return fdlambda(c, w1, w2, h, compliance, lambda);
 }
 
-__device__ __forceinline__ Acpd<float> facpd(const FBody& a, const FBody& b) {
-    Acpd<float> r;
-    r.I1 = world_tensor(a.q(), a.Iinv);
-    r.I2 = world_tensor(b.q(), b.Iinv);
-    return r;
-}
-
 // ang_dlambda on the FP32 path
-__device__ __forceinline__ float fang_dlambda(const Acpd<float>& A, float h, float compliance, float lambda, V3<float> dq) {
+__device__ __forceinline__ float fang_dlambda(const FBody& a, const FBody& b, float h, float compliance, float lambda, V3<float> dq) {
     V3<float> n;
     const float th = funit(dq, n);
     if (th <= 0.f) return 0.f;
-    return fdlambda(th, vdot(n, mmulv(A.I1, n)), vdot(n, mmulv(A.I2, n)), h, compliance, lambda);
+    return fdlambda(th, vdot(n, fIinv(a, n)), vdot(n, fIinv(b, n)), h, compliance, lambda);
 }
 
-__device__ __forceinline__ void fang_apply(FBody& a, FBody& b, const Acpd<float>& A, float dl, V3<float> dq) {
+__device__ __forceinline__ void fang_apply(FBody& a, FBody& b, float dl, V3<float> dq) {
     V3<float> n;
     const float th = funit(dq, n);
     if (th <= 0.f) return;
     const V3<float> imp = vscale(-dl, n);
-    const V3<float> a1 = mmulv(A.I1, imp), a2 = mmulv(A.I2, imp);
+    const V3<float> a1 = fIinv(a, imp), a2 = fIinv(b, imp);
     const Qt<float> q1 = qmul(qt<float>(a1.x, a1.y, a1.z, 0.f), a.q());
     const Qt<float> q2 = qmul(qt<float>(a2.x, a2.y, a2.z, 0.f), b.q());
     if (!a.fixed) frot_update(a, qt<float>(0.5f * q1.x, 0.5f * q1.y, 0.5f * q1.z, 0.5f * q1.w));
@@ -594,13 +600,46 @@ __device__ __forceinline__ Qt<double> fq64(const WorldView<float>& W, const FBod
 // angular correction of one joint limit (limit_angle's dq, FP64) on the deltas
 __device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64, float h, double* lam) {
     const V3<float> dq = v3cast<float>(dq64);
-    const Acpd<float> B = facpd(a, b);
     V3<float> n;
     const float th = funit(dq, n);
     if (th <= 0.f) return;
-    const float dl = fdlambda(th, vdot(n, mmulv(B.I1, n)), vdot(n, mmulv(B.I2, n)), h, 0.f, (float)*lam);
-    fang_apply(a, b, B, dl, dq);
+    const float dl = fdlambda(th, vdot(n, fIinv(a, n)), vdot(n, fIinv(b, n)), h, 0.f, (float)*lam);
+    fang_apply(a, b, dl, dq);
     *lam += (double)dl;
+}
+
+// FP64 evaluation of a joint limit that the FP32 screen could not rule out (rare): kind 0 the hinge
+// limit (pbd.cpp:279-298), 1 the spherical swing limit, 2 the spherical twist limit (pbd.cpp:327-378),
+// each from the FP64 orientations q0 + dq, applying its correction to a and b. Out of line, so that
+// the joint solve's common path keeps its values in registers.
+static __device__ __noinline__ void flimit64(const WorldView<float>& W, FBody& a, FBody& b, const ExtConstraint& C, float h,
+                                             double* lam, int kind) {
+    const double EPS64 = 1e-50;
+    const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
+    V3<double> dq64;
+    if (kind == 0) {
+        if (limit_angle<double>(qaxis(qa, C.a1), qaxis(qa, C.l1), qaxis(qb, C.l2), C.lo, C.hi, dq64))
+            flimit_apply(a, b, dq64, h, &lam[2]);
+    } else if (kind == 1) {
+        const V3<double> n1 = qaxis(qa, C.a1), n2 = qaxis(qb, C.a2);
+        const V3<double> n = vcross(n1, n2);
+        const double nl = vlen(n);
+        if (nl > EPS64 && limit_angle<double>(v3<double>(n.x / nl, n.y / nl, n.z / nl), n1, n2, C.lo, C.hi, dq64))
+            flimit_apply(a, b, dq64, h, &lam[1]);
+    } else {
+        const V3<double> a1 = qaxis(qa, C.a1), b1 = qaxis(qa, C.l1), a2 = qaxis(qb, C.a2), b2 = qaxis(qb, C.l2);
+        V3<double> n = vadd(a1, a2);
+        const double nl = vlen(n);
+        if (nl > EPS64) {
+            n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
+            const V3<double> n1 = vsub(b1, vscale(vdot(n, b1), n)), n2 = vsub(b2, vscale(vdot(n, b2), n));
+            const double l1 = vlen(n1), l2 = vlen(n2);
+            if (l1 > EPS64 && l2 > EPS64 &&
+                limit_angle<double>(n, v3<double>(n1.x / l1, n1.y / l1, n1.z / l1), v3<double>(n2.x / l2, n2.y / l2, n2.z / l2),
+                                    C.lo2, C.hi2, dq64))
+                flimit_apply(a, b, dq64, h, &lam[2]);
+        }
+    }
 }
 
 static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint& C, double* lam, float h) {
@@ -608,63 +647,51 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
     const V3<float> r1 = v3<float>(C.r1f[0], C.r1f[1], C.r1f[2]);
     const V3<float> r2 = v3<float>(C.r2f[0], C.r2f[1], C.r2f[2]);
     const V3<float> base_ab = fbase(W, C.e1, C.e2);
-    auto anchor = [&](const Pcpd<float>& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
+    auto anchor = [&](const FPcpd& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
     switch (C.type) {
     case CON_POSITIONAL: {  // pbd.cpp:81-97
         const double4_32a pa = W.pos[C.e1], pb = W.pos[C.e2];
         const V3<float> base = v3<float>((float)((pa.x - pb.x) - C.distance[0]), (float)((pa.y - pb.y) - C.distance[1]),
                                          (float)((pa.z - pb.z) - C.distance[2]));
         const V3<float> dx = vadd(base, vsub(a.dx, b.dx));
-        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const FPcpd p = fpcpd(a, b, r1, r2);
         const float dl = fpos_dlambda_c(a, b, p, h, C.compliance_f, (float)lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
     } break;
     case CON_MUTUAL_ORIENTATION: {  // pbd.cpp:156-173
-        const Acpd<float> A = facpd(a, b);
         const Qt<float> aux = qmul(a.q(), qinverse(b.q()));
         const V3<float> dq = v3<float>(2.f * aux.x, 2.f * aux.y, 2.f * aux.z);
-        const float dl = fang_dlambda(A, h, C.compliance_f, (float)lam[0], dq);
-        fang_apply(a, b, A, dl, dq);
+        const float dl = fang_dlambda(a, b, h, C.compliance_f, (float)lam[0], dq);
+        fang_apply(a, b, dl, dq);
         lam[0] += (double)dl;
     } break;
     case CON_HINGE: {  // pbd.cpp:245-299
-        const Acpd<float> A = facpd(a, b);
         const V3<float> dq = vcross(qaxis(a.q(), C.a1), qaxis(b.q(), C.a2));
-        float dl = fang_dlambda(A, h, C.compliance_f, (float)lam[1], dq);
-        fang_apply(a, b, A, dl, dq);
+        float dl = fang_dlambda(a, b, h, C.compliance_f, (float)lam[1], dq);
+        fang_apply(a, b, dl, dq);
         lam[1] += (double)dl;
-        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const FPcpd p = fpcpd(a, b, r1, r2);
         const V3<float> dx = anchor(p);
         dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
         if (C.limited && limit_may_act(qaxis(a.q(), C.a1), qaxis(a.q(), C.l1), qaxis(b.q(), C.l2), C.lo, C.hi)) {
-            const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
-            V3<double> dq64;
-            if (limit_angle<double>(qaxis(qa, C.a1), qaxis(qa, C.l1), qaxis(qb, C.l2), C.lo, C.hi, dq64))
-                flimit_apply(a, b, dq64, h, &lam[2]);
+            flimit64(W, a, b, C, h, lam, 0);
         }
     } break;
     case CON_SPHERICAL: {  // pbd.cpp:301-379
-        const Pcpd<float> p = fpcpd(a, b, r1, r2);
+        const FPcpd p = fpcpd(a, b, r1, r2);
         const V3<float> dx = anchor(p);
         const float dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
         lam[0] += (double)dl;
-        const double EPS64 = 1e-50;
         {   // swing
             const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2), fn = vcross(f1, f2);
             const float fl = vlen(fn);
             const bool never = C.lo <= -PI_REF && C.hi >= PI_REF;   // limits at or beyond +-pi never act
             if (!never && (fl < 1e-3f || limit_may_act(vscale(1.f / fl, fn), f1, f2, C.lo, C.hi))) {
-                const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
-                const V3<double> n1 = qaxis(qa, C.a1), n2 = qaxis(qb, C.a2);
-                V3<double> n = vcross(n1, n2);
-                const double nl = vlen(n);
-                V3<double> dq64;
-                if (nl > EPS64 && limit_angle<double>(v3<double>(n.x / nl, n.y / nl, n.z / nl), n1, n2, C.lo, C.hi, dq64))
-                    flimit_apply(a, b, dq64, h, &lam[1]);
+                flimit64(W, a, b, C, h, lam, 1);
             }
         }
         {   // twist, on the orientations after the swing correction
@@ -683,22 +710,7 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
                 act = (l1 < 1e-3f || l2 < 1e-3f) ? !never
                                                  : limit_may_act(gn, vscale(1.f / l1, h1), vscale(1.f / l2, h2), C.lo2, C.hi2);
             }
-            if (act) {
-                const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
-                const V3<double> a1 = qaxis(qa, C.a1), b1 = qaxis(qa, C.l1), a2 = qaxis(qb, C.a2), b2 = qaxis(qb, C.l2);
-                V3<double> n = vadd(a1, a2);
-                const double nl = vlen(n);
-                if (nl > EPS64) {
-                    n = v3<double>(n.x / nl, n.y / nl, n.z / nl);
-                    V3<double> n1 = vsub(b1, vscale(vdot(n, b1), n)), n2 = vsub(b2, vscale(vdot(n, b2), n));
-                    const double l1 = vlen(n1), l2 = vlen(n2);
-                    V3<double> dq64;
-                    if (l1 > EPS64 && l2 > EPS64 &&
-                        limit_angle<double>(n, v3<double>(n1.x / l1, n1.y / l1, n1.z / l1),
-                                            v3<double>(n2.x / l2, n2.y / l2, n2.z / l2), C.lo2, C.hi2, dq64))
-                        flimit_apply(a, b, dq64, h, &lam[2]);
-                }
-            }
+            if (act) flimit64(W, a, b, C, h, lam, 2);
         }
     } break;
     default: break;

@@ -54,7 +54,9 @@ struct ExtConstraint {
 struct Shape {               // one convex hull's topology (collider_convex_hull_create output)
     int32_t nv, nf;
     int32_t vert_off;        // into shape_verts (local, pre-scaled vertices, FP64)
-    int32_t face_off;        // into face_normal / face_elem_start
+    int32_t face_off;        // into face_normal (this hull's geometry)
+    int32_t elem_off;        // into face_elem_start; the topology tables (elem_off, v2f/v2n/f2n_off) are
+                             //     shared by every hull of one topology (scaled copies of one mesh)
     int32_t v2f_off, v2n_off;   // into csr_start for vertex -> faces, vertex -> neighbours
     int32_t f2n_off;            // into csr_start for face -> neighbour faces
     int32_t max_face_valence;
@@ -126,7 +128,7 @@ struct WorldView {
     const double* face_normal;   // [3 * total faces] local face normals
     const float* shape_verts_f;  // FP32 copies of shape_verts / face_normal (the FP32 build's
     const float* face_normal_f;  // transform reads them without FP64 conversions)
-    const int32_t* face_elem_start;  // [total faces + num shapes] CSR starts (per shape: nf+1 entries)
+    const int32_t* face_elem_start;  // [faces of the distinct topologies + 1] CSR starts (from Shape::elem_off)
     const int32_t* face_elem;        // vertex indices of faces
     const int32_t* csr_start;        // shared CSR start table for v2f / v2n / f2n
     const int32_t* csr_data;
