@@ -161,7 +161,7 @@ struct rp_world {
     DevBuf d_rec, d_slot_entity;                   // the records on the device; entity of each body slot
     cudaEvent_t ev_rec = nullptr;                  // the last record upload (h_rec is refilled after it)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
-    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist;
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist, d_single_hull;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     int cta_from = 256;               // tunable: batched sweeps give a whole CTA to scenes of this cost or more
@@ -557,6 +557,13 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(upload(w->d_body_scene, body_scene, st));
         RP_CUDA(upload(w->d_slot_entity, w->slot_to_entity, st));
         RP_CUDA(upload(w->d_col_body, col_body, st));
+        std::vector<uint8_t> single(std::max<size_t>(N, 1), 0);
+        for (size_t slot = 0; slot < N; ++slot) {
+            const int32_t c = col_start[slot];
+            single[slot] = col_start[slot + 1] - c == 1 && cols[(size_t)c].type == COL_HULL &&
+                           shapes[(size_t)cols[(size_t)c].shape].nv <= 64;
+        }
+        RP_CUDA(upload(w->d_single_hull, single, st));
         RP_CUDA(w->d_pose_f.ensure(std::max<size_t>(N, 1) * 32));
         for (DevBuf* b : {&w->d_sdx, &w->d_sdq, &w->d_pred_d, &w->d_prev_qf}) {
             RP_CUDA(b->ensure(std::max<size_t>(N, 1) * 16));
@@ -718,6 +725,7 @@ WorldView<R> make_view(rp_world* w) {
     V.pred_d = w->d_pred_d.as<float4>();
     V.prev_qf = w->d_prev_qf.as<float4>();
     V.col_body = w->d_col_body.as<int32_t>();
+    V.single_hull = w->d_single_hull.as<uint8_t>();
     V.work_list = w->d_work_list.as<int32_t>();
     V.work_state = w->d_work_state.as<int32_t>();
     V.gjk_list = w->d_gjk_list.as<int32_t>();
@@ -1836,7 +1844,7 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
     int best[4] = {RP_MODE_PHASED, 8, cta0, 512};
     float best_ms = 0.f;
     // each candidate timed twice (the faster run counts); a later candidate replaces the best only
-    // when it is at least 3 % faster, so timing noise does not move the choice off the default
+    // when it is at least 1 % faster, so timing noise does not move the choice off the default
     auto consider = [&](int mode, int group, int cta, int solo) -> rp_status {
         set_tune(mode, group, cta, solo);
         float ms = 0.f, ms2 = 0.f;
@@ -1844,7 +1852,7 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
         if (r == RP_OK) r = trial(ms2);
         if (r != RP_OK) return r;
         ms = std::min(ms, ms2);
-        if (best_ms == 0.f || ms < 0.97f * best_ms) {
+        if (best_ms == 0.f || ms < 0.99f * best_ms) {
             best_ms = ms;
             best[0] = mode; best[1] = group; best[2] = cta; best[3] = solo;
         }

@@ -109,6 +109,31 @@ __device__ __forceinline__ void warp_argmin_first(T& v, int& idx) {
         if (ov < v || (ov == v && oi < idx)) { v = ov; idx = oi; }
     }
 }
+// FP32 specialisations on the warp-reduce unit: the value as an order-preserving unsigned key
+// (-0 folded onto +0, so equal floats give equal keys), one reduction for the extreme key, one for the
+// smallest index among the lanes that hold it: the same "first index wins" result as the shuffle
+// rounds above, in two instructions. (Lane values are never NaN: every caller starts from +-FLT_MAX
+// and keeps a value only through a strict comparison.)
+__device__ __forceinline__ unsigned f32_order_key(float f) {
+    const unsigned b = __float_as_uint(f + 0.0f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float f32_from_order_key(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ void warp_argmax_first(float& v, int& idx) {
+    const unsigned k = f32_order_key(v);
+    const unsigned m = __reduce_max_sync(0xffffffffu, k);
+    idx = (int)__reduce_min_sync(0xffffffffu, k == m ? (unsigned)idx : 0xffffffffu);
+    v = f32_from_order_key(m);
+}
+__device__ __forceinline__ void warp_argmin_first(float& v, int& idx) {
+    const unsigned k = f32_order_key(v);
+    const unsigned m = __reduce_min_sync(0xffffffffu, k);
+    idx = (int)__reduce_min_sync(0xffffffffu, k == m ? (unsigned)idx : 0xffffffffu);
+    v = f32_from_order_key(m);
+}
+
 __device__ __forceinline__ int warp_incl_scan(int x) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -188,12 +213,17 @@ __device__ __forceinline__ V3<R> support_mink(const ColView<R>& a, const ColView
         R dot = vdot(cv_vertex(b, i), nd);
         if (dot > bb) { bb = dot; ib = i; }
     }
+    if constexpr (sizeof(R) == 4) {
+        warp_argmax_first(ba, ia);
+        warp_argmax_first(bb, ib);
+    } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        R ova = __shfl_xor_sync(0xffffffffu, ba, o), ovb = __shfl_xor_sync(0xffffffffu, bb, o);
-        int oia = __shfl_xor_sync(0xffffffffu, ia, o), oib = __shfl_xor_sync(0xffffffffu, ib, o);
-        if (ova > ba || (ova == ba && oia < ia)) { ba = ova; ia = oia; }
-        if (ovb > bb || (ovb == bb && oib < ib)) { bb = ovb; ib = oib; }
+        for (int o = 16; o > 0; o >>= 1) {
+            R ova = __shfl_xor_sync(0xffffffffu, ba, o), ovb = __shfl_xor_sync(0xffffffffu, bb, o);
+            int oia = __shfl_xor_sync(0xffffffffu, ia, o), oib = __shfl_xor_sync(0xffffffffu, ib, o);
+            if (ova > ba || (ova == ba && oia < ia)) { ba = ova; ia = oia; }
+            if (ovb > bb || (ovb == bb && oib < ib)) { bb = ovb; ib = oib; }
+        }
     }
     if (ia == 0x7fffffff) ia = 0;
     if (ib == 0x7fffffff) ib = 0;

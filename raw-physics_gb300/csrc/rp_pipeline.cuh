@@ -84,11 +84,8 @@ __device__ void single_views(const WorldView<R>& W, V3<R>* stage_a, V3<R>* stage
 // True when both bodies have exactly one collider, a hull whose vertices fit the staging area.
 template <typename R>
 __device__ __forceinline__ bool single_hulls(const WorldView<R>& W, int a, int b) {
-    const int ca = W.col_start[a], cb = W.col_start[b];
-    if (W.col_start[a + 1] - ca != 1 || W.col_start[b + 1] - cb != 1) return false;
-    const Collider A = W.colliders[ca], B = W.colliders[cb];
-    if (A.type != COL_HULL || B.type != COL_HULL) return false;
-    return W.shapes[A.shape].nv <= STAGE_V && W.shapes[B.shape].nv <= STAGE_V;
+    static_assert(STAGE_V == 64, "single_hull flags are built for hulls of at most 64 vertices");
+    return W.single_hull[a] && W.single_hull[b];
 }
 
 // Copies the warp's contacts of global pair slot gp into the scene's contact buffer.

@@ -187,6 +187,8 @@ struct WorldView {
     float4* pred_d;              // [N] FP32 build: (float)(predicted position - previous position)
     float4* prev_qf;             // [N]             (float) previous orientation
     const int32_t* col_body;     // [colliders] body of each collider
+    const uint8_t* single_hull;  // [bodies] 1: the body's only collider is a hull of at most 64 vertices
+                                 //     (the narrowphase warp kernels' case)
     int32_t* work_list;          // [pair capacity] global pair slots narrowphased this frame
     int32_t* work_state;         // [pair capacity] per work item: WS_* below
     int32_t* gjk_list;           // [pair capacity] work items needing GJK this substep (queue[2] of them)
