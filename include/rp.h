@@ -125,6 +125,11 @@ rp_status rp_world_set_mode(rp_world* w, int32_t mode);
  * then also picks the colouring's priority scheme. No counterpart in the reference. */
 enum { RP_SWEEP_REFERENCE = 0, RP_SWEEP_COLOURED = 1 };
 rp_status rp_world_set_sweep_order(rp_world* w, int32_t order);
+/* How a batch's sweeps spread scenes over the GPU (a launch shape: results do not depend on it):
+ * 0 one warp per scene (the default), 1 one CTA per scene, n >= 2 a whole CTA for every scene whose
+ * sweep cost (dynamic bodies + 8 per joint) is n or more and one warp for each other scene.
+ * rp_autotune chooses among these (its choice[2]). No counterpart in the reference. */
+rp_status rp_world_set_sweep_assignment(rp_world* w, int32_t cta);
 /* Bound of every device-side wait of this world (the grid barriers of a single large scene's
  * cooperative kernels), in microseconds; 1 s by default, at most 60 s; 0 gives up at the first wait
  * that finds its barrier incomplete. A wait that runs out abandons the frame: every CTA leaves the

@@ -164,7 +164,7 @@ struct rp_world {
     DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist, d_single_hull;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
-    int cta_from = 256;               // tunable: batched sweeps give a whole CTA to scenes of this cost or more
+    int cta_from = 0;                 // tunable: batched sweeps give a whole CTA to scenes of this cost or more (0: none)
     std::vector<int64_t> order_cost;  // sweep cost of the scenes in scene_order (decreasing)
     int cta_scenes = 0;               // how many leading scenes of scene_order that is
     uint64_t wait_ns = 1000000000ull; // bound of every device-side wait (rp_world_set_wait_limit)
@@ -2321,6 +2321,16 @@ rp_status rp_world_set_sweep_order(rp_world* w, int32_t order) {
     if (order != RP_SWEEP_REFERENCE && order != RP_SWEEP_COLOURED) return fail(RP_ERR_INVALID, "bad sweep order");
     w->sweep_order = order;
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }   // the order is a kernel argument
+    return RP_OK;
+}
+
+rp_status rp_world_set_sweep_assignment(rp_world* w, int32_t cta) {
+    if (check_world(w)) return RP_ERR_INVALID;
+    if (cta < 0) return fail(RP_ERR_INVALID, "bad sweep assignment");
+    w->pipe.sweep_cta = cta == 1 ? 1 : 0;
+    w->cta_from = cta == 1 ? 0 : cta;
+    set_cta_scenes(w);
+    w->layout_gen++;   // recapture the frame graph with the new launch shapes
     return RP_OK;
 }
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "rp_world_set_mode": (_i, [_W, _i]),
     "rp_world_set_wait_limit": (_i, [_W, _u64]),
     "rp_world_set_sweep_order": (_i, [_W, _i]),
+    "rp_world_set_sweep_assignment": (_i, [_W, _i]),
     "rp_transformed_hulls_size": (_i, [_W, _P(_u64), _P(_u64)]),
     "rp_transformed_hulls": (_i, [_W, _P(_d), _P(_d)]),
     "rp_last_schedule": (_i, [_W, _i, _i, _P(_i), _P(_i), _u, _P(_u)]),
@@ -461,6 +462,11 @@ class World:
         """Gauss-Seidel order of the sweeps: "reference" (the reference's serial order, the default)
         or "coloured" (graph-coloured; results differ from the reference's by the reordering)."""
         self._check(self.lib.rp_world_set_sweep_order(self.h, self.SWEEP_ORDERS[order]))
+
+    def set_sweep_assignment(self, cta: int):
+        """Scenes per warp or CTA in a batch's sweeps: 0 one warp per scene (default), 1 one CTA per
+        scene, n >= 2 a CTA for scenes of sweep cost n or more (a launch shape; same results)."""
+        self._check(self.lib.rp_world_set_sweep_assignment(self.h, int(cta)))
 
     def set_wait_limit(self, microseconds: int):
         """Bound of every device-side wait (grid barriers); a wait that runs out undoes the call and

@@ -307,6 +307,30 @@ def test_batched_form_matches_oracle_per_scene(ext_built, oracle_built):
         assert np.array_equal(got["phased"][idx], o.get_state()), "scene %d" % s
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batched_sweep_assignments_agree(ext_built, precision):
+    """The batched sweeps' scene assignment is a launch shape only: one warp per scene, one CTA per
+    scene and the hybrid (a CTA for the costlier scenes) give identical states, in both builds."""
+    from rawphys import scenes as S
+    batch = S.batched_scenes(24, seed=7, min_bodies=2, max_bodies=60, chain_fraction=0.5, chain_links=(8, 16))
+    got = {}
+    for cta in (0, 1, 24):
+        w = ext_built.World(0, precision)
+        w.set_sweep_assignment(cta)
+        first = w.load_batch(batch)
+        w.simulate(batch.dt, batch.substeps, batch.pos_iters, batch.collisions, 6)
+        got[cta] = w.get_state()[first:]
+        assert (w.status() & ~(1 << 8)) == 0
+        w.close()
+    assert np.array_equal(got[0], got[1]) and np.array_equal(got[0], got[24])
+    with pytest.raises(ext_built.RPError):
+        w = ext_built.World(0, precision)
+        try:
+            w.set_sweep_assignment(-1)
+        finally:
+            w.close()
+
+
 def test_batched_form_fp32_per_step_error(ext_built, oracle_built):
     """FP32 batched form: per-step position error from identical states against the oracle, per
     scene of a mixed batch (contacts and joints)."""
