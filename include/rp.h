@@ -125,7 +125,8 @@ rp_status rp_world_set_mode(rp_world* w, int32_t mode);
  * then also picks the colouring's priority scheme. No counterpart in the reference. */
 enum { RP_SWEEP_REFERENCE = 0, RP_SWEEP_COLOURED = 1 };
 rp_status rp_world_set_sweep_order(rp_world* w, int32_t order);
-/* How a batch's sweeps spread scenes over the GPU (a launch shape: results do not depend on it):
+/* How a batch's sweeps spread scenes over the GPU (a launch shape: the same schedule under every
+ * choice, so FP64 results are identical and FP32 results agree to rounding):
  * 0 one warp per scene (the default), 1 one CTA per scene, n >= 2 a whole CTA for every scene whose
  * sweep cost (dynamic bodies + 8 per joint) is n or more and one warp for each other scene.
  * rp_autotune chooses among these (its choice[2]). No counterpart in the reference. */
@@ -141,7 +142,10 @@ rp_status rp_world_set_wait_limit(rp_world* w, uint64_t microseconds);
  * from their current state under each candidate launch configuration — launch mode, threads per
  * collider in the hull transform (4/8/16/32), and the sweep layout (levels swept by one CTA below
  * 128..2048 nodes for one large scene; for a batch, which scenes a warp and which a whole CTA sweeps) —
- * keeps the fastest, and restores the state. Every configuration gives identical results. Call it with
+ * keeps the fastest, and restores the state. Every configuration runs the same schedule: results are
+ * identical in RP_PRECISION_FP64 and agree to rounding in RP_PRECISION_FP32 (each kernel instantiation
+ * may contract multiply-adds differently). Each candidate is timed twice; one replaces the default only
+ * when at least 1 % faster. Call it with
  * no forces pending. choice receives {mode, transform threads, batch sweep assignment (0: a warp per
  * scene, 1: a CTA per scene, n >= 2: a CTA for scenes of n or more bodies plus 8 per joint, a warp for
  * the rest), solo level size}. */

@@ -465,7 +465,8 @@ class World:
 
     def set_sweep_assignment(self, cta: int):
         """Scenes per warp or CTA in a batch's sweeps: 0 one warp per scene (default), 1 one CTA per
-        scene, n >= 2 a CTA for scenes of sweep cost n or more (a launch shape; same results)."""
+        scene, n >= 2 a CTA for scenes of sweep cost n or more (a launch shape: FP64 results identical,
+        FP32 equal to rounding)."""
         self._check(self.lib.rp_world_set_sweep_assignment(self.h, int(cta)))
 
     def set_wait_limit(self, microseconds: int):
@@ -474,8 +475,8 @@ class World:
         self._check(self.lib.rp_world_set_wait_limit(self.h, int(microseconds)))
 
     def autotune(self, frames: int = 3) -> dict:
-        """Pick the fastest launch configuration for the loaded scenes (results are identical under
-        every configuration); returns the choice."""
+        """Pick the fastest launch configuration for the loaded scenes (the same schedule under every
+        configuration: FP64 results identical, FP32 equal to rounding); returns the choice."""
         s = self.scene
         out = (_i * 4)()
         self._check(self.lib.rp_autotune(self.h, float(s.dt), int(s.substeps), int(s.pos_iters), int(bool(s.collisions)),
