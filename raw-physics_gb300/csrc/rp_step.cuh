@@ -423,25 +423,41 @@ __device__ void broad_phase(const WorldView<R>& W, const G& g, int s, int* smem)
     if constexpr (std::is_same<G, GridGroup>::value) {
         if (n >= SORTED_BROAD_MIN && n <= SORTED_BROAD_MAX) { broad_phase_sorted(W, g, s, smem); return; }
     }
+    // A CTA stages the scene's FP32 bounds (position, radius + 0.05) in shared memory once, so the
+    // FP32 rejection of each of the n(n-1)/2 pairs reads them instead of converting two FP64 poses
+    // (FP64 conversions issue at a small fraction of the FP32 rate on GB300); only pairs the
+    // rejection keeps load the FP64 poses for the exact test. Same tests, same pairs, same order.
+    constexpr int BROAD_STAGE = 1024;
+    float4* sf = nullptr;
+    if constexpr (std::is_same<G, CtaGroup>::value) {
+        __shared__ float4 s_bounds[BROAD_STAGE];
+        if (n <= BROAD_STAGE) {
+            for (int i = g.rank(); i < n; i += g.size()) {
+                const double4_32a p = W.pos[b0 + i];
+                s_bounds[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)W.radius[b0 + i] + 0.05f);
+            }
+            sf = s_bounds;
+            g.sync();
+        }
+    }
+    auto bound = [&](int i) {
+        if (sf) return sf[i];
+        const double4_32a p = W.pos[b0 + i];
+        return make_float4((float)p.x, (float)p.y, (float)p.z, (float)W.radius[b0 + i] + 0.05f);
+    };
     const int pcap = W.scene_pair_cap[s + 1] - W.scene_pair_cap[s];
     int2* pairs = W.pairs + W.scene_pair_cap[s];
     const int lane = threadIdx.x & 31;
     const int gw = g.rank() >> 5, nw = g.size() >> 5;
     // per-row counts (warp per row)
     for (int i = gw; i < n; i += nw) {
-        double4_32a pi = W.pos[b0 + i];
-        double ri = W.radius[b0 + i];
-        float4 fi = make_float4((float)pi.x, (float)pi.y, (float)pi.z, (float)ri + 0.05f);
+        const float4 fi = bound(i);
         int cnt = 0;
         for (int jb = i + 1; jb < n; jb += 32) {
             int j = jb + lane;
             bool hit = false;
-            if (j < n) {
-                double4_32a pj = W.pos[b0 + j];
-                double rj = W.radius[b0 + j];
-                float4 fj = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)rj + 0.05f);
-                hit = !broad_reject(fi, fj) && broad_exact(pi, pj, ri, rj);
-            }
+            if (j < n && !broad_reject(fi, bound(j)))
+                hit = broad_exact(W.pos[b0 + i], W.pos[b0 + j], W.radius[b0 + i], W.radius[b0 + j]);
             cnt += __popc(__ballot_sync(0xffffffffu, hit));
         }
         if (lane == 0) W.row_count[b0 + i] = cnt;
@@ -456,19 +472,13 @@ __device__ void broad_phase(const WorldView<R>& W, const G& g, int s, int* smem)
         if (g.rank() == 0) atomicOr(&W.status[s], (uint32_t)ST_PAIR_OVERFLOW);
     }
     for (int i = gw; i < n; i += nw) {
-        double4_32a pi = W.pos[b0 + i];
-        double ri = W.radius[b0 + i];
-        float4 fi = make_float4((float)pi.x, (float)pi.y, (float)pi.z, (float)ri + 0.05f);
+        const float4 fi = bound(i);
         int out = W.row_count[b0 + i];
         for (int jb = i + 1; jb < n; jb += 32) {
             int j = jb + lane;
             bool hit = false;
-            if (j < n) {
-                double4_32a pj = W.pos[b0 + j];
-                double rj = W.radius[b0 + j];
-                float4 fj = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)rj + 0.05f);
-                hit = !broad_reject(fi, fj) && broad_exact(pi, pj, ri, rj);
-            }
+            if (j < n && !broad_reject(fi, bound(j)))
+                hit = broad_exact(W.pos[b0 + i], W.pos[b0 + j], W.radius[b0 + i], W.radius[b0 + j]);
             unsigned m = __ballot_sync(0xffffffffu, hit);
             int pos = out + __popc(m & ((1u << lane) - 1u));
             if (hit && pos < pcap) pairs[pos] = make_int2(b0 + i, b0 + j);
