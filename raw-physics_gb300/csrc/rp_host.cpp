@@ -161,7 +161,7 @@ struct rp_world {
     DevBuf d_rec, d_slot_entity;                   // the records on the device; entity of each body slot
     cudaEvent_t ev_rec = nullptr;                  // the last record upload (h_rec is refilled after it)
     double adj_prof[6] = {0, 0, 0, 0, 0, 0};      // last adjoint's slowest scene (rp_adjoint_profile)
-    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist, d_single_hull;
+    DevBuf d_pose_f, d_body_scene, d_col_body, d_scene_order, d_gjk_list, d_hit_list, d_work_list, d_work_state, d_work_simplex, d_work_epa, d_queue, d_work_off, d_work_face, d_fallback, d_tstamp, d_tlist, d_single_hull, d_pair_base, d_ext_base;
     int mode = RP_MODE_AUTO;          // RP_MODE_*: how a frame is launched
     int solo_nodes = 512;             // tunable: grid sweeps run levels up to this size on one CTA
     int cta_from = 0;                 // tunable: batched sweeps give a whole CTA to scenes of this cost or more (0: none)
@@ -576,6 +576,8 @@ rp_status build_device(rp_world* w) {
         RP_CUDA(w->d_work_simplex.ensure(std::max<size_t>(P, 1) * 16 * R));
         RP_CUDA(w->d_work_epa.ensure(std::max<size_t>(P, 1) * 4 * 8));
         RP_CUDA(w->d_work_off.ensure(std::max<size_t>(P, 1) * 16));
+        RP_CUDA(w->d_pair_base.ensure(std::max<size_t>(P, 1) * 16));
+        RP_CUDA(w->d_ext_base.ensure(std::max<size_t>(E, 1) * 16));
         RP_CUDA(w->d_fallback.ensure(std::max<size_t>(P, 1) * 4));
         RP_CUDA(w->d_work_face.ensure(std::max<size_t>(P, 1) * 12 * 4));
         std::vector<int32_t> order((size_t)S);
@@ -733,6 +735,8 @@ WorldView<R> make_view(rp_world* w) {
     V.work_simplex = w->d_work_simplex.as<R>();
     V.work_epa = w->d_work_epa.as<double>();
     V.work_off = w->d_work_off.as<float4>();
+    V.pair_base = w->d_pair_base.as<float4>();
+    V.ext_base = w->d_ext_base.as<float4>();
     V.fallback_list = w->d_fallback.as<int32_t>();
     V.work_face = w->d_work_face.as<float>();
     V.queue = w->d_queue.as<int32_t>();

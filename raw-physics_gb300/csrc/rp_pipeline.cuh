@@ -251,6 +251,14 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
     if (frame_abandoned(W.status)) return;
     __shared__ int scan_smem[32];
     __shared__ int base_smem;
+    if constexpr (!std::is_same<R, double>::value) {   // the joints' FP32 solve frames of this substep
+        const int ne = W.scene_ext[W.num_scenes];
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+            const ExtConstraint& C = W.ext[e];
+            const double4_32a pa = W.pos[C.e1], pb = W.pos[C.e2];
+            W.ext_base[e] = make_float4((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z), 0.f);
+        }
+    }
     const int n = W.queue[0];
     unsigned long long apart = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -268,10 +276,12 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_cull(WorldView<R> W, int enabled
                 else if (bounds_apart_f(W, a, b)) ++apart;
                 else gjk = true;
             }
-            if (gjk && !std::is_same<R, double>::value) {
-                // the pair frame's offset for the warp kernels: one FP64 difference per pair here
+            if ((gjk || state == WS_GENERAL) && !std::is_same<R, double>::value) {
+                // one FP64 difference per pair and substep: the pair frame's offset for the warp kernels
+                // and the FP32 sweeps' solve frame of the pair
                 const double4_32a pa = W.pos[a], pb = W.pos[b];
-                W.work_off[k] = make_float4((float)(pb.x - pa.x), (float)(pb.y - pa.y), (float)(pb.z - pa.z), 0.f);
+                if (gjk) W.work_off[k] = make_float4((float)(pb.x - pa.x), (float)(pb.y - pa.y), (float)(pb.z - pa.z), 0.f);
+                W.pair_base[gp] = make_float4((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z), 0.f);
             }
             W.work_state[k] = state;
             if (state == WS_NONE && !gjk) { W.pair_ccount[gp] = 0; W.pair_cstart[gp] = 0; }

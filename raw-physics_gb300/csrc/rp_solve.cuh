@@ -424,6 +424,12 @@ __device__ __forceinline__ void store_fbody(const WorldView<float>& W, const FBo
     W.sdq[B.idx] = make_float4(B.dq.x, B.dq.y, B.dq.z, B.dq.w);
 }
 
+// (float)(x_a - x_b) of two bodies' predicted positions, as stored in pair_base / ext_base
+__device__ __forceinline__ float4 fbase4(const WorldView<float>& W, int a, int b) {
+    const double4_32a pa = W.pos[a], pb = W.pos[b];
+    return make_float4((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z), 0.f);
+}
+
 // (float)(x_a - x_b) of the two bodies' predicted positions: the FP32 offset a node solves around
 __device__ __forceinline__ V3<float> fbase(const WorldView<float>& W, int a, int b) {
     const double4_32a pa = W.pos[a], pb = W.pos[b];
@@ -598,14 +604,14 @@ __device__ __forceinline__ Qt<double> fq64(const WorldView<float>& W, const FBod
 }
 
 // angular correction of one joint limit (limit_angle's dq, FP64) on the deltas
-__device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64, float h, double* lam) {
+__device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64, float h, float* lam) {
     const V3<float> dq = v3cast<float>(dq64);
     V3<float> n;
     const float th = funit(dq, n);
     if (th <= 0.f) return;
-    const float dl = fdlambda(th, vdot(n, fIinv(a, n)), vdot(n, fIinv(b, n)), h, 0.f, (float)*lam);
+    const float dl = fdlambda(th, vdot(n, fIinv(a, n)), vdot(n, fIinv(b, n)), h, 0.f, *lam);
     fang_apply(a, b, dl, dq);
-    *lam += (double)dl;
+    *lam += dl;
 }
 
 // FP64 evaluation of a joint limit that the FP32 screen could not rule out (rare): kind 0 the hinge
@@ -613,7 +619,7 @@ __device__ __forceinline__ void flimit_apply(FBody& a, FBody& b, V3<double> dq64
 // each from the FP64 orientations q0 + dq, applying its correction to a and b. Out of line, so that
 // the joint solve's common path keeps its values in registers.
 static __device__ __noinline__ void flimit64(const WorldView<float>& W, FBody& a, FBody& b, const ExtConstraint& C, float h,
-                                             double* lam, int kind) {
+                                             float* lam, int kind) {
     const double EPS64 = 1e-50;
     const Qt<double> qa = fq64(W, a), qb = fq64(W, b);
     V3<double> dq64;
@@ -642,11 +648,14 @@ static __device__ __noinline__ void flimit64(const WorldView<float>& W, FBody& a
     }
 }
 
-static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint& C, double* lam, float h) {
+// lam: the joint's Lagrange multipliers of the substep as FP32 (they start at zero every substep and
+// enter only through compliance, zero for the joints of the workloads); base: (float)(x_e1 - x_e2)
+// of the predicted positions, rounded once per substep by the cull.
+static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint& C, float4 base, float* lam, float h) {
     FBody a = load_fbody(W, C.e1), b = load_fbody(W, C.e2);
     const V3<float> r1 = v3<float>(C.r1f[0], C.r1f[1], C.r1f[2]);
     const V3<float> r2 = v3<float>(C.r2f[0], C.r2f[1], C.r2f[2]);
-    const V3<float> base_ab = fbase(W, C.e1, C.e2);
+    const V3<float> base_ab = v3<float>(base.x, base.y, base.z);
     auto anchor = [&](const FPcpd& p) { return vadd(vadd(base_ab, vsub(a.dx, b.dx)), vsub(p.r1, p.r2)); };
     switch (C.type) {
     case CON_POSITIONAL: {  // pbd.cpp:81-97
@@ -655,27 +664,27 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
                                          (float)((pa.z - pb.z) - C.distance[2]));
         const V3<float> dx = vadd(base, vsub(a.dx, b.dx));
         const FPcpd p = fpcpd(a, b, r1, r2);
-        const float dl = fpos_dlambda_c(a, b, p, h, C.compliance_f, (float)lam[0], dx);
+        const float dl = fpos_dlambda_c(a, b, p, h, C.compliance_f, lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
-        lam[0] += (double)dl;
+        lam[0] += dl;
     } break;
     case CON_MUTUAL_ORIENTATION: {  // pbd.cpp:156-173
         const Qt<float> aux = qmul(a.q(), qinverse(b.q()));
         const V3<float> dq = v3<float>(2.f * aux.x, 2.f * aux.y, 2.f * aux.z);
-        const float dl = fang_dlambda(a, b, h, C.compliance_f, (float)lam[0], dq);
+        const float dl = fang_dlambda(a, b, h, C.compliance_f, lam[0], dq);
         fang_apply(a, b, dl, dq);
-        lam[0] += (double)dl;
+        lam[0] += dl;
     } break;
     case CON_HINGE: {  // pbd.cpp:245-299
         const V3<float> dq = vcross(qaxis(a.q(), C.a1), qaxis(b.q(), C.a2));
-        float dl = fang_dlambda(a, b, h, C.compliance_f, (float)lam[1], dq);
+        float dl = fang_dlambda(a, b, h, C.compliance_f, lam[1], dq);
         fang_apply(a, b, dl, dq);
-        lam[1] += (double)dl;
+        lam[1] += dl;
         const FPcpd p = fpcpd(a, b, r1, r2);
         const V3<float> dx = anchor(p);
-        dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
+        dl = fpos_dlambda_c(a, b, p, h, 0.f, lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
-        lam[0] += (double)dl;
+        lam[0] += dl;
         if (C.limited && limit_may_act(qaxis(a.q(), C.a1), qaxis(a.q(), C.l1), qaxis(b.q(), C.l2), C.lo, C.hi)) {
             flimit64(W, a, b, C, h, lam, 0);
         }
@@ -683,9 +692,9 @@ static __device__ void fext_solve(const WorldView<float>& W, const ExtConstraint
     case CON_SPHERICAL: {  // pbd.cpp:301-379
         const FPcpd p = fpcpd(a, b, r1, r2);
         const V3<float> dx = anchor(p);
-        const float dl = fpos_dlambda_c(a, b, p, h, 0.f, (float)lam[0], dx);
+        const float dl = fpos_dlambda_c(a, b, p, h, 0.f, lam[0], dx);
         fpos_apply(a, b, p, dl, dx);
-        lam[0] += (double)dl;
+        lam[0] += dl;
         {   // swing
             const V3<float> f1 = qaxis(a.q(), C.a1), f2 = qaxis(b.q(), C.a2), fn = vcross(f1, f2);
             const float fl = vlen(fn);

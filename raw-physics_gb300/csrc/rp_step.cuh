@@ -1147,7 +1147,7 @@ __device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
     const int e0 = W.scene_ext[s], ne = W.scene_ext[s + 1] - e0;
     if (k < ne) {
         if constexpr (EXACT) ext_solve<R, EXACT>(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
-        else fext_solve(W, W.ext[e0 + k], W.ext_lambda + 4 * (size_t)(e0 + k), h);
+        else fext_solve(W, W.ext[e0 + k], W.ext_base[e0 + k], reinterpret_cast<float*>(W.ext_lambda + 4 * (size_t)(e0 + k)), h);
         return;
     }
     const int p = W.scene_pair_cap[s] + (k - ne);
@@ -1163,7 +1163,8 @@ __device__ void solve_node(const WorldView<R>& W, int s, int k, R h) {
         store_pose(W, b);
     } else {
         FBody a = load_fbody(W, pr.x), b = load_fbody(W, pr.y);
-        const V3<float> base_ab = fbase(W, pr.x, pr.y);
+        const float4 bb = W.pair_base[p];
+        const V3<float> base_ab = v3<float>(bb.x, bb.y, bb.z);
         for (int i = 0; i < nc; ++i) fcollision_solve(W, a, b, base_ab, c + 12 * i, mus);
         store_fbody(W, a);
         store_fbody(W, b);
@@ -1324,6 +1325,16 @@ __device__ void step_scene(const WorldView<R>& W, const G& g, int s, const StepP
             for (int p = g.rank(); p < np; p += g.size()) W.pair_ccount[W.scene_pair_cap[s] + p] = 0;
         }
         g.sync();
+        if constexpr (!EXACT) {   // the FP32 sweeps' per-substep solve frames (the phased form's cull writes them)
+            const int np = min(W.pair_count[s], W.scene_pair_cap[s + 1] - W.scene_pair_cap[s]);
+            const int pb = W.scene_pair_cap[s];
+            for (int p = g.rank(); p < np; p += g.size()) {
+                const int2 pr = W.pairs[pb + p];
+                W.pair_base[pb + p] = fbase4(W, pr.x, pr.y);
+            }
+            for (int e = e0 + g.rank(); e < e1; e += g.size()) W.ext_base[e] = fbase4(W, W.ext[e].e1, W.ext[e].e2);
+            g.sync();
+        }
         mark(PH_NARROW);
         resched(W, g, s);
         mark(PH_SCHEDULE);

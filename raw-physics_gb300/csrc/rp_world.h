@@ -195,6 +195,9 @@ struct WorldView {
     int32_t* hit_list;           // [pair capacity] work items needing a manifold this substep (queue[3])
     R* work_simplex;             // [16 * pair capacity] GJK simplex of a hit (a, b, c, d)
     double* work_epa;            // [4 * pair capacity] EPA normal (FP64) and penetration of a hit
+    float4* pair_base;           // [pair capacity] FP32 build: (float)(x_a - x_b) of a pair slot's predicted
+                                 //     positions, rounded once per substep (the sweeps' solve frame)
+    float4* ext_base;            // [external constraints] the same for each joint's two bodies
     float4* work_off;            // [pair capacity] FP32 build: body b's origin relative to body a's (xyz; the
                                  //     FP64 difference rounded once per pair and substep by k_cull)
     int32_t* fallback_list;      // [pair capacity] FP32 build: work items whose FP32 EPA or edge contact met a
