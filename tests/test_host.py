@@ -128,6 +128,15 @@ def test_argument_validation(ext_built):
     with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
         w.set_state(np.full((1, rp.STATE_DOUBLES), np.inf))
     assert e == 0 and w.num_entities() == 1
+    # launch-shape and order settings: accepted values only, no device needed
+    for cta in (0, 1, 96):
+        w.set_sweep_assignment(cta)
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.set_sweep_assignment(-1)
+    w.set_sweep_order("coloured")
+    w.set_sweep_order("reference")
+    with pytest.raises(rp.RPError, match="RP_ERR_INVALID"):
+        w.set_wait_limit(61_000_000)                                              # above 60 s
     w.close()
 
 
