@@ -307,6 +307,30 @@ def test_batched_form_matches_oracle_per_scene(ext_built, oracle_built):
         assert np.array_equal(got["phased"][idx], o.get_state()), "scene %d" % s
 
 
+def test_fp32_persistent_and_phased_forms_agree(ext_built):
+    """The FP32 build in its two launch modes (one persistent kernel per frame; the phase-major
+    pipeline) runs the same substep: from the same state, one frame of a mixed batch (contacts,
+    hinge and spherical chains) agrees to rounding for most bodies (median <= 1e-6 m) and within the
+    FP32 build's per-step spread where a contact's sign test flips (<= 1e-2 m)."""
+    from rawphys import scenes as S
+    batch = S.batched_scenes(16, seed=11, min_bodies=2, max_bodies=48, chain_fraction=0.5, chain_links=(8, 12))
+    got, start = {}, None
+    for mode in ("phased", "persistent"):
+        w = ext_built.World(0, "fp32")
+        w.set_mode(mode)
+        first = w.load_batch(batch)
+        if start is None:
+            w.simulate(batch.dt, batch.substeps, batch.pos_iters, batch.collisions, 3)
+            start = w.get_state()
+        w.set_state(start)
+        w.simulate(batch.dt, batch.substeps, batch.pos_iters, batch.collisions, 1)
+        got[mode] = w.get_state()[first:]
+        assert (w.status() & ~(1 << 8)) == 0
+        w.close()
+    d = np.linalg.norm(got["phased"][:, 0:3] - got["persistent"][:, 0:3], axis=1)
+    assert np.median(d) <= 1e-6 and d.max() <= 1e-2, (np.median(d), d.max())
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_batched_sweep_assignments_agree(ext_built, precision):
     """The batched sweeps' scene assignment is a launch shape only: one warp per scene, one CTA per
