@@ -430,11 +430,6 @@ __device__ __forceinline__ float4 fbase4(const WorldView<float>& W, int a, int b
     return make_float4((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z), 0.f);
 }
 
-// (float)(x_a - x_b) of the two bodies' predicted positions: the FP32 offset a node solves around
-__device__ __forceinline__ V3<float> fbase(const WorldView<float>& W, int a, int b) {
-    const double4_32a pa = W.pos[a], pb = W.pos[b];
-    return v3<float>((float)(pa.x - pb.x), (float)(pa.y - pb.y), (float)(pa.z - pb.z));
-}
 
 // The position sweep's corrections into the FP64 pose (x += dx, q = normalize(q + dq)), and the
 // FP32 orientation copy the velocity sweep reads; bodies the sweep did not touch keep their pose.
