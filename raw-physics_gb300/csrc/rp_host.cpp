@@ -1845,7 +1845,7 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
         w->layout_gen++;   // recapture the frame graph with the new launch shapes
     };
     const int cta0 = w->pipe.sweep_cta ? 1 : w->cta_from;
-    int best[4] = {RP_MODE_PHASED, 8, cta0, 512};
+    int best[4] = {RP_MODE_PHASED, 4, cta0, 512};
     float best_ms = 0.f;
     // each candidate timed twice (the faster run counts); a later candidate replaces the best only
     // when it is at least 1 % faster, so timing noise does not move the choice off the default
@@ -1863,10 +1863,10 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
         return RP_OK;
     };
     // coordinate search: launch mode, then the hull-transform group, then the sweep layout
-    s = consider(RP_MODE_PHASED, 8, cta0, 512);
-    if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, cta0, 512);
+    s = consider(RP_MODE_PHASED, 4, cta0, 512);
+    if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 4, cta0, 512);
     if (s == RP_OK && best[0] == RP_MODE_PHASED) {
-        for (int g : {4, 16, 32})
+        for (int g : {8, 16, 32})
             if (s == RP_OK) s = consider(RP_MODE_PHASED, g, cta0, 512);
         const int g = best[1];
         if (w->grid_mode) {
@@ -1879,7 +1879,7 @@ rp_status rp_autotune(rp_world* w, double dt, uint32_t substeps, uint32_t iters,
         }
     } else if (s == RP_OK && w->grid_mode) {
         for (int solo : {128, 256, 1024, 2048})
-            if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 8, 0, solo);
+            if (s == RP_OK) s = consider(RP_MODE_PERSISTENT, 4, 0, solo);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

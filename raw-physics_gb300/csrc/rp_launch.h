@@ -12,7 +12,7 @@ struct PipeConfig {
     int cull_blocks = 0, gjk_blocks = 0, epa_blocks = 0, manifold_blocks = 0, general_blocks = 0;
     int setup_grid_blocks = 0, sweep_grid_blocks = 0, vsweep_grid_blocks = 0, sweep_warp_blocks = 0;
     // tunable (rp_autotune): the schedule does not depend on them (FP64 results identical, FP32 to rounding)
-    int transform_group = 8;     // threads per collider in the hull transform
+    int transform_group = 4;     // threads per collider in the hull transform
     int sweep_cta = 0;           // batched sweeps: one CTA per scene instead of one warp per scene
 };
 struct PipeDims {

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(PIPE_BLOCK) k_predict(WorldView<R> W, int nbod
 
 // The hulls of the bodies k_cull listed for this substep (tlist: bodies of the pairs that go on to
 // GJK or the general path; the narrowphase reads no other transformed hull), `group` threads per
-// collider (a power of two up to 32; 8 by default: the typical hull has 8-64 vertices, so a whole
+// collider (a power of two up to 32; 4 by default: the typical hull has 8-64 vertices, so a whole
 // warp per collider would leave most lanes idle).
 template <typename R, bool EXACT>
 __global__ void __launch_bounds__(PIPE_BLOCK) k_transform(WorldView<R> W, int group) {
