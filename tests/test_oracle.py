@@ -117,6 +117,32 @@ def test_port_matches_reference_live(oracle_built):
         assert np.array_equal(sa, b.get_state())
 
 
+def test_port_matches_reference_on_batched_scenes(oracle_built):
+    """The port is the oracle of the batched workload's per-step error (bench.py), so it is also
+    compared live with the reference on scenes of that generator: piles of the four hull shapes,
+    hinge chains with +-pi/2 limits and spherical chains, a size-stratified handful, 12 frames each,
+    bit for bit."""
+    from oracle.oracle import reference_available
+    from rawphys import scenes as S
+    if not reference_available():
+        pytest.skip("reference build not present (only where the reference checkout exists)")
+    batch = S.batched_scenes(48, seed=0, max_bodies=256)
+    sizes = np.bincount(batch.scene, minlength=batch.num_scenes)
+    first_chain = {}
+    for c in batch.constraints:
+        first_chain.setdefault(c.kind, int(batch.scene[c.e2]))
+    assert {"hinge", "spherical"} <= set(first_chain), first_chain
+    picks = sorted(set([int(np.argmax(sizes)), int(np.argmin(sizes)), first_chain["hinge"], first_chain["spherical"]] +
+                       [int(i) for i in np.argsort(sizes)[len(sizes) // 2:len(sizes) // 2 + 2]]))
+    for s_ in picks:
+        scene = S.batch_scene(batch, s_)
+        a = oracle_built("port").load(scene)
+        a.step(12)
+        b = oracle_built("reference").load(scene)
+        b.step(12)
+        assert np.array_equal(a.get_state(), b.get_state()), "scene %d (%d bodies)" % (s_, sizes[s_])
+
+
 def test_port_forces_and_edge_cases(oracle_built):
     """Extra forces (world and local frame), dt <= 0 no-op, collisions off: port == reference."""
     from oracle.oracle import reference_available
